@@ -1,0 +1,199 @@
+/* spac_fk.h -- C ABI of the GB300 Feynman-Kac solver (libspac_fk.so).
+ *
+ * The GPU replacement for SpAc's FeynmanKacSolver node and point solves and
+ * for the G/B scatter into SistemaLineal.  Plain C types only; every call
+ * returns an int status (FK_OK = 0, negative on error; the message is in
+ * fk_last_error).  No exception crosses the ABI and there is no CPU fallback:
+ * without a usable CUDA device fk_create fails with FK_ERR_NO_DEVICE.
+ *
+ * Conventions
+ *  - Coordinates, step sizes and outputs are double on the host side.
+ *  - Output pointers may be host or device memory (checked with
+ *    cudaPointerGetAttributes); device pointers are written in place on the
+ *    context's stream and the call returns after the stream has drained.
+ *  - Random numbers: counter-based Philox4x32-10.  Path p of item i in a call
+ *    with stream id s uses counter (step/2, p, i, s) and key (seed lo, seed hi);
+ *    the stream id advances by one after every solve call unless set with
+ *    fk_set_stream.  Results are therefore reproducible for a given seed and
+ *    call sequence, independent of the launch shape.
+ *  - Step loop: a path is stopped after max_steps steps (fk_set_max_steps,
+ *    default 2^24); such paths are counted in fk_stats.n_capped and make the
+ *    call return FK_ERR_STEP_CAP after all outputs are written.
+ */
+#ifndef SPAC_FK_H
+#define SPAC_FK_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FK_OK 0
+#define FK_ERR_ARG (-1)
+#define FK_ERR_CUDA (-2)
+#define FK_ERR_REGISTRY (-3)
+#define FK_ERR_STEP_CAP (-4)
+#define FK_ERR_NOT_FOUND (-5)
+#define FK_ERR_NO_DEVICE (-6)
+#define FK_ERR_CAPACITY (-7)
+
+/* BVP coefficient sets compiled as fused device functors.  Each is the GPU
+ * twin of a set of reference coefficient function pointers (BVP/BVP.hpp:17-28):
+ *  FK_PROBLEM_FRANKE   BVPs/Franke_Poisson.hpp:4-73 (u, g, c = 0, f = -Lap u,
+ *                      sigma = 1.41421356237 I, b = 0, F = -sigma^T grad u)
+ *  FK_PROBLEM_MONEGROS BVPs/Monegros_Revamped.hpp:4-75 (c = -1)
+ *  FK_PROBLEM_ANISO    sigma sigma^T = 2(1 + 0.5 sin 2pi x sin 2pi y) I,
+ *                      b = (y - 1/2, 1/2 - x), c = -(1 + x^2 + y^2),
+ *                      u = Franke (1 + x y), f = -(L u)
+ *  FK_PROBLEM_DISK     Franke rescaled to the disk (prob = cx, cy, R):
+ *                      u(x) = Franke((x - c)/(2R) + 1/2), sigma = 1.41421356237 I */
+enum { FK_PROBLEM_FRANKE = 0, FK_PROBLEM_MONEGROS = 1, FK_PROBLEM_ANISO = 2, FK_PROBLEM_DISK = 3 };
+/* Frontera distance functors: Dominios/Rectangulo.hpp:7-229 (x0,y0,x1,y1) and
+ * Dominios/Circulo.hpp:7-22 (r,cx,cy). */
+enum { FK_SHAPE_RECT = 0, FK_SHAPE_CIRCLE = 1 };
+/* Control variate term xi += Y F(X).dW (FeynmanKacSolver.cpp:14):
+ * none (F = 0, the reference default), exact (F = -sigma^T grad u), or a
+ * learned MLP (F = -sigma^T grad u_hat). */
+enum { FK_CV_NONE = 0, FK_CV_EXACT = 1, FK_CV_MLP = 2 };
+/* Arithmetic of the path stepping; per-node sums are FP64 in both. */
+enum { FK_FP64 = 0, FK_FP32 = 1 };
+
+typedef struct fk_ctx fk_ctx;
+
+typedef struct {
+  int problem;      /* FK_PROBLEM_* */
+  int cv;           /* FK_CV_* */
+  int dom_shape;    /* FK_SHAPE_* of frontera_dominio */
+  double dom[4];    /* its parameters */
+  double prob[4];   /* problem parameters (FK_PROBLEM_DISK: cx, cy, R) */
+  int mlp_id;       /* FK_CV_MLP: network from fk_mlp_create */
+} fk_bvp_desc;
+
+/* Per-solve statistics: the public members of FeynmanKacSolver after Update()
+ * (Solvers/FeynmanKacSolver.hpp:80-83, FeynmanKacSolver.cpp:294-323), with the
+ * reference's xi/xixi slot aliasing reproduced, followed by plain extras. */
+typedef struct {
+  double phi, phiphi, phi_VR, phiphi_VR, xi, xixi, xiphi, APL, RNGC;
+  double B;             /* node solves: averaged B (Update(Nudo&), :324-334) */
+  double n_paths;
+  double n_domain_exits;
+  double n_capped;
+  double xi_mean;       /* true E[xi] and E[xi^2] */
+  double xi_sq_mean;
+  double mean_steps;
+} fk_stats;
+
+/* Reference arc (Mesh/Interfaz.hpp:14-37): nodes on a circle arc with the
+ * inverse-multiquadric-in-theta RBF stencil (Interfaz.cpp:206-264). */
+typedef struct {
+  double cx, cy, radius, c2;
+  int interior;          /* arc code of Interfaz::Inicia_Cuadrado */
+  int n;                 /* nodes on the arc */
+  const double* theta;   /* n node angles (posicion_angular) */
+  const int* gids;       /* n global node ids (indice_global) */
+  const double* iPsi;    /* n*n column-major inverse of Psi, or NULL: computed
+                            on the GPU in FP64 (full-pivot Gauss-Jordan) */
+} fk_arc_desc;
+
+/* One node solve (Solve_OMP_Analytic(Nudo&, N, h, rho, BVP, Interfaz)). */
+typedef struct {
+  double x, y;           /* Nudo::posicion_cartesiana */
+  double h;              /* time step */
+  unsigned paths;        /* numero_trayectorias */
+  int frontera;          /* Nudo::frontera: B = g(x), no paths */
+  int row;               /* Nudo::indice_global (CSR row) */
+  int stencil;           /* arc id (fk_register_arc) */
+} fk_node_item;
+
+/* ---- context ------------------------------------------------------------ */
+int fk_create(fk_ctx** ctx, int device, unsigned long long seed);
+int fk_destroy(fk_ctx* ctx);
+const char* fk_last_error(const fk_ctx* ctx);
+int fk_set_stream(fk_ctx* ctx, unsigned stream_id);
+int fk_get_stream(const fk_ctx* ctx, unsigned* stream_id);
+int fk_set_max_steps(fk_ctx* ctx, int max_steps);
+/* Launch shape of the path kernel: threads per block and paths per work
+ * chunk (0 = autotuned / default). */
+int fk_set_launch(fk_ctx* ctx, int block_threads, int chunk_paths);
+/* cudaStream_t of the context, as void* */
+int fk_cuda_stream(const fk_ctx* ctx, void** stream);
+/* Device time (ms, CUDA events on the context stream) of the kernels of the
+ * last solve: [0] path kernel, [1] finalize/scatter kernel, [2] launches. */
+int fk_last_timing(const fk_ctx* ctx, double out[3]);
+
+/* ---- problem registry (BVP) ---------------------------------------------- */
+int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* desc, int* bvp_id);
+
+/* ---- point solves: Solve_OMP_Analytic(X0, N, h, rho, BVP)
+ *      (Solvers/FeynmanKacSolver.cpp:335-342), n points in one launch.
+ *      sub_shape/sub_params (4 per point) may be NULL: subdomain = domain. */
+int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsigned* paths,
+                    const double* h, const int* sub_shape, const double* sub_params,
+                    int precision, fk_stats* out);
+
+/* ---- node solves on reference arcs --------------------------------------- */
+int fk_register_arc(fk_ctx* ctx, const fk_arc_desc* arc, int* arc_id);
+/* the arc's iPsi as used by the kernels (n*n column-major) */
+int fk_arc_ipsi(fk_ctx* ctx, int arc_id, double* iPsi);
+/* Batched Solve_OMP_Analytic(Nudo&, ...) (FeynmanKacSolver.cpp:344-355):
+ * G receives, for item k, the arc's n averaged G entries at offset
+ * sum_{j<k} n(items[j].stencil); B[k] the averaged B; stats may be NULL. */
+int fk_solve_nodes_arc(fk_ctx* ctx, int bvp_id, int n_items, const fk_node_item* items,
+                       int precision, double* G, double* B, fk_stats* stats);
+
+/* ---- meshes and batched G/B assembly -------------------------------------- */
+/* Malla::Construye_Cuadrado (Mesh/Malla.cpp:12-83): circles on a grid, FK
+ * items for the interior nodes of perimeter circles (main_test_serial.cpp:54-62). */
+int fk_mesh_circles(fk_ctx* ctx, const double dom[4], int n_side, double superposicion,
+                    double theta0, int nodes_per_circle, double c2_corner, double c2_side,
+                    int* mesh_id);
+/* Square patches (no reference counterpart): n_sub x n_sub subdomains of
+ * [x0,x1]x[y0,y1], each enlarged by `enlarge` times its width on every side;
+ * nodes_per_side equispaced nodes on each patch side inside the domain; one FK
+ * item per (node, patch strictly containing it); exit values by a Gaussian
+ * RBF (phi = exp(-(eps r)^2), eps = eps_spacing / node spacing) on the `knn`
+ * nearest nodes of the exit patch's boundary. */
+int fk_mesh_square_patches(fk_ctx* ctx, const double dom[4], int n_sub, int nodes_per_side,
+                           double enlarge, double eps_spacing, int knn, int* mesh_id);
+typedef struct {
+  int n_rows, nnz, n_items, n_nodes, n_stencils, max_stencil;
+  double spacing;        /* square patches: node spacing along a side */
+} fk_mesh_info;
+int fk_mesh_get_info(fk_ctx* ctx, int mesh_id, fk_mesh_info* info);
+/* node table: xy[2*n_nodes]; flags[n_nodes] (bit0 = frontera) */
+int fk_mesh_nodes(fk_ctx* ctx, int mesh_id, double* xy, int* flags);
+/* items: row[n_items], xy[2*n_items], stencil[n_items], frontera[n_items] */
+int fk_mesh_items(fk_ctx* ctx, int mesh_id, int* row, double* xy, int* stencil, int* frontera);
+/* stencil s: node ids (global rows) of its nodes, count returned in *n */
+int fk_mesh_stencil_nodes(fk_ctx* ctx, int mesh_id, int s, int* gids, int* n);
+/* SistemaLineal::Inicializa_CSR (Mesh/SistemaLineal.cpp:39-66): sorted CSR
+ * pattern, diagonal = number of containing patches, placeholder 1e-23. */
+int fk_mesh_csr(fk_ctx* ctx, int mesh_id, int* rowptr, int* col, double* val0);
+/* Assemble: paths per item (or per-item array `paths_per_item` if non-NULL),
+ * time step h.  Writes val (CSR values = pattern + sum of item G rows, as
+ * SistemaLineal::Actualiza_GB, Mesh/SistemaLineal.cpp:68-88) and B; item_G /
+ * item_B / item_stats (optional, NULL to skip) receive per-item results. */
+int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsigned* paths_per_item,
+                double h, int precision, double* val, double* B, double* item_G, double* item_B,
+                fk_stats* item_stats);
+
+/* ---- learned control variate: MLP 2 -> W -> W -> W -> 1 (SiLU), BF16 weights,
+ *      FP32 master copy, trained by the library's own kernels ------------- */
+int fk_mlp_create(fk_ctx* ctx, int width, const double in_lo[2], const double in_scale[2],
+                  unsigned long long init_seed, int* mlp_id);
+/* parameters packed W1(Wx2),b1,W2(WxW),b2,W3(WxW),b3,W4(1xW),b4 (row-major, FP32 master) */
+int fk_mlp_num_params(fk_ctx* ctx, int mlp_id, int* n);
+int fk_mlp_get_params(fk_ctx* ctx, int mlp_id, float* params);
+int fk_mlp_set_params(fk_ctx* ctx, int mlp_id, const float* params);
+/* Adam training on (xy, target): steps, batch, learning rate; loss history
+ * (may be NULL, length steps). */
+int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, int steps,
+                 int batch, double lr, unsigned long long shuffle_seed, float* loss_history);
+/* forward + input gradient at n points: out[3*n] = (u_hat, du/dx, du/dy) */
+int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, double* out);
+/* loss and parameter gradient of mean((u_hat - target)^2) on a batch (FP32 grad) */
+int fk_mlp_loss_grad(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target,
+                     double* loss, float* grad);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -319,6 +319,15 @@ Coef coefficients(const orc_bvp* B, double x, double y) {
   return c;
 }
 
+// sigma alone (the same expressions as in coefficients())
+M2 sigma_of(const orc_bvp* B, double x, double y) {
+  if (B->problem == ORC_PROBLEM_ANISO) {
+    double s = std::sqrt(2.0 * aniso_a(x, y));
+    return M2{1.0 * s, 0.0 * s, 0.0 * s, 1.0 * s};
+  }
+  return M2{1.41421356237, 0.0, 0.0, 1.41421356237};
+}
+
 // ------------------------------------------------------------ exit rule -----
 // Dentro (FeynmanKacSolver.cpp:68-106) for absorbing boundaries: the boundary
 // with the larger signed distance wins (tie -> domain); the path stops once
@@ -331,10 +340,10 @@ int dentro(const orc_bvp* B, int sub_shape, const double* sub, V2 X, double sqrt
     d = da;
     proj = pa;
     N = na;
-    M2 s = (d < 0.0) ? coefficients(B, X.x, X.y).s : coefficients(B, proj.x, proj.y).s;
+    M2 s = (d < 0.0) ? sigma_of(B, X.x, X.y) : sigma_of(B, proj.x, proj.y);
     return (d < kGobet * norm(tmul(N, s)) * sqrth) ? ORC_OUT_INSIDE : ORC_OUT_DOMAIN;
   }
-  M2 s = (d < 0.0) ? coefficients(B, X.x, X.y).s : coefficients(B, proj.x, proj.y).s;
+  M2 s = (d < 0.0) ? sigma_of(B, X.x, X.y) : sigma_of(B, proj.x, proj.y);
   return (d < kGobet * norm(tmul(N, s)) * sqrth) ? ORC_OUT_INSIDE : ORC_OUT_SUBDOMAIN;
 }
 
@@ -620,7 +629,11 @@ int orc_node_solve_arc(void* s, const orc_bvp* b, double x, double y, int fronte
   return 0;
 }
 
-int orc_knn_weights(const orc_knn* st, double x, double y, int* idx, double* w) {
+}  // extern "C"
+
+namespace {
+// k nearest patch-boundary nodes of (x, y), ascending local index
+void knn_select(const orc_knn* st, double x, double y, int* idx) {
   int m = st->m, k = st->k;
   std::vector<std::pair<double, int>> d(m);
   for (int a = 0; a < m; ++a) {
@@ -630,6 +643,10 @@ int orc_knn_weights(const orc_knn* st, double x, double y, int* idx, double* w) 
   std::partial_sort(d.begin(), d.begin() + k, d.end());
   for (int a = 0; a < k; ++a) idx[a] = d[a].second;
   std::sort(idx, idx + k);
+}
+// inverse of A_W(a,b) = exp(-eps^2 |x_a - x_b|^2) for the window idx
+std::vector<double> knn_inverse(const orc_knn* st, const int* idx) {
+  int k = st->k;
   double e2 = st->eps * st->eps;
   std::vector<double> A(static_cast<size_t>(k) * k), inv;
   for (int j = 0; j < k; ++j)
@@ -638,6 +655,12 @@ int orc_knn_weights(const orc_knn* st, double x, double y, int* idx, double* w) 
       A[i + j * k] = std::exp(-e2 * (dx * dx + dy * dy));
     }
   gj_inverse(k, A, inv);
+  return inv;
+}
+// w = A_W^{-1} phi_W(x)
+void knn_apply(const orc_knn* st, const int* idx, const std::vector<double>& inv, double x, double y, double* w) {
+  int k = st->k;
+  double e2 = st->eps * st->eps;
   std::vector<double> phi(k);
   for (int a = 0; a < k; ++a) {
     double dx = x - st->xy[2 * idx[a]], dy = y - st->xy[2 * idx[a] + 1];
@@ -648,6 +671,14 @@ int orc_knn_weights(const orc_knn* st, double x, double y, int* idx, double* w) 
     for (int c = 0; c < k; ++c) s += inv[a + c * k] * phi[c];
     w[a] = s;
   }
+}
+}  // namespace
+
+extern "C" {
+
+int orc_knn_weights(const orc_knn* st, double x, double y, int* idx, double* w) {
+  knn_select(st, x, y, idx);
+  knn_apply(st, idx, knn_inverse(st, idx), x, y, w);
   return 0;
 }
 
@@ -661,6 +692,7 @@ int orc_node_solve_knn(void* s, const orc_bvp* b, double x, double y, const orc_
   int m = st->m, k = st->k;
   std::vector<double> Gl(m, 0.0), w(k);
   std::vector<int> idx(k);
+  std::map<std::vector<int>, std::vector<double>> cache;
   double Bl = 0.0, e0 = 0.0, e1 = 0.0, ndom = 0.0, nsteps = 0.0;
   Sums sums;
   for (unsigned n = 0; n < N; ++n) {
@@ -672,7 +704,11 @@ int orc_node_solve_knn(void* s, const orc_bvp* b, double x, double y, const orc_
       ndom += 1.0;
     } else {
       score = ex[n].Z + ex[n].Y * c.u;
-      orc_knn_weights(st, ex[n].x, ex[n].y, idx.data(), w.data());
+      // one inverse per distinct window (a CPU solver would tabulate them)
+      knn_select(st, ex[n].x, ex[n].y, idx.data());
+      auto itc = cache.find(idx);
+      if (itc == cache.end()) itc = cache.emplace(idx, knn_inverse(st, idx.data())).first;
+      knn_apply(st, idx.data(), itc->second, ex[n].x, ex[n].y, w.data());
       for (int a = 0; a < k; ++a) Gl[idx[a]] += -ex[n].Y * w[a];
       Bl += ex[n].Z + ex[n].xi;
     }

@@ -1,0 +1,773 @@
+// C ABI of libspac_fk (include/spac_fk.h): context, registries, meshes and the
+// launch sequence path kernel -> finalize/scatter on the context stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/spac_fk.h"
+#include "fk_device.cuh"
+#include "fk_internal.h"
+#include "fk_mesh.h"
+#include "fk_mlp.h"
+
+namespace fk {
+
+// device buffer that grows and never shrinks
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+  ~DBuf() { if (p) cudaFree(p); }
+};
+
+template <typename T>
+static cudaError_t upload(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  cudaError_t e = b.ensure(std::max<size_t>(v.size() * sizeof(T), 16));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+struct StencilSet {
+  int kind = 0;  // 0 none, 1 arcs, 2 patches
+  std::vector<ArcDev> arcs;
+  std::vector<double> arc_theta;
+  std::vector<int> arc_gid_off;  // per arc: offset into arc_gids
+  std::vector<int> arc_gids;
+  std::vector<PatchDev> patches;
+  std::vector<double> patch_nodes;
+  std::vector<int> patch_gids;
+  long long ipsi_total = 0, ainv_total = 0;
+  int nmax = 0;
+  DBuf d_arcs, d_theta, d_ipsi, d_patches, d_nodes, d_ainv;
+  bool uploaded = false;
+  int size_of(int s) const { return kind == 1 ? arcs[s].n : patches[s].m; }
+  long long acc_of(int s) const {
+    return kind == 1 ? arcs[s].n : static_cast<long long>(patches[s].nwin) * patches[s].k;
+  }
+};
+
+struct Mesh {
+  HostMesh host;
+  StencilSet st;
+  std::vector<long long> g_off;  // per item
+  long long g_total = 0;
+  std::vector<int> csr_idx;      // per item entry
+  std::vector<int> rows;         // per item
+  DBuf d_val0, d_csr_idx, d_g_off, d_row;
+  bool uploaded = false;
+};
+
+}  // namespace fk
+
+struct fk_ctx {
+  int device = 0;
+  unsigned long long seed = 0;
+  unsigned stream_id = 0;
+  int max_steps = 1 << 24;
+  int block = 256, chunk = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double timing[3] = {0, 0, 0};
+  std::string err;
+  std::vector<fk::BvpDev> bvps;
+  fk::DBuf d_bvps;
+  fk::StencilSet arcs;   // arcs registered with fk_register_arc
+  std::vector<std::unique_ptr<fk::Mesh>> meshes;
+  std::vector<std::unique_ptr<fk::Mlp>> mlps;
+  // workspace
+  fk::DBuf w_items, w_chunks, w_stats, w_acc, w_queue, w_gout, w_bout, w_sout, w_val, w_B, w_goff, w_row, w_tmp;
+};
+
+namespace {
+
+int fail(fk_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+int cuda_fail(fk_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, FK_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define FK_CUDA(call)                                      \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// copy n bytes from device workspace to a user pointer (host or device)
+cudaError_t copy_out(void* dst, const void* src, size_t n, cudaStream_t s) {
+  if (!dst || n == 0) return cudaSuccess;
+  return cudaMemcpyAsync(dst, src, n, is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s);
+}
+
+int need_device(fk_ctx* ctx) {
+  if (ctx->device < 0) return fail(ctx, FK_ERR_NO_DEVICE, "host-only context (device -1) cannot solve");
+  cudaSetDevice(ctx->device);
+  return FK_OK;
+}
+
+int upload_stencils(fk_ctx* ctx, fk::StencilSet& S, const std::vector<char>* have_ipsi,
+                    const std::vector<double>* host_ipsi);
+
+int check_bvp(fk_ctx* ctx, int bvp_id) {
+  if (bvp_id < 0 || bvp_id >= static_cast<int>(ctx->bvps.size())) return fail(ctx, FK_ERR_REGISTRY, "unknown bvp id");
+  return FK_OK;
+}
+
+// Uploads a stencil set and computes its FP64 inverses on the GPU.
+int upload_stencils(fk_ctx* ctx, fk::StencilSet& S, const std::vector<char>* have_ipsi,
+                    const std::vector<double>* host_ipsi) {
+  cudaStream_t s = ctx->stream;
+  if (S.kind == 1) {
+    FK_CUDA(fk::upload(S.d_arcs, S.arcs, s));
+    FK_CUDA(fk::upload(S.d_theta, S.arc_theta, s));
+    FK_CUDA(S.d_ipsi.ensure(std::max<long long>(S.ipsi_total, 1) * sizeof(double)));
+    const int n_arcs = static_cast<int>(S.arcs.size());
+    if (n_arcs > 0) {
+      FK_CUDA(ctx->w_tmp.ensure(std::max<long long>(S.ipsi_total, 1) * sizeof(double)));
+      FK_CUDA(fk::launch_build_psi(S.d_arcs.as<fk::ArcDev>(), S.d_theta.as<double>(), n_arcs,
+                                   ctx->w_tmp.as<double>(), s));
+      std::vector<int> ns;
+      std::vector<long long> offs;
+      for (int a = 0; a < n_arcs; ++a)
+        if (!have_ipsi || !(*have_ipsi)[a]) { ns.push_back(S.arcs[a].n); offs.push_back(S.arcs[a].ipsi_off); }
+      if (!ns.empty()) {
+        fk::DBuf dn, doff;
+        FK_CUDA(fk::upload(dn, ns, s));
+        FK_CUDA(fk::upload(doff, offs, s));
+        FK_CUDA(fk::launch_inverse(ctx->w_tmp.as<double>(), S.d_ipsi.as<double>(), dn.as<int>(), doff.as<long long>(),
+                                   S.nmax, static_cast<int>(ns.size()), s));
+        FK_CUDA(cudaStreamSynchronize(s));
+      }
+      if (have_ipsi && host_ipsi) {
+        for (int a = 0; a < n_arcs; ++a)
+          if ((*have_ipsi)[a])
+            FK_CUDA(cudaMemcpyAsync(S.d_ipsi.as<double>() + S.arcs[a].ipsi_off, host_ipsi->data() + S.arcs[a].ipsi_off,
+                                    sizeof(double) * S.arcs[a].n * S.arcs[a].n, cudaMemcpyHostToDevice, s));
+      }
+    }
+  } else if (S.kind == 2) {
+    FK_CUDA(fk::upload(S.d_patches, S.patches, s));
+    FK_CUDA(fk::upload(S.d_nodes, S.patch_nodes, s));
+    FK_CUDA(S.d_ainv.ensure(std::max<long long>(S.ainv_total, 1) * sizeof(double)));
+    const int n_p = static_cast<int>(S.patches.size());
+    std::vector<long long> win_base(n_p + 1, 0);
+    for (int p = 0; p < n_p; ++p) win_base[p + 1] = win_base[p] + S.patches[p].nwin;
+    const long long total = win_base[n_p];
+    if (total > 0) {
+      const int k = S.patches[0].k;
+      fk::DBuf dwb;
+      FK_CUDA(fk::upload(dwb, win_base, s));
+      FK_CUDA(ctx->w_tmp.ensure(std::max<long long>(S.ainv_total, 1) * sizeof(double)));
+      FK_CUDA(fk::launch_build_windows(S.d_patches.as<fk::PatchDev>(), S.d_nodes.as<double>(), n_p,
+                                       dwb.as<long long>(), total, k, ctx->w_tmp.as<double>(), s));
+      std::vector<int> ns(total, k);
+      std::vector<long long> offs(total);
+      for (long long w = 0; w < total; ++w) offs[w] = w * k * k;  // windows are contiguous in pool order
+      fk::DBuf dn, doff;
+      FK_CUDA(fk::upload(dn, ns, s));
+      FK_CUDA(fk::upload(doff, offs, s));
+      FK_CUDA(fk::launch_inverse(ctx->w_tmp.as<double>(), S.d_ainv.as<double>(), dn.as<int>(), doff.as<long long>(), k,
+                                 static_cast<int>(total), s));
+      FK_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  S.uploaded = true;
+  return FK_OK;
+}
+
+void add_arc(fk::StencilSet& S, const fk::MeshStencil& M, const int* gids_override) {
+  fk::ArcDev a;
+  a.cx = M.cx; a.cy = M.cy; a.c2 = M.c2; a.radius = M.radius; a.interior = M.interior;
+  a.n = static_cast<int>(M.nodes.size());
+  a.theta_off = static_cast<long long>(S.arc_theta.size());
+  a.ipsi_off = S.ipsi_total;
+  S.ipsi_total += static_cast<long long>(a.n) * a.n;
+  S.nmax = std::max(S.nmax, a.n);
+  S.arc_gid_off.push_back(static_cast<int>(S.arc_gids.size()));
+  for (int i = 0; i < a.n; ++i) {
+    S.arc_theta.push_back(M.nodes[i].theta);
+    S.arc_gids.push_back(gids_override ? gids_override[i] : M.nodes[i].gid);
+  }
+  S.arcs.push_back(a);
+}
+
+void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
+  fk::PatchDev p;
+  std::memset(&p, 0, sizeof(p));
+  for (int i = 0; i < 4; ++i) {
+    p.rect[i] = M.rect[i];
+    p.side_first[i] = M.side_first[i]; p.side_count[i] = M.side_count[i]; p.side_axis[i] = M.side_axis[i];
+    p.side_fixed[i] = M.side_fixed[i]; p.side_start[i] = M.side_start[i]; p.side_step[i] = M.side_step[i];
+  }
+  p.eps2 = eps * eps;
+  p.m = static_cast<int>(M.nodes.size());
+  p.k = k;
+  p.closed = M.closed ? 1 : 0;
+  p.nwin = p.closed ? p.m : p.m - k + 1;
+  p.node_off = static_cast<long long>(S.patch_nodes.size());
+  p.ainv_off = S.ainv_total;
+  S.ainv_total += static_cast<long long>(p.nwin) * k * k;
+  for (const fk::MeshNode& nd : M.nodes) {
+    S.patch_nodes.push_back(nd.x);
+    S.patch_nodes.push_back(nd.y);
+    S.patch_gids.push_back(nd.gid);
+  }
+  S.nmax = std::max(S.nmax, p.m);
+  S.patches.push_back(p);
+}
+
+// Runs items through the path kernel and the finalize kernel.
+struct RunOut {
+  double* item_G = nullptr;       // device workspace results
+  double* item_B = nullptr;
+  double* item_stats = nullptr;
+  bool capped = false;
+};
+
+int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::ItemDev>& items, fk::StencilSet* S,
+              const std::vector<long long>* g_off, long long g_total, const int* d_csr_idx, double* d_csr_val,
+              const int* d_row, double* d_B, RunOut& out) {
+  cudaStream_t s = ctx->stream;
+  const int n = static_cast<int>(items.size());
+  const int kind = S ? S->kind : 0;
+  const fk::BvpDev& bvp = ctx->bvps[bvp_id];
+  if (precision != FK_FP64 && precision != FK_FP32) return fail(ctx, FK_ERR_ARG, "precision must be FK_FP64 or FK_FP32");
+  // per-item stencil accumulator offsets
+  std::vector<fk::ItemDev> it = items;
+  long long acc_total = 0;
+  int acc_words = 0;
+  for (auto& x : it) {
+    x.acc_off = acc_total;
+    if (kind != 0 && x.stencil >= 0) {
+      const long long w = S->acc_of(x.stencil);
+      acc_total += w;
+      acc_words = std::max<int>(acc_words, static_cast<int>(w));
+    }
+  }
+  // chunks: balance the persistent grid
+  long long total_paths = 0;
+  for (auto& x : it) if (!x.frontera) total_paths += x.paths;
+  const int block = ctx->block;
+  const size_t sacc_bytes =
+      static_cast<size_t>(acc_words) * ((precision == FK_FP64 || kind == 1) ? sizeof(double) : sizeof(float));
+  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes);
+  const int grid = std::max(1, ctx->num_sms * occ);
+  long long chunk = ctx->chunk;
+  if (chunk <= 0) {
+    chunk = total_paths / (4LL * grid);
+    chunk = std::max<long long>(block, std::min<long long>(chunk, 16384));
+    chunk = (chunk + block - 1) / block * block;
+  }
+  std::vector<fk::ChunkDev> chunks;
+  for (int i = 0; i < n; ++i) {
+    if (it[i].frontera || it[i].paths == 0) continue;
+    for (unsigned p0 = 0; p0 < it[i].paths; p0 += static_cast<unsigned>(chunk)) {
+      const unsigned p1 = static_cast<unsigned>(std::min<long long>(it[i].paths, p0 + chunk));
+      chunks.push_back(fk::ChunkDev{i, p0, p1});
+    }
+  }
+  FK_CUDA(fk::upload(ctx->w_items, it, s));
+  FK_CUDA(fk::upload(ctx->w_chunks, chunks, s));
+  FK_CUDA(ctx->w_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
+  FK_CUDA(cudaMemsetAsync(ctx->w_stats.p, 0, static_cast<size_t>(n) * fk::kNumStats * sizeof(double), s));
+  FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
+  if (acc_total > 0) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
+  FK_CUDA(ctx->w_queue.ensure(16));
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, sizeof(int), s));
+
+  fk::LaunchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.bvp = ctx->d_bvps.as<fk::BvpDev>() + bvp_id;
+  a.items = ctx->w_items.as<fk::ItemDev>();
+  a.chunks = ctx->w_chunks.as<fk::ChunkDev>();
+  a.n_chunks = static_cast<int>(chunks.size());
+  if (kind == 1) { a.arcs = S->d_arcs.as<fk::ArcDev>(); a.arc_theta = S->d_theta.as<double>(); }
+  if (kind == 2) { a.patches = S->d_patches.as<fk::PatchDev>(); a.patch_nodes = S->d_nodes.as<double>(); }
+  a.queue = ctx->w_queue.as<int>();
+  a.stats = ctx->w_stats.as<double>();
+  a.acc = ctx->w_acc.as<double>();
+  a.key0 = static_cast<uint32_t>(ctx->seed);
+  a.key1 = static_cast<uint32_t>(ctx->seed >> 32);
+  a.stream = ctx->stream_id;
+  a.max_steps = ctx->max_steps;
+  a.cv = (bvp.cv == FK_CV_EXACT) ? 1 : 0;
+  a.stencil_kind = kind;
+  a.acc_words = acc_words;
+  FK_CUDA(cudaEventRecord(ctx->ev[0], s));
+  if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s));
+  FK_CUDA(cudaEventRecord(ctx->ev[1], s));
+
+  // finalize
+  FK_CUDA(ctx->w_gout.ensure(std::max<size_t>(g_total * sizeof(double), 16)));
+  FK_CUDA(ctx->w_bout.ensure(std::max<size_t>(n * sizeof(double), 16)));
+  FK_CUDA(ctx->w_sout.ensure(std::max<size_t>(static_cast<size_t>(n) * 16 * sizeof(double), 16)));
+  if (g_off) FK_CUDA(fk::upload(ctx->w_goff, *g_off, s));
+  fk::FinalizeArgs f;
+  std::memset(&f, 0, sizeof(f));
+  f.bvp = a.bvp;
+  f.items = a.items;
+  f.n_items = n;
+  if (kind == 1) { f.arcs = a.arcs; f.arc_ipsi = S->d_ipsi.as<double>(); }
+  if (kind == 2) { f.patches = a.patches; f.patch_ainv = S->d_ainv.as<double>(); }
+  f.stats = a.stats;
+  f.acc = a.acc;
+  f.stencil_kind = kind;
+  f.g_off = g_off ? ctx->w_goff.as<long long>() : nullptr;
+  f.item_G = kind ? ctx->w_gout.as<double>() : nullptr;
+  f.item_B = ctx->w_bout.as<double>();
+  f.item_stats = ctx->w_sout.as<double>();
+  f.csr_idx = d_csr_idx;
+  f.csr_val = d_csr_val;
+  f.row = d_row;
+  f.B = d_B;
+  FK_CUDA(fk::launch_finalize(f, bvp.problem, s));
+  FK_CUDA(cudaEventRecord(ctx->ev[2], s));
+  FK_CUDA(cudaStreamSynchronize(s));
+  float t0 = 0, t1 = 0;
+  cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[2]);
+  ctx->timing[0] = t0;
+  ctx->timing[1] = t1;
+  ctx->timing[2] = chunks.empty() ? 1 : 2;
+  ctx->stream_id++;
+  out.item_G = f.item_G;
+  out.item_B = f.item_B;
+  out.item_stats = f.item_stats;
+  // capped paths?
+  std::vector<double> cap(n);
+  std::vector<double> st(static_cast<size_t>(n) * 16);
+  FK_CUDA(cudaMemcpy(st.data(), f.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) if (st[static_cast<size_t>(i) * 16 + 12] > 0) out.capped = true;
+  return FK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fk_create(fk_ctx** out, int device, unsigned long long seed) {
+  if (!out) return FK_ERR_ARG;
+  *out = nullptr;
+  if (device == -1) {  // host-only context: meshes and CSR patterns, no solves
+    fk_ctx* ctx = new fk_ctx();
+    ctx->device = -1;
+    ctx->seed = seed;
+    ctx->arcs.kind = 1;
+    *out = ctx;
+    return FK_OK;
+  }
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+    cudaGetLastError();
+    return FK_ERR_NO_DEVICE;
+  }
+  fk_ctx* ctx = new fk_ctx();
+  ctx->device = device;
+  ctx->seed = seed;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return FK_ERR_NO_DEVICE;
+  }
+  for (auto& e : ctx->ev) cudaEventCreate(&e);
+  ctx->arcs.kind = 1;
+  *out = ctx;
+  return FK_OK;
+}
+
+int fk_destroy(fk_ctx* ctx) {
+  if (!ctx) return FK_ERR_ARG;
+  if (ctx->device < 0) {
+    delete ctx;
+    return FK_OK;
+  }
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
+  ctx->meshes.clear();
+  ctx->mlps.clear();
+  cudaStream_t s = ctx->stream;
+  delete ctx;
+  if (s) cudaStreamDestroy(s);
+  return FK_OK;
+}
+
+const char* fk_last_error(const fk_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fk_set_stream(fk_ctx* ctx, unsigned id) { if (!ctx) return FK_ERR_ARG; ctx->stream_id = id; return FK_OK; }
+int fk_get_stream(const fk_ctx* ctx, unsigned* id) { if (!ctx || !id) return FK_ERR_ARG; *id = ctx->stream_id; return FK_OK; }
+int fk_set_max_steps(fk_ctx* ctx, int m) {
+  if (!ctx || m < 1) return fail(ctx, FK_ERR_ARG, "max_steps must be >= 1");
+  ctx->max_steps = m;
+  return FK_OK;
+}
+int fk_set_launch(fk_ctx* ctx, int block, int chunk) {
+  if (!ctx) return FK_ERR_ARG;
+  if (block != 0 && (block < 32 || block > 256 || block % 32)) return fail(ctx, FK_ERR_ARG, "block must be 32..256, multiple of 32");
+  if (chunk < 0) return fail(ctx, FK_ERR_ARG, "chunk must be >= 0");
+  ctx->block = block ? block : 256;
+  ctx->chunk = chunk;
+  return FK_OK;
+}
+int fk_cuda_stream(const fk_ctx* ctx, void** s) { if (!ctx || !s) return FK_ERR_ARG; *s = ctx->stream; return FK_OK; }
+int fk_last_timing(const fk_ctx* ctx, double out[3]) {
+  if (!ctx || !out) return FK_ERR_ARG;
+  for (int i = 0; i < 3; ++i) out[i] = ctx->timing[i];
+  return FK_OK;
+}
+
+int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* d, int* id) {
+  if (!ctx || !d || !id) return fail(ctx, FK_ERR_ARG, "null argument");
+  if (d->problem < 0 || d->problem > 3) return fail(ctx, FK_ERR_REGISTRY, "unknown problem functor");
+  if (d->cv < FK_CV_NONE || d->cv > FK_CV_MLP) return fail(ctx, FK_ERR_ARG, "unknown control-variate mode");
+  const int need_shape = (d->problem == FK_PROBLEM_DISK) ? FK_SHAPE_CIRCLE : FK_SHAPE_RECT;
+  if (d->dom_shape != need_shape) return fail(ctx, FK_ERR_ARG, "domain shape does not match the problem functor");
+  if (d->cv == FK_CV_MLP && (d->mlp_id < 0 || d->mlp_id >= static_cast<int>(ctx->mlps.size())))
+    return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  for (int i = 0; i < 4; ++i)
+    if (!std::isfinite(d->dom[i]) || !std::isfinite(d->prob[i])) return fail(ctx, FK_ERR_ARG, "non-finite parameters");
+  if (d->dom_shape == FK_SHAPE_RECT && !(d->dom[2] > d->dom[0] && d->dom[3] > d->dom[1]))
+    return fail(ctx, FK_ERR_ARG, "empty rectangle domain");
+  if (d->dom_shape == FK_SHAPE_CIRCLE && !(d->dom[0] > 0)) return fail(ctx, FK_ERR_ARG, "non-positive radius");
+  fk::BvpDev b;
+  std::memset(&b, 0, sizeof(b));
+  b.problem = d->problem;
+  b.cv = d->cv;
+  b.dom_shape = d->dom_shape;
+  b.mlp = d->mlp_id;
+  for (int i = 0; i < 4; ++i) { b.dom[i] = d->dom[i]; b.prob[i] = d->prob[i]; }
+  ctx->bvps.push_back(b);
+  if (ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    FK_CUDA(fk::upload(ctx->d_bvps, ctx->bvps, ctx->stream));
+    FK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  *id = static_cast<int>(ctx->bvps.size()) - 1;
+  return FK_OK;
+}
+
+static void stats_to_struct(const double* s, fk_stats* o) {
+  o->phi = s[0]; o->phiphi = s[1]; o->phi_VR = s[2]; o->phiphi_VR = s[3]; o->xi = s[4]; o->xixi = s[5];
+  o->xiphi = s[6]; o->APL = s[7]; o->RNGC = s[8]; o->B = s[9]; o->n_paths = s[10]; o->n_domain_exits = s[11];
+  o->n_capped = s[12]; o->xi_mean = s[13]; o->xi_sq_mean = s[14]; o->mean_steps = s[15];
+}
+
+int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsigned* paths, const double* h,
+                    const int* sub_shape, const double* sub_params, int precision, fk_stats* out) {
+  if (!ctx) return FK_ERR_ARG;
+  if (n < 0 || (n > 0 && (!xy || !paths || !h || !out))) return fail(ctx, FK_ERR_ARG, "null argument");
+  int rc = check_bvp(ctx, bvp_id);
+  if (rc) return rc;
+  if (n == 0) return FK_OK;
+  if ((rc = need_device(ctx))) return rc;
+  std::vector<fk::ItemDev> items(n);
+  for (int i = 0; i < n; ++i) {
+    fk::ItemDev& it = items[i];
+    std::memset(&it, 0, sizeof(it));
+    if (!(h[i] > 0) || !std::isfinite(xy[2 * i]) || !std::isfinite(xy[2 * i + 1]))
+      return fail(ctx, FK_ERR_ARG, "point solve: h must be > 0 and coordinates finite");
+    it.x = xy[2 * i]; it.y = xy[2 * i + 1]; it.h = h[i]; it.sqrth = std::sqrt(h[i]);
+    it.paths = paths[i]; it.stencil = -1; it.frontera = 0;
+    it.sub_shape = sub_shape ? sub_shape[i] : -1;
+    if (sub_params) for (int q = 0; q < 4; ++q) it.sub[q] = sub_params[4 * i + q];
+    if (it.sub_shape > 1) return fail(ctx, FK_ERR_ARG, "unknown subdomain shape");
+  }
+  RunOut ro;
+  rc = run_items(ctx, bvp_id, precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro);
+  if (rc) return rc;
+  std::vector<double> st(static_cast<size_t>(n) * 16);
+  FK_CUDA(cudaMemcpy(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &out[i]);
+  if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+int fk_register_arc(fk_ctx* ctx, const fk_arc_desc* d, int* id) {
+  if (!ctx || !d || !id) return fail(ctx, FK_ERR_ARG, "null argument");
+  if (d->n < 1 || d->n > 64 || !d->theta || !d->gids) return fail(ctx, FK_ERR_ARG, "arc needs 1..64 nodes with angles and ids");
+  if (int rc0 = need_device(ctx)) return rc0;
+  fk::MeshStencil M;
+  M.cx = d->cx; M.cy = d->cy; M.radius = d->radius; M.c2 = d->c2; M.interior = d->interior;
+  for (int i = 0; i < d->n; ++i) {
+    fk::MeshNode nd;
+    std::memset(&nd, 0, sizeof(nd));
+    nd.theta = d->theta[i];
+    nd.gid = d->gids[i];
+    M.nodes.push_back(nd);
+  }
+  // append and (re)upload the registered-arc pool
+  fk::StencilSet& S = ctx->arcs;
+  std::vector<char> have(S.arcs.size(), 1);
+  std::vector<double> host_ipsi;
+  {
+    // keep already computed inverses
+    host_ipsi.assign(S.ipsi_total + static_cast<long long>(d->n) * d->n, 0.0);
+    if (S.ipsi_total > 0) FK_CUDA(cudaMemcpy(host_ipsi.data(), S.d_ipsi.p, S.ipsi_total * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  add_arc(S, M, nullptr);
+  have.push_back(d->iPsi ? 1 : 0);
+  if (d->iPsi) std::memcpy(host_ipsi.data() + S.arcs.back().ipsi_off, d->iPsi, sizeof(double) * d->n * d->n);
+  int rc = upload_stencils(ctx, S, &have, &host_ipsi);
+  if (rc) return rc;
+  FK_CUDA(cudaStreamSynchronize(ctx->stream));
+  *id = static_cast<int>(S.arcs.size()) - 1;
+  return FK_OK;
+}
+
+int fk_arc_ipsi(fk_ctx* ctx, int arc_id, double* iPsi) {
+  if (!ctx || !iPsi) return fail(ctx, FK_ERR_ARG, "null argument");
+  if (arc_id < 0 || arc_id >= static_cast<int>(ctx->arcs.arcs.size())) return fail(ctx, FK_ERR_REGISTRY, "unknown arc id");
+  const fk::ArcDev& a = ctx->arcs.arcs[arc_id];
+  FK_CUDA(cudaMemcpy(iPsi, ctx->arcs.d_ipsi.as<double>() + a.ipsi_off, sizeof(double) * a.n * a.n, cudaMemcpyDeviceToHost));
+  return FK_OK;
+}
+
+int fk_solve_nodes_arc(fk_ctx* ctx, int bvp_id, int n, const fk_node_item* items, int precision, double* G, double* B,
+                       fk_stats* stats) {
+  if (!ctx) return FK_ERR_ARG;
+  if (n < 0 || (n > 0 && (!items || !G || !B))) return fail(ctx, FK_ERR_ARG, "null argument");
+  int rc = check_bvp(ctx, bvp_id);
+  if (rc) return rc;
+  if (n == 0) return FK_OK;
+  if ((rc = need_device(ctx))) return rc;
+  fk::StencilSet& S = ctx->arcs;
+  std::vector<fk::ItemDev> it(n);
+  std::vector<long long> goff(n);
+  long long gt = 0;
+  for (int i = 0; i < n; ++i) {
+    const fk_node_item& q = items[i];
+    if (q.stencil < 0 || q.stencil >= static_cast<int>(S.arcs.size())) return fail(ctx, FK_ERR_REGISTRY, "unknown arc id");
+    if (!(q.h > 0)) return fail(ctx, FK_ERR_ARG, "h must be > 0");
+    fk::ItemDev& d = it[i];
+    std::memset(&d, 0, sizeof(d));
+    const fk::ArcDev& a = S.arcs[q.stencil];
+    d.x = q.x; d.y = q.y; d.h = q.h; d.sqrth = std::sqrt(q.h); d.paths = q.paths; d.stencil = q.stencil;
+    d.frontera = q.frontera ? 1 : 0; d.sub_shape = FK_SHAPE_CIRCLE;
+    d.sub[0] = a.radius; d.sub[1] = a.cx; d.sub[2] = a.cy;
+    goff[i] = gt;
+    gt += a.n;
+  }
+  RunOut ro;
+  rc = run_items(ctx, bvp_id, precision, it, &S, &goff, gt, nullptr, nullptr, nullptr, nullptr, ro);
+  if (rc) return rc;
+  FK_CUDA(copy_out(G, ro.item_G, gt * sizeof(double), ctx->stream));
+  FK_CUDA(copy_out(B, ro.item_B, n * sizeof(double), ctx->stream));
+  if (stats) {
+    std::vector<double> st(static_cast<size_t>(n) * 16);
+    FK_CUDA(cudaMemcpyAsync(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FK_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &stats[i]);
+  }
+  FK_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+static int finish_mesh(fk_ctx* ctx, std::unique_ptr<fk::Mesh>& M, int* id) {
+  fk::HostMesh& h = M->host;
+  fk::StencilSet& S = M->st;
+  S.kind = h.kind;
+  for (const fk::MeshStencil& st : h.stencils) {
+    if (h.kind == 1) add_arc(S, st, nullptr); else add_patch(S, st, h.knn, h.eps);
+  }
+  if (h.kind == 1 && S.nmax > 64) return fail(ctx, FK_ERR_CAPACITY, "arcs with more than 64 nodes");
+  // item -> G offsets and CSR positions
+  M->g_off.resize(h.items.size());
+  M->g_total = 0;
+  std::vector<int> rows;
+  for (size_t i = 0; i < h.items.size(); ++i) {
+    const fk::MeshItem& q = h.items[i];
+    M->g_off[i] = M->g_total;
+    const int sz = S.size_of(q.stencil);
+    const int* gids = (h.kind == 1) ? &S.arc_gids[S.arc_gid_off[q.stencil]] : nullptr;
+    std::vector<int> pg;
+    if (h.kind == 2) {
+      for (const fk::MeshNode& nd : h.stencils[q.stencil].nodes) pg.push_back(nd.gid);
+      gids = pg.data();
+    }
+    for (int j = 0; j < sz; ++j) {
+      int pos = -1;
+      for (int c = h.rowptr[q.row]; c < h.rowptr[q.row + 1]; ++c)
+        if (h.col[c] == gids[j]) { pos = c; break; }
+      if (pos < 0) return fail(ctx, FK_ERR_NOT_FOUND, "stencil node missing from the CSR row");
+      M->csr_idx.push_back(pos);
+    }
+    M->g_total += sz;
+    rows.push_back(q.row);
+  }
+  M->rows = rows;
+  ctx->meshes.push_back(std::move(M));
+  *id = static_cast<int>(ctx->meshes.size()) - 1;
+  return FK_OK;
+}
+
+int fk_mesh_circles(fk_ctx* ctx, const double dom[4], int n_side, double superposicion, double theta0,
+                    int nodes_per_circle, double c2_corner, double c2_side, int* mesh_id) {
+  if (!ctx || !dom || !mesh_id) return fail(ctx, FK_ERR_ARG, "null argument");
+  std::unique_ptr<fk::Mesh> M(new fk::Mesh());
+  if (!fk::build_circle_mesh(dom, n_side, superposicion, theta0, nodes_per_circle, c2_corner, c2_side, M->host, ctx->err))
+    return FK_ERR_ARG;
+  return finish_mesh(ctx, M, mesh_id);
+}
+
+int fk_mesh_square_patches(fk_ctx* ctx, const double dom[4], int n_sub, int nodes_per_side, double enlarge,
+                           double eps_spacing, int knn, int* mesh_id) {
+  if (!ctx || !dom || !mesh_id) return fail(ctx, FK_ERR_ARG, "null argument");
+  if (knn > 32) return fail(ctx, FK_ERR_ARG, "knn must be <= 32");
+  std::unique_ptr<fk::Mesh> M(new fk::Mesh());
+  if (!fk::build_square_patch_mesh(dom, n_sub, nodes_per_side, enlarge, eps_spacing, knn, M->host, ctx->err))
+    return FK_ERR_ARG;
+  return finish_mesh(ctx, M, mesh_id);
+}
+
+static fk::Mesh* get_mesh(fk_ctx* ctx, int id) {
+  if (!ctx || id < 0 || id >= static_cast<int>(ctx->meshes.size())) return nullptr;
+  return ctx->meshes[id].get();
+}
+
+static int upload_mesh(fk_ctx* ctx, fk::Mesh* M) {
+  if (M->uploaded) return FK_OK;
+  int rc = upload_stencils(ctx, M->st, nullptr, nullptr);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  FK_CUDA(fk::upload(M->d_val0, M->host.val0, s));
+  FK_CUDA(fk::upload(M->d_csr_idx, M->csr_idx, s));
+  FK_CUDA(fk::upload(M->d_row, M->rows, s));
+  FK_CUDA(cudaStreamSynchronize(s));
+  M->uploaded = true;
+  return FK_OK;
+}
+
+int fk_mesh_get_info(fk_ctx* ctx, int mesh_id, fk_mesh_info* info) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M || !info) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  info->n_rows = M->host.n_rows;
+  info->nnz = M->host.nnz;
+  info->n_items = static_cast<int>(M->host.items.size());
+  info->n_nodes = static_cast<int>(M->host.nodes.size());
+  info->n_stencils = static_cast<int>(M->host.stencils.size());
+  int mx = 0;
+  for (size_t s = 0; s < M->host.stencils.size(); ++s) mx = std::max<int>(mx, static_cast<int>(M->host.stencils[s].nodes.size()));
+  info->max_stencil = mx;
+  info->spacing = M->host.spacing;
+  return FK_OK;
+}
+
+int fk_mesh_nodes(fk_ctx* ctx, int mesh_id, double* xy, int* flags) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  for (size_t i = 0; i < M->host.nodes.size(); ++i) {
+    if (xy) { xy[2 * i] = M->host.nodes[i].x; xy[2 * i + 1] = M->host.nodes[i].y; }
+    if (flags) flags[i] = M->host.nodes[i].frontera ? 1 : 0;
+  }
+  return FK_OK;
+}
+
+int fk_mesh_items(fk_ctx* ctx, int mesh_id, int* row, double* xy, int* stencil, int* frontera) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  for (size_t i = 0; i < M->host.items.size(); ++i) {
+    const fk::MeshItem& q = M->host.items[i];
+    if (row) row[i] = q.row;
+    if (xy) { xy[2 * i] = q.x; xy[2 * i + 1] = q.y; }
+    if (stencil) stencil[i] = q.stencil;
+    if (frontera) frontera[i] = q.frontera ? 1 : 0;
+  }
+  return FK_OK;
+}
+
+int fk_mesh_stencil_nodes(fk_ctx* ctx, int mesh_id, int s, int* gids, int* n) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M || !n) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (s < 0 || s >= static_cast<int>(M->host.stencils.size())) return fail(ctx, FK_ERR_REGISTRY, "unknown stencil");
+  const fk::MeshStencil& S = M->host.stencils[s];
+  *n = static_cast<int>(S.nodes.size());
+  if (gids) for (size_t i = 0; i < S.nodes.size(); ++i) gids[i] = S.nodes[i].gid;
+  return FK_OK;
+}
+
+int fk_mesh_csr(fk_ctx* ctx, int mesh_id, int* rowptr, int* col, double* val0) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (rowptr) std::memcpy(rowptr, M->host.rowptr.data(), sizeof(int) * M->host.rowptr.size());
+  if (col) std::memcpy(col, M->host.col.data(), sizeof(int) * M->host.col.size());
+  if (val0) std::memcpy(val0, M->host.val0.data(), sizeof(double) * M->host.val0.size());
+  return FK_OK;
+}
+
+int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsigned* paths_per_item, double h,
+                int precision, double* val, double* B, double* item_G, double* item_B, fk_stats* item_stats) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  int rc = check_bvp(ctx, bvp_id);
+  if (rc) return rc;
+  if (!(h > 0)) return fail(ctx, FK_ERR_ARG, "h must be > 0");
+  if ((rc = need_device(ctx))) return rc;
+  if (ctx->bvps.size() * sizeof(fk::BvpDev) > ctx->d_bvps.bytes) {
+    FK_CUDA(fk::upload(ctx->d_bvps, ctx->bvps, ctx->stream));
+  }
+  if ((rc = upload_mesh(ctx, M))) return rc;
+  const fk::HostMesh& hm = M->host;
+  const int n = static_cast<int>(hm.items.size());
+  std::vector<fk::ItemDev> it(n);
+  for (int i = 0; i < n; ++i) {
+    const fk::MeshItem& q = hm.items[i];
+    fk::ItemDev& d = it[i];
+    std::memset(&d, 0, sizeof(d));
+    d.x = q.x; d.y = q.y; d.h = h; d.sqrth = std::sqrt(h);
+    d.paths = paths_per_item ? paths_per_item[i] : paths;
+    d.stencil = q.stencil; d.frontera = q.frontera ? 1 : 0;
+    const fk::MeshStencil& S = hm.stencils[q.stencil];
+    if (hm.kind == 1) { d.sub_shape = FK_SHAPE_CIRCLE; d.sub[0] = S.radius; d.sub[1] = S.cx; d.sub[2] = S.cy; }
+    else { d.sub_shape = FK_SHAPE_RECT; for (int k = 0; k < 4; ++k) d.sub[k] = S.rect[k]; }
+  }
+  cudaStream_t s = ctx->stream;
+  FK_CUDA(ctx->w_val.ensure(std::max<size_t>(hm.nnz * sizeof(double), 16)));
+  FK_CUDA(ctx->w_B.ensure(std::max<size_t>(hm.n_rows * sizeof(double), 16)));
+  FK_CUDA(cudaMemcpyAsync(ctx->w_val.p, M->d_val0.p, hm.nnz * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  FK_CUDA(cudaMemsetAsync(ctx->w_B.p, 0, hm.n_rows * sizeof(double), s));
+  RunOut ro;
+  rc = run_items(ctx, bvp_id, precision, it, &M->st, &M->g_off, M->g_total, M->d_csr_idx.as<int>(),
+                 ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro);
+  if (rc) return rc;
+  FK_CUDA(copy_out(val, ctx->w_val.p, hm.nnz * sizeof(double), s));
+  FK_CUDA(copy_out(B, ctx->w_B.p, hm.n_rows * sizeof(double), s));
+  FK_CUDA(copy_out(item_G, ro.item_G, M->g_total * sizeof(double), s));
+  FK_CUDA(copy_out(item_B, ro.item_B, n * sizeof(double), s));
+  if (item_stats) {
+    std::vector<double> st(static_cast<size_t>(n) * 16);
+    FK_CUDA(cudaMemcpyAsync(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &item_stats[i]);
+  }
+  FK_CUDA(cudaStreamSynchronize(s));
+  if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+}  // extern "C"

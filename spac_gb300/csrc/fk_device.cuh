@@ -1,0 +1,320 @@
+// Device building blocks of the GB300 Feynman-Kac path kernels: Philox4x32-10
+// normals, the Frontera distance functors, the fused BVP coefficient functors
+// and the exit rule.  Everything is templated on the stepping type R (float
+// or double); accumulations above the path level are FP64.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fk {
+
+constexpr double kGobet = -0.5826;  // Gobet-Menozzi shift, FeynmanKacSolver.cpp:169,184
+
+// ------------------------------------------------------------------ Philox ----
+// Philox4x32-10 (Salmon et al., SC'11).  Counter (step/2, path, item, stream),
+// key (seed lo, seed hi).
+__device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Box-Muller pair from two 32-bit words: u = (word + 1/2) 2^-32 in (0,1).
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& z0, double& z1) {
+  const double inv32 = 2.3283064365386962890625e-10;
+  const double u1 = (static_cast<double>(a) + 0.5) * inv32;
+  const double u2 = (static_cast<double>(b) + 0.5) * inv32;
+  const double rad = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincos(6.283185307179586 * u2, &s, &c);
+  z0 = rad * c;
+  z1 = rad * s;
+}
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
+  const float inv32 = 2.3283064365386962890625e-10f;
+  const float u1 = (static_cast<float>(a) + 0.5f) * inv32;  // rounds into (0, 1]
+  const float u2 = (static_cast<float>(b) + 0.5f) * inv32;
+  const float rad = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  z0 = rad * c;
+  z1 = rad * s;
+}
+
+// ------------------------------------------------------------ geometry -------
+template <typename R>
+struct Bnd {
+  R d;        // signed distance (negative inside)
+  R ex, ey;   // closest boundary point (exit point)
+  R nx, ny;   // outward normal
+};
+
+// Circulo (Dominios/Circulo.hpp:7-22): p = [r, cx, cy]; |x - c| clamped at 5e-4.
+template <typename R>
+__device__ __forceinline__ Bnd<R> circle_dist(R x, R y, R r0, R cx, R cy) {
+  Bnd<R> b;
+  R nx = x - cx, ny = y - cy;
+  R r = sqrt(nx * nx + ny * ny);
+  r = r > R(5e-4) ? r : R(5e-4);
+  nx = nx / r;
+  ny = ny / r;
+  b.nx = nx;
+  b.ny = ny;
+  b.ex = nx * r0 + cx;
+  b.ey = ny * r0 + cy;
+  b.d = r - r0;
+  return b;
+}
+
+// Rectangulo (Dominios/Rectangulo.hpp:7-229): p = [x0, y0, x1, y1].  Signs
+// sx, sy pick the quadrant (a point on a centre line is in the lower/left
+// one); inside, the side with the larger offset wins (tie -> horizontal side);
+// outside, the corner if both offsets exceed the half sides.
+template <typename R>
+__device__ __forceinline__ Bnd<R> rect_dist(R x, R y, R x0, R y0, R x1, R y1) {
+  const R kDiag = R(0.70710678118f);
+  Bnd<R> b;
+  const R cx = R(0.5) * (x0 + x1), cy = R(0.5) * (y0 + y1);
+  const R hx = x1 - cx, hy = y1 - cy;
+  const R dx = fabs(x - cx), dy = fabs(y - cy);
+  const bool px = x > cx, py = y > cy;
+  const R sx = px ? R(1) : R(-1), sy = py ? R(1) : R(-1);
+  const R bx = px ? hx + cx : -hx + cx;
+  const R by = py ? hy + cy : -hy + cy;
+  const R ox = dx - hx, oy = dy - hy;
+  b.ex = x;
+  b.ey = y;
+  bool side_x;
+  if ((dx <= hx) && (dy <= hy)) {
+    side_x = ox > oy;
+  } else if (dx > hx && dy > hy) {
+    b.ex = bx;
+    b.ey = by;
+    b.nx = sx * kDiag;
+    b.ny = sy * kDiag;
+    b.d = sqrt(ox * ox + oy * oy);
+    return b;
+  } else {
+    side_x = dx > hx;
+  }
+  if (side_x) {
+    b.ex = bx;
+    b.nx = sx;
+    b.ny = R(0);
+    b.d = ox;
+  } else {
+    b.ey = by;
+    b.nx = R(0);
+    b.ny = sy;
+    b.d = oy;
+  }
+  return b;
+}
+
+// Branch-cut angle of an exit point for the arc stencil (Mesh/Nudo.hpp:7-32
+// dispatched as in Interfaz::Update_G, Mesh/Interfaz.cpp:222-251).
+__device__ __forceinline__ double arc_theta(int interior, double dx, double dy) {
+  const double a = atan2(dy, dx);
+  const double pi = 3.141592653589793;
+  switch (interior) {
+    case -33: case -44: case -2: return (a >= 0) ? a : a + 2.0 * pi;
+    case -1: return (a <= -0.5 * pi) ? 2.0 * pi + a : a;
+    case -3: return (a <= 0.5 * pi) ? 2.0 * pi + a : a;
+    default: return a;  // -11, -22, -4
+  }
+}
+
+// ----------------------------------------------------------- problems -------
+struct BvpDev {
+  int problem, cv, dom_shape, mlp;
+  double dom[4];
+  double prob[4];
+};
+
+template <typename R>
+struct StepCoef {
+  R f, c, bx, by, s, Fx, Fy;  // source, potential, drift, sigma = s I, control field F
+};
+
+// Franke test function with its gradient and Laplacian, each exponential
+// evaluated once (BVPs/Franke_Poisson.hpp:4-60).
+template <typename R>
+struct FrankeEval {
+  R e1, e2, e3, e4, a, b, c, d, p, q, r, t;  // t unused
+  __device__ __forceinline__ FrankeEval(R x, R y) {
+    a = R(9) * x - R(2);
+    b = R(9) * y - R(2);
+    c = R(9) * x + R(1);
+    d = R(9) * y + R(1);
+    p = R(9) * x - R(7);
+    q = R(9) * y - R(3);
+    r = R(9) * x - R(4);
+    t = R(9) * y - R(7);
+    e1 = exp(R(-0.25) * (a * a + b * b));
+    e2 = exp(R(-1.0 / 49.0) * (c * c) - R(0.1) * d);
+    e3 = exp(R(-0.25) * (p * p + q * q));
+    e4 = exp(R(-1) * (r * r + t * t));
+  }
+  __device__ __forceinline__ R u() const { return R(0.75) * e1 + R(0.75) * e2 + R(0.5) * e3 - R(0.2) * e4; }
+  __device__ __forceinline__ R ux() const {
+    return R(-3.375) * a * e1 - R(27.0 / 98.0) * c * e2 - R(2.25) * p * e3 + R(3.6) * r * e4;
+  }
+  __device__ __forceinline__ R uy() const {
+    return R(-3.375) * b * e1 - R(0.675) * e2 - R(2.25) * q * e3 + R(3.6) * t * e4;
+  }
+  __device__ __forceinline__ R uxx() const {
+    return R(-3.375) * (R(9) - R(4.5) * (a * a)) * e1 -
+           R(27.0 / 98.0) * (R(9) - R(18.0 / 49.0) * (c * c)) * e2 -
+           R(2.25) * (R(9) - R(4.5) * (p * p)) * e3 + R(3.6) * (R(9) - R(18) * (r * r)) * e4;
+  }
+  __device__ __forceinline__ R uyy() const {
+    return R(-3.375) * (R(9) - R(4.5) * (b * b)) * e1 + R(243.0 / 400.0) * e2 -
+           R(2.25) * (R(9) - R(4.5) * (q * q)) * e3 + R(3.6) * (R(9) - R(18) * (t * t)) * e4;
+  }
+};
+
+__device__ __forceinline__ float sinpi_(float v) { return sinpif(v); }
+__device__ __forceinline__ double sinpi_(double v) { return sinpi(v); }
+
+// Monegros with c = -1 (BVPs/Monegros_Revamped.hpp:4-75).
+template <typename R>
+struct MonegrosEval {
+  R u, ux, uy, lap;
+  __device__ __forceinline__ MonegrosEval(R x, R y) {
+    const R k1 = R(1.0), k2 = R(0.01), k3 = R(0.02), k4 = R(0.12), k5 = R(0.05), k6 = R(0.05), k7 = R(-0.12),
+            sf = R(0.333);
+    const R rho = sqrt(k1 + k2 * x * x + k3 * y * y);
+    R sr, cr;
+    sr = sin(rho);
+    cr = cos(rho);
+    const R a1 = k4 * x + k5 * y, a2 = k6 * x + k7 * y;
+    const R s1 = sin(a1), c1 = cos(a1), s2 = sin(a2), c2 = cos(a2);
+    const R th = tanh(s1 + s2);
+    const R th2m1 = th * th - R(1);
+    u = R(3) + sf * (sr + th);
+    ux = sf * (cr * k2 * x / rho - (k4 * c1 + k6 * c2) * th2m1);
+    uy = sf * (cr * k1 * k3 * y / rho - (k5 * c1 + k7 * c2) * th2m1);
+    const R r3 = rho * rho * rho;
+    const R uxx = sf * (((k2 / rho) - (k2 * k2 * x * x / r3)) * cr - (x * x * k2 * k2 / (rho * rho)) * sr +
+                        R(2) * (k4 * c1 + k6 * c2) * (k4 * c1 + k6 * c2) * th2m1 * th +
+                        (k4 * k4 * s1 + k6 * k6 * s2) * th2m1);
+    const R uyy = sf * (((k3 / rho) - (k3 * k3 * y * y / r3)) * cr - (y * y * k3 * k3 / (rho * rho)) * sr +
+                        R(2) * (k5 * c1 + k7 * c2) * (k5 * c1 + k7 * c2) * th2m1 * th +
+                        (k5 * k5 * s1 + k7 * k7 * s2) * th2m1);
+    lap = uxx + uyy;
+  }
+};
+
+template <int PROB>
+struct Problem;
+
+// FK_PROBLEM_FRANKE: sigma = 1.41421356237 I, b = 0, c = 0, f = -Lap u.
+template <>
+struct Problem<0> {
+  template <typename R>
+  __device__ static R sigma(const BvpDev&, R, R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, bool cv, StepCoef<R>& o) {
+    FrankeEval<R> F(x, y);
+    o.s = R(1.41421356237);
+    o.f = -F.uxx() - F.uyy();
+    o.c = R(0);
+    o.bx = R(0);
+    o.by = R(0);
+    if (cv) {
+      o.Fx = -o.s * F.ux();
+      o.Fy = -o.s * F.uy();
+    }
+  }
+  template <typename R>
+  __device__ static R u(const BvpDev&, R x, R y) { return FrankeEval<R>(x, y).u(); }
+};
+
+// FK_PROBLEM_MONEGROS: sigma = 1.41421356237 I, b = 0, c = -1, f = -Lap u + u.
+template <>
+struct Problem<1> {
+  template <typename R>
+  __device__ static R sigma(const BvpDev&, R, R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, bool cv, StepCoef<R>& o) {
+    MonegrosEval<R> M(x, y);
+    o.s = R(1.41421356237);
+    o.c = R(-1);
+    o.f = -M.lap - o.c * M.u;
+    o.bx = R(0);
+    o.by = R(0);
+    if (cv) {
+      o.Fx = -o.s * M.ux;
+      o.Fy = -o.s * M.uy;
+    }
+  }
+  template <typename R>
+  __device__ static R u(const BvpDev&, R x, R y) { return MonegrosEval<R>(x, y).u; }
+};
+
+// FK_PROBLEM_ANISO.
+template <>
+struct Problem<2> {
+  template <typename R>
+  __device__ static R coef_a(R x, R y) {
+    return R(1) + R(0.5) * sinpi_(R(2) * x) * sinpi_(R(2) * y);
+  }
+  template <typename R>
+  __device__ static R sigma(const BvpDev&, R x, R y) { return sqrt(R(2) * coef_a(x, y)); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, bool cv, StepCoef<R>& o) {
+    FrankeEval<R> F(x, y);
+    const R q = R(1) + x * y;
+    const R Fv = F.u(), Fx = F.ux(), Fy = F.uy();
+    const R u = Fv * q;
+    const R ux = Fx * q + Fv * y, uy = Fy * q + Fv * x;
+    const R lap = (F.uxx() + F.uyy()) * q + R(2) * (Fx * y + Fy * x);
+    const R a = coef_a(x, y);
+    o.s = sqrt(R(2) * a);
+    o.c = -(R(1) + x * x + y * y);
+    o.bx = y - R(0.5);
+    o.by = R(0.5) - x;
+    o.f = -(a * lap + o.bx * ux + o.by * uy + o.c * u);
+    if (cv) {
+      o.Fx = -o.s * ux;
+      o.Fy = -o.s * uy;
+    }
+  }
+  template <typename R>
+  __device__ static R u(const BvpDev&, R x, R y) { return FrankeEval<R>(x, y).u() * (R(1) + x * y); }
+};
+
+// FK_PROBLEM_DISK: Franke mapped from the disk's bounding box to [0,1]^2.
+template <>
+struct Problem<3> {
+  template <typename R>
+  __device__ static R sigma(const BvpDev&, R, R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev& b, R x, R y, bool cv, StepCoef<R>& o) {
+    const R inv = R(1) / (R(2) * R(b.prob[2]));
+    const R xi = (x - R(b.prob[0])) * inv + R(0.5), eta = (y - R(b.prob[1])) * inv + R(0.5);
+    FrankeEval<R> F(xi, eta);
+    o.s = R(1.41421356237);
+    o.f = -(F.uxx() + F.uyy()) * (inv * inv);
+    o.c = R(0);
+    o.bx = R(0);
+    o.by = R(0);
+    if (cv) {
+      o.Fx = -o.s * F.ux() * inv;
+      o.Fy = -o.s * F.uy() * inv;
+    }
+  }
+  template <typename R>
+  __device__ static R u(const BvpDev& b, R x, R y) {
+    const R inv = R(1) / (R(2) * R(b.prob[2]));
+    return FrankeEval<R>((x - R(b.prob[0])) * inv + R(0.5), (y - R(b.prob[1])) * inv + R(0.5)).u();
+  }
+};
+
+}  // namespace fk

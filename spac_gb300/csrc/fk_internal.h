@@ -1,0 +1,110 @@
+// Internal host/device interface of libspac_fk: the device-side records the
+// kernels read and the host launchers the C ABI calls.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fk {
+
+struct BvpDev;
+
+// One solve item: a point (Solve_OMP_Analytic(X0,...)) or a node of a mesh
+// solved against one stencil (Solve_OMP_Analytic(Nudo&, ..., Interfaz)).
+struct ItemDev {
+  double x, y, h, sqrth;
+  double sub[4];          // subdomain boundary parameters
+  unsigned paths;
+  int stencil;            // arc / patch index, -1 for point solves
+  int frontera;           // B = g(x), no paths
+  int sub_shape;          // point solves: 0 rect, 1 circle, -1 = domain
+  long long acc_off;      // first double of this item's stencil accumulator
+};
+
+struct ChunkDev {
+  int item;
+  unsigned p0, p1;
+};
+
+// Reference arc stencil (Interfaz): iPsi applied per item after the paths.
+struct ArcDev {
+  double cx, cy, c2, radius;
+  int interior, n;
+  long long theta_off, ipsi_off;  // into the arc theta / iPsi pools
+};
+
+// Gaussian k-nearest stencil on a rectangular patch boundary.
+struct PatchDev {
+  double rect[4];
+  double eps2;
+  int m, k, closed, nwin;
+  long long node_off;   // 2*m doubles (x, y) in chain order
+  long long ainv_off;   // nwin * k * k doubles, column-major per window
+  // sides: chain index of the first node, node count, axis (0: node x varies),
+  // fixed coordinate, coordinate of the first node and signed step
+  int side_first[4], side_count[4], side_axis[4];
+  double side_fixed[4], side_start[4], side_step[4];
+};
+
+// Per-item FP64 sums written by the path kernel: score, score^2, xi + xi^2
+// (the reference's aliased xi slot), score + xi, (score + xi)^2, xi score,
+// steps, B, domain exits, capped paths, xi^2.
+enum { kStatScore = 0, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScore, kStatSteps, kStatB, kStatDom,
+       kStatCap, kStatXi2, kNumStats = 12 };
+
+struct LaunchArgs {
+  const BvpDev* bvp;
+  const ItemDev* items;
+  const ChunkDev* chunks;
+  int n_chunks;
+  const ArcDev* arcs;
+  const double* arc_theta;
+  const PatchDev* patches;
+  const double* patch_nodes;
+  int* queue;              // chunk counter (zeroed before launch)
+  double* stats;           // n_items * kNumStats
+  double* acc;             // stencil accumulators
+  uint32_t key0, key1, stream;
+  int max_steps;
+  int cv;
+  int stencil_kind;        // 0 none, 1 arc, 2 patch
+  int acc_words;           // shared accumulator length (elements) per CTA
+  const void* mlp;         // device MLP parameters (FK_CV_MLP)
+};
+
+struct FinalizeArgs {
+  const BvpDev* bvp;
+  const ItemDev* items;
+  int n_items;
+  const ArcDev* arcs;
+  const double* arc_ipsi;
+  const PatchDev* patches;
+  const double* patch_ainv;
+  const double* stats;
+  const double* acc;
+  int stencil_kind;
+  const long long* g_off;   // item -> first entry in item_G
+  double* item_G;           // may be null
+  double* item_B;           // may be null
+  double* item_stats;       // n_items * 16 (fk_stats layout), may be null
+  const int* csr_idx;       // item -> csr positions (g_off indexed), may be null
+  double* csr_val;          // may be null
+  const int* row;           // item -> row (for B scatter)
+  double* B;                // may be null
+};
+
+// host launchers (fk_kernels.cu)
+cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block,
+                         size_t smem, cudaStream_t s);
+int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem);
+cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s);
+// batched FP64 full-pivot Gauss-Jordan inverse: matrix b is ns[b] x ns[b],
+// column-major at offset offs[b] of A (input) and inv (output); ns[b] <= 64
+cudaError_t launch_inverse(const double* A, double* inv, const int* ns, const long long* offs, int nmax, int count,
+                           cudaStream_t s);
+// builds Psi for arcs (theta-IMQ) / A_W for patch windows into `out` (column-major)
+cudaError_t launch_build_psi(const ArcDev* arcs, const double* theta, int n_arcs, double* out, cudaStream_t s);
+cudaError_t launch_build_windows(const PatchDev* patches, const double* nodes, int n_patches,
+                                 const long long* win_base, long long total_windows, int k, double* out,
+                                 cudaStream_t s);
+
+}  // namespace fk

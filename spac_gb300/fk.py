@@ -1,0 +1,344 @@
+"""ctypes binding of libspac_fk (include/spac_fk.h) with numpy arrays.
+
+`Context` is a 1:1 wrapper of the C ABI; `FeynmanKacSolverGPU` mirrors the
+public interface of the reference's FeynmanKacSolver
+(Solvers/FeynmanKacSolver.hpp:43-98): the two Solve_OMP_Analytic overloads
+and the public statistics members they fill.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib_path
+
+FK_OK = 0
+FK_ERR_ARG, FK_ERR_CUDA, FK_ERR_REGISTRY, FK_ERR_STEP_CAP = -1, -2, -3, -4
+FK_ERR_NOT_FOUND, FK_ERR_NO_DEVICE, FK_ERR_CAPACITY = -5, -6, -7
+FRANKE, MONEGROS, ANISO, DISK = 0, 1, 2, 3
+RECT, CIRCLE = 0, 1
+CV_NONE, CV_EXACT, CV_MLP = 0, 1, 2
+FP64, FP32 = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_uint)
+_fp = C.POINTER(C.c_float)
+
+
+class BvpDesc(C.Structure):
+    _fields_ = [("problem", C.c_int), ("cv", C.c_int), ("dom_shape", C.c_int), ("dom", C.c_double * 4),
+                ("prob", C.c_double * 4), ("mlp_id", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL",
+                                          "RNGC", "B", "n_paths", "n_domain_exits", "n_capped", "xi_mean",
+                                          "xi_sq_mean", "mean_steps")]
+
+
+STAT_FIELDS = [f[0] for f in Stats._fields_]
+
+
+class ArcDesc(C.Structure):
+    _fields_ = [("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double), ("c2", C.c_double),
+                ("interior", C.c_int), ("n", C.c_int), ("theta", _dp), ("gids", _ip), ("iPsi", _dp)]
+
+
+class NodeItem(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("h", C.c_double), ("paths", C.c_uint),
+                ("frontera", C.c_int), ("row", C.c_int), ("stencil", C.c_int)]
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [("n_rows", C.c_int), ("nnz", C.c_int), ("n_items", C.c_int), ("n_nodes", C.c_int),
+                ("n_stencils", C.c_int), ("max_stencil", C.c_int), ("spacing", C.c_double)]
+
+
+_LIB = None
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "fk_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_ulonglong]),
+    "fk_destroy": (C.c_int, [C.c_void_p]),
+    "fk_last_error": (C.c_char_p, [C.c_void_p]),
+    "fk_set_stream": (C.c_int, [C.c_void_p, C.c_uint]),
+    "fk_get_stream": (C.c_int, [C.c_void_p, _up]),
+    "fk_set_max_steps": (C.c_int, [C.c_void_p, C.c_int]),
+    "fk_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "fk_cuda_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "fk_last_timing": (C.c_int, [C.c_void_p, _dp]),
+    "fk_register_bvp": (C.c_int, [C.c_void_p, C.POINTER(BvpDesc), _ip]),
+    "fk_solve_points": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _up, _dp, _ip, _dp, C.c_int,
+                                  C.POINTER(Stats)]),
+    "fk_register_arc": (C.c_int, [C.c_void_p, C.POINTER(ArcDesc), _ip]),
+    "fk_arc_ipsi": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "fk_solve_nodes_arc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(NodeItem), C.c_int, _dp, _dp,
+                                     C.POINTER(Stats)]),
+    "fk_mesh_circles": (C.c_int, [C.c_void_p, _dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
+                                  C.c_double, _ip]),
+    "fk_mesh_square_patches": (C.c_int, [C.c_void_p, _dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                         _ip]),
+    "fk_mesh_get_info": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(MeshInfo)]),
+    "fk_mesh_nodes": (C.c_int, [C.c_void_p, C.c_int, _dp, _ip]),
+    "fk_mesh_items": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _ip, _ip]),
+    "fk_mesh_stencil_nodes": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _ip]),
+    "fk_mesh_csr": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp]),
+    "fk_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint, _up, C.c_double, C.c_int, _dp, _dp, _dp,
+                              _dp, C.POINTER(Stats)]),
+    "fk_mlp_create": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.c_ulonglong, _ip]),
+    "fk_mlp_num_params": (C.c_int, [C.c_void_p, C.c_int, _ip]),
+    "fk_mlp_get_params": (C.c_int, [C.c_void_p, C.c_int, _fp]),
+    "fk_mlp_set_params": (C.c_int, [C.c_void_p, C.c_int, _fp]),
+    "fk_mlp_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double,
+                               C.c_ulonglong, _fp]),
+    "fk_mlp_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
+    "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
+}
+
+
+def load():
+    """Load libspac_fk.so and bind every declared entry point."""
+    global _LIB
+    if _LIB is None:
+        L = C.CDLL(lib_path())
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        _LIB = L
+    return _LIB
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+class FKError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libspac_fk error {code}: {msg}")
+        self.code = code
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_ip)
+
+
+def _u(a):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    return a, a.ctypes.data_as(_up)
+
+
+def stats_dict(s):
+    return {k: getattr(s, k) for k in STAT_FIELDS}
+
+
+def stats_array(arr):
+    return {k: np.array([getattr(s, k) for s in arr]) for k in STAT_FIELDS}
+
+
+class Context:
+    """One GPU context (device, Philox seed, stream, registries)."""
+
+    def __init__(self, device=0, seed=1234):
+        self.L = load()
+        self.h = C.c_void_p()
+        rc = self.L.fk_create(C.byref(self.h), device, seed)
+        if rc != FK_OK:
+            raise FKError(rc, "fk_create failed (no usable CUDA device?)")
+
+    def close(self):
+        if self.h:
+            self.L.fk_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc, allow=()):
+        if rc != FK_OK and rc not in allow:
+            raise FKError(rc, self.L.fk_last_error(self.h).decode())
+        return rc
+
+    # -- context
+    def set_stream(self, s):
+        self.check(self.L.fk_set_stream(self.h, s))
+
+    def get_stream(self):
+        v = C.c_uint()
+        self.check(self.L.fk_get_stream(self.h, C.byref(v)))
+        return v.value
+
+    def set_max_steps(self, m):
+        self.check(self.L.fk_set_max_steps(self.h, m))
+
+    def set_launch(self, block=0, chunk=0):
+        self.check(self.L.fk_set_launch(self.h, block, chunk))
+
+    def cuda_stream(self):
+        v = C.c_void_p()
+        self.check(self.L.fk_cuda_stream(self.h, C.byref(v)))
+        return v.value
+
+    def last_timing(self):
+        out = (C.c_double * 3)()
+        self.check(self.L.fk_last_timing(self.h, out))
+        return list(out)
+
+    # -- registry
+    def register_bvp(self, problem, cv=CV_NONE, dom=(0, 0, 1, 1), dom_shape=None, prob=(0, 0, 0, 0), mlp_id=-1):
+        if dom_shape is None:
+            dom_shape = CIRCLE if problem == DISK else RECT
+        d = BvpDesc(problem, cv, dom_shape, (C.c_double * 4)(*dom), (C.c_double * 4)(*prob), mlp_id)
+        i = C.c_int()
+        self.check(self.L.fk_register_bvp(self.h, C.byref(d), C.byref(i)))
+        return i.value
+
+    # -- point solves
+    def solve_points(self, bvp, xy, paths, h, precision=FP64, sub_shape=None, sub_params=None, allow=()):
+        xy, pxy = _d(np.reshape(xy, (-1, 2)))
+        n = xy.shape[0]
+        paths, pp = _u(np.broadcast_to(paths, (n,)))
+        h, ph = _d(np.broadcast_to(h, (n,)))
+        ss = ps = None
+        if sub_shape is not None:
+            ss, ps_ = _i(np.broadcast_to(sub_shape, (n,)))
+            sp, psp = _d(np.reshape(sub_params, (n, 4)))
+        out = (Stats * n)()
+        rc = self.L.fk_solve_points(self.h, bvp, n, pxy, pp, ph, ps_ if ss is not None else None,
+                                    psp if ss is not None else None, precision, out)
+        self.check(rc, allow)
+        return stats_array(out)
+
+    # -- arcs / node solves
+    def register_arc(self, cx, cy, radius, c2, interior, theta, gids, iPsi=None):
+        theta, pt = _d(theta)
+        gids, pg = _i(gids)
+        ip = None
+        if iPsi is not None:
+            iPsi, ip = _d(np.asfortranarray(iPsi).ravel(order="F"))
+        d = ArcDesc(cx, cy, radius, c2, interior, len(theta), pt, pg, ip)
+        i = C.c_int()
+        self.check(self.L.fk_register_arc(self.h, C.byref(d), C.byref(i)))
+        return i.value
+
+    def arc_ipsi(self, arc_id, n):
+        out = np.zeros(n * n)
+        self.check(self.L.fk_arc_ipsi(self.h, arc_id, out.ctypes.data_as(_dp)))
+        return out.reshape((n, n), order="F")
+
+    def solve_nodes_arc(self, bvp, items, arc_sizes, precision=FP64):
+        n = len(items)
+        arr = (NodeItem * n)(*[NodeItem(*it) for it in items])
+        gt = int(sum(arc_sizes[it[6]] for it in items))
+        G = np.zeros(gt)
+        B = np.zeros(n)
+        st = (Stats * n)()
+        self.check(self.L.fk_solve_nodes_arc(self.h, bvp, n, arr, precision, G.ctypes.data_as(_dp),
+                                             B.ctypes.data_as(_dp), st))
+        return G, B, stats_array(st)
+
+    # -- meshes
+    def mesh_circles(self, dom, n_side, superposicion, theta0, nodes_per_circle, c2_corner=1.5, c2_side=1.1):
+        dom, pd = _d(dom)
+        i = C.c_int()
+        self.check(self.L.fk_mesh_circles(self.h, pd, n_side, superposicion, theta0, nodes_per_circle, c2_corner,
+                                          c2_side, C.byref(i)))
+        return i.value
+
+    def mesh_square_patches(self, dom, n_sub, nodes_per_side, enlarge=0.25, eps_spacing=3.0, knn=20):
+        dom, pd = _d(dom)
+        i = C.c_int()
+        self.check(self.L.fk_mesh_square_patches(self.h, pd, n_sub, nodes_per_side, enlarge, eps_spacing, knn,
+                                                 C.byref(i)))
+        return i.value
+
+    def mesh_info(self, mesh):
+        m = MeshInfo()
+        self.check(self.L.fk_mesh_get_info(self.h, mesh, C.byref(m)))
+        return {k: getattr(m, k) for k, _ in MeshInfo._fields_}
+
+    def mesh_nodes(self, mesh):
+        info = self.mesh_info(mesh)
+        xy = np.zeros((info["n_nodes"], 2))
+        fl = np.zeros(info["n_nodes"], dtype=np.int32)
+        self.check(self.L.fk_mesh_nodes(self.h, mesh, xy.ctypes.data_as(_dp), fl.ctypes.data_as(_ip)))
+        return xy, fl
+
+    def mesh_items(self, mesh):
+        info = self.mesh_info(mesh)
+        n = info["n_items"]
+        row = np.zeros(n, dtype=np.int32)
+        xy = np.zeros((n, 2))
+        st = np.zeros(n, dtype=np.int32)
+        fr = np.zeros(n, dtype=np.int32)
+        self.check(self.L.fk_mesh_items(self.h, mesh, row.ctypes.data_as(_ip), xy.ctypes.data_as(_dp),
+                                        st.ctypes.data_as(_ip), fr.ctypes.data_as(_ip)))
+        return row, xy, st, fr
+
+    def mesh_stencil_nodes(self, mesh, s):
+        n = C.c_int()
+        self.check(self.L.fk_mesh_stencil_nodes(self.h, mesh, s, None, C.byref(n)))
+        g = np.zeros(n.value, dtype=np.int32)
+        self.check(self.L.fk_mesh_stencil_nodes(self.h, mesh, s, g.ctypes.data_as(_ip), C.byref(n)))
+        return g
+
+    def mesh_csr(self, mesh):
+        info = self.mesh_info(mesh)
+        rp = np.zeros(info["n_rows"] + 1, dtype=np.int32)
+        col = np.zeros(info["nnz"], dtype=np.int32)
+        v0 = np.zeros(info["nnz"])
+        self.check(self.L.fk_mesh_csr(self.h, mesh, rp.ctypes.data_as(_ip), col.ctypes.data_as(_ip),
+                                      v0.ctypes.data_as(_dp)))
+        return rp, col, v0
+
+    def assemble(self, mesh, bvp, paths, h, precision=FP64, paths_per_item=None, items=True, allow=()):
+        info = self.mesh_info(mesh)
+        val = np.zeros(info["nnz"])
+        B = np.zeros(info["n_rows"])
+        pp = None
+        if paths_per_item is not None:
+            ppi, pp = _u(paths_per_item)
+        G = iB = st = None
+        if items:
+            sizes = [len(self.mesh_stencil_nodes(mesh, s)) for s in range(info["n_stencils"])]
+            _, _, stn, _ = self.mesh_items(mesh)
+            G = np.zeros(int(sum(sizes[s] for s in stn)))
+            iB = np.zeros(info["n_items"])
+            st = (Stats * info["n_items"])()
+        rc = self.L.fk_assemble(self.h, mesh, bvp, int(paths), pp, h, precision, val.ctypes.data_as(_dp),
+                                B.ctypes.data_as(_dp), G.ctypes.data_as(_dp) if items else None,
+                                iB.ctypes.data_as(_dp) if items else None, st if items else None)
+        self.check(rc, allow)
+        return dict(val=val, B=B, item_G=G, item_B=iB, item_stats=stats_array(st) if items else None)
+
+
+class FeynmanKacSolverGPU:
+    """Mirror of FeynmanKacSolver's public interface on the GPU path.
+
+    Solve_OMP_Analytic(X0, N, h, rho, bvp) fills phi, phiphi, phi_VR,
+    phiphi_VR, xi, xixi, xiphi, APL, RNGC (FeynmanKacSolver.cpp:335-342);
+    rho (reflecting boundaries) is accepted and unused, as every boundary of
+    the supported problems is absorbing.
+    """
+
+    def __init__(self, ctx, precision=FP64):
+        self.ctx = ctx
+        self.precision = precision
+        self.N = 0
+        for k in ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL", "RNGC"):
+            setattr(self, k, 0.0)
+
+    def Solve_OMP_Analytic(self, X0, N, h, rho, bvp):
+        st = self.ctx.solve_points(bvp, np.asarray(X0, dtype=np.float64).reshape(1, 2), N, h, self.precision)
+        self.N = N
+        for k in ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL", "RNGC"):
+            setattr(self, k, float(st[k][0]))
+        return self

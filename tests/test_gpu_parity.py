@@ -1,0 +1,272 @@
+"""GPU kernels (through the C ABI) against the CPU oracle and the reference.
+
+FP64 stepping on the same Philox stream follows the same paths as the
+oracle, so per-node results agree to rounding (rtol 1e-9 on averages; 1e-6
+absolute on G entries, whose RBF inverse has condition ~1e10).  FP32 stepping
+is compared with FP64 on the same stream (paired differences well inside one
+standard error), and against the reference's own results within 4 combined
+standard errors (the random streams differ).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+SEED = 20251203
+RTOL = 1e-9
+
+
+def _oracle_session(orc, gpu):
+    return orc.Session(orc.RNG_PHILOX, seed=SEED)
+
+
+CASES = [  # problem, cv, dom, points, sub (shape, params) or None, h
+    (0, 0, (0, 0, 1, 1), [(0.3, 0.4), (0.05, 0.9), (0.5, 0.5)], None, 1e-3),
+    (0, 1, (0, 0, 1, 1), [(0.7, 0.2)], None, 2e-3),
+    (2, 0, (0, 0, 1, 1), [(0.25, 0.75), (0.9, 0.1)], None, 1e-3),
+    (2, 1, (0, 0, 1, 1), [(0.6, 0.45)], None, 1e-3),
+    (1, 1, (-200, -200, 200, 200), [(-72.0, -38.0)], (0, (-72.3, -38.2, -71.75, -37.7)), 1e-3),
+    (3, 0, (0.8, 0.1, -0.2), [(0.3, 0.1), (-0.5, -0.4)], None, 1e-3),
+]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_point_solves_fp64_match_oracle(gpu, orc, fk, case):
+    problem, cv, dom, pts, sub, h = CASES[case]
+    prob = (dom[1], dom[2], dom[0], 0) if problem == fk.DISK else (0, 0, 0, 0)
+    dshape = fk.CIRCLE if problem == fk.DISK else fk.RECT
+    b = gpu.register_bvp(problem, cv=cv, dom=dom, prob=prob)
+    N = 1500
+    gpu.set_stream(100 + case)
+    kw = {}
+    if sub is not None:
+        kw = dict(sub_shape=[sub[0]] * len(pts), sub_params=np.tile(sub[1], (len(pts), 1)))
+    st = gpu.solve_points(b, np.array(pts), N, h, fk.FP64, **kw)
+    s = _oracle_session(orc, gpu)
+    s.set_stream(100 + case)
+    ob = orc.bvp(problem, cv=cv, dom=dom, dom_shape=dshape, prob=prob)
+    osub = orc.shape(sub[0], sub[1]) if sub is not None else None
+    for i, (x, y) in enumerate(pts):
+        o = s.point_solve(ob, x, y, N, h, item=i, sub=osub)
+        for k in orc.STAT_NAMES:
+            assert np.isclose(st[k][i], o[k], rtol=RTOL, atol=1e-12), (k, i, st[k][i], o[k])
+        assert st["n_paths"][i] == N and st["n_capped"][i] == 0
+
+
+def test_point_solves_fp32_paired_with_fp64(gpu, fk):
+    b = gpu.register_bvp(fk.ANISO)
+    pts = np.array([[0.3, 0.4], [0.8, 0.7], [0.1, 0.5]])
+    N = 20000
+    gpu.set_stream(7)
+    s64 = gpu.solve_points(b, pts, N, 1e-3, fk.FP64)
+    gpu.set_stream(7)
+    s32 = gpu.solve_points(b, pts, N, 1e-3, fk.FP32)
+    se = np.sqrt((s64["phiphi"] - s64["phi"] ** 2) / N)
+    assert np.all(np.abs(s32["phi"] - s64["phi"]) < 0.5 * se)
+    assert np.all(np.abs(s32["APL"] - s64["APL"]) < 0.02 * s64["APL"])
+
+
+def test_point_solves_match_reference_statistically(gpu, fk):
+    """Reference results (golden, its own random stream) within 4 combined SE."""
+    pts = np.load(os.path.join(GOLDEN, "points.npy"))
+    for row in pts:
+        problem, use_F = int(row[0]), int(row[1])
+        dom, x, y, sk = tuple(row[2:6]), row[6], row[7], int(row[8])
+        sub, N_ref, h = row[9:13], int(row[13]), row[14]
+        ref = dict(zip(("phi", "phiphi", "phi_VR", "phiphi_VR"), row[15:19]))
+        b = gpu.register_bvp(problem, cv=use_F, dom=dom)
+        kw = {}
+        if sk:
+            kw = dict(sub_shape=[0 if sk == 2 else 1], sub_params=np.array([sub]))
+        N = 200000
+        for prec in (fk.FP64, fk.FP32):
+            st = gpu.solve_points(b, np.array([[x, y]]), N, h, prec, **kw)
+            for m, mm in (("phi", "phiphi"), ("phi_VR", "phiphi_VR")):
+                v_ref = max(ref[mm] - ref[m] ** 2, 0.0) / N_ref
+                v_gpu = max(st[mm][0] - st[m][0] ** 2, 0.0) / N
+                assert abs(st[m][0] - ref[m]) <= 4 * np.sqrt(v_ref + v_gpu) + 1e-12, (problem, use_F, m, prec)
+
+
+def test_exact_control_variate_reduces_variance(gpu, fk):
+    pts = np.array([[0.3, 0.4], [0.6, 0.7]])
+    b0 = gpu.register_bvp(fk.FRANKE, cv=fk.CV_NONE)
+    b1 = gpu.register_bvp(fk.FRANKE, cv=fk.CV_EXACT)
+    s0 = gpu.solve_points(b0, pts, 20000, 1e-4, fk.FP64)
+    s1 = gpu.solve_points(b1, pts, 20000, 1e-4, fk.FP64)
+    v0 = s0["phiphi_VR"] - s0["phi_VR"] ** 2
+    v1 = s1["phiphi_VR"] - s1["phi_VR"] ** 2
+    assert np.all(v1 < v0 / 20)
+
+
+def _golden_arcs(name):
+    from test_oracle_pin import _arcs, _mesh
+    m = _mesh(name)
+    return m, _arcs(m)
+
+
+def test_arc_inverse_bit_exact_with_reference(gpu):
+    _, arcs = _golden_arcs("serial")
+    for a in arcs:
+        if "iPsi" not in a:
+            continue
+        aid = gpu.register_arc(a["cx"], a["cy"], a["radius"], a["c2"], a["interior"], a["theta"], a["gids"])
+        assert np.array_equal(gpu.arc_ipsi(aid, a["n"]), a["iPsi"])
+
+
+def test_arc_node_solves_match_oracle(gpu, orc, fk):
+    A = np.load(os.path.join(GOLDEN, "assembly_unit3_p0_f0.npz"))
+    m, arcs = _golden_arcs("unit3")
+    node_xy = {int(g): (x, y) for g, (x, y) in zip(m["node_int"][:, 0], m["node_dbl"][:, :2])}
+    ids = {}
+    for k, a in enumerate(arcs):
+        if "iPsi" in a:
+            ids[k] = gpu.register_arc(a["cx"], a["cy"], a["radius"], a["c2"], a["interior"], a["theta"], a["gids"],
+                                      iPsi=a["iPsi"])
+    sizes = {ids[k]: arcs[k]["n"] for k in ids}
+    items = []
+    for row, iface, frontera, nG in A["item_int"]:
+        x, y = node_xy[int(row)]
+        items.append((x, y, 1e-3, 300, int(frontera), int(row), ids[int(iface)]))
+    for problem, cv in ((fk.FRANKE, 0), (fk.ANISO, 1)):
+        b = gpu.register_bvp(problem, cv=cv)
+        gpu.set_stream(55)
+        G, B, st = gpu.solve_nodes_arc(b, items, sizes, fk.FP64)
+        s = _oracle_session(orc, gpu)
+        s.set_stream(55)
+        ob = orc.bvp(problem, cv=cv)
+        off = 0
+        for i, (row, iface, frontera, nG) in enumerate(A["item_int"]):
+            x, y = node_xy[int(row)]
+            Go, Bo, sto = s.node_solve_arc(ob, x, y, frontera, arcs[iface], 300, 1e-3, item=i)
+            n = arcs[iface]["n"]
+            assert np.isclose(B[i], Bo, rtol=RTOL, atol=1e-12), i
+            if not frontera:
+                assert np.allclose(G[off:off + n], Go, rtol=0, atol=1e-6), i
+                for k in ("phi", "phi_VR", "APL", "RNGC"):
+                    assert np.isclose(st[k][i], sto[k], rtol=RTOL, atol=1e-12), (k, i)
+            off += n
+
+
+def _oracle_assembly(orc, gpu, mesh, problem, cv, N, h, stream, kind):
+    """Per-item oracle node solves + Actualiza_GB on the product's mesh."""
+    import ctypes as C
+    info = gpu.mesh_info(mesh)
+    row, ixy, st, fr = gpu.mesh_items(mesh)
+    rp, col, v0 = gpu.mesh_csr(mesh)
+    nxy, _ = gpu.mesh_nodes(mesh)
+    s = orc.Session(orc.RNG_PHILOX, seed=SEED)
+    s.set_stream(stream)
+    ob = orc.bvp(problem, cv=cv)
+    val, B = v0.copy(), np.zeros(info["n_rows"])
+    items_G, items_B = [], []
+    L = orc.load()
+    for i in range(info["n_items"]):
+        gids = gpu.mesh_stencil_nodes(mesh, st[i])
+        x, y = ixy[i]
+        if kind == "patch":
+            a, bb = divmod(int(st[i]), int(round(np.sqrt(info["n_stencils"]))))
+            rect = _patch_rect(gpu, mesh, st[i])
+            G, Bv, _, _ = s.node_solve_knn(ob, x, y, rect, nxy[gids], 6, gpu._eps, N, h, item=i)
+        items_G.append(G)
+        items_B.append(Bv)
+        cols = np.ascontiguousarray(gids, dtype=np.int32)
+        Gc = np.ascontiguousarray(G)
+        L.orc_actualiza_gb(int(row[i]), len(Gc), cols.ctypes.data_as(C.POINTER(C.c_int)),
+                           Gc.ctypes.data_as(C.POINTER(C.c_double)), Bv, rp.ctypes.data_as(C.POINTER(C.c_int)),
+                           col.ctypes.data_as(C.POINTER(C.c_int)), val.ctypes.data_as(C.POINTER(C.c_double)),
+                           B.ctypes.data_as(C.POINTER(C.c_double)))
+    return np.concatenate(items_G), np.array(items_B), val, B
+
+
+def _patch_rect(gpu, mesh, s):
+    return gpu._rects[s]
+
+
+def test_square_patch_assembly_matches_oracle(gpu, orc, fk):
+    n_sub, nps, e, eps_sp, k = 3, 9, 0.25, 1.0, 6
+    mesh = gpu.mesh_square_patches((0, 0, 1, 1), n_sub, nps, e, eps_sp, k)
+    info = gpu.mesh_info(mesh)
+    H = 1.0 / n_sub
+    gpu._rects = {a * n_sub + b: ((a - e) * H, (b - e) * H, (a + 1 + e) * H, (b + 1 + e) * H)
+                  for a in range(n_sub) for b in range(n_sub)}
+    gpu._eps = eps_sp / info["spacing"]
+    for problem, cv in ((fk.ANISO, 0), (fk.FRANKE, 1)):
+        b = gpu.register_bvp(problem, cv=cv)
+        gpu.set_stream(77)
+        r = gpu.assemble(mesh, b, 256, 5e-4, fk.FP64)
+        G, Bi, val, B = _oracle_assembly(orc, gpu, mesh, problem, cv, 256, 5e-4, 77, "patch")
+        assert np.allclose(r["item_B"], Bi, rtol=RTOL, atol=1e-12)
+        assert np.allclose(r["item_G"], G, rtol=1e-9, atol=1e-9)
+        assert np.allclose(r["val"], val, rtol=1e-9, atol=1e-9)
+        assert np.allclose(r["B"], B, rtol=RTOL, atol=1e-12)
+
+
+def test_circle_assembly_matches_oracle(gpu, orc, fk):
+    m, arcs = _golden_arcs("unit3")
+    mesh = gpu.mesh_circles((0, 0, 1, 1), 3, 1.2, 0.121, 20)
+    b = gpu.register_bvp(fk.FRANKE)
+    gpu.set_stream(31)
+    r = gpu.assemble(mesh, b, 200, 1e-3, fk.FP64)
+    # CSR pattern equals the reference's; values from oracle node solves on the same stream
+    rp, col, v0 = gpu.mesh_csr(mesh)
+    assert np.array_equal(rp, m["rowptr"]) and np.array_equal(col, m["col"])
+    row, ixy, st, fr = gpu.mesh_items(mesh)
+    s = orc.Session(orc.RNG_PHILOX, seed=SEED)
+    s.set_stream(31)
+    ob = orc.bvp(fk.FRANKE)
+    val, B = v0.copy(), np.zeros(len(rp) - 1)
+    off = 0
+    for i in range(len(row)):
+        a = arcs[st[i]]
+        G, Bv, _ = s.node_solve_arc(ob, ixy[i, 0], ixy[i, 1], fr[i], a, 200, 1e-3, item=i)
+        assert np.isclose(r["item_B"][i], Bv, rtol=RTOL, atol=1e-12)
+        if not fr[i]:
+            assert np.allclose(r["item_G"][off:off + a["n"]], G, atol=1e-6)
+            for j, g in enumerate(a["gids"]):
+                pos = rp[row[i]] + np.searchsorted(col[rp[row[i]]:rp[row[i] + 1]], g)
+                val[pos] += G[j]
+        B[row[i]] += Bv
+        off += a["n"]
+    assert np.allclose(r["val"], val, atol=1e-6)
+    assert np.allclose(r["B"], B, rtol=1e-9, atol=1e-12)
+
+
+def test_square_patch_fp32_paired_with_fp64(gpu, fk):
+    mesh = gpu.mesh_square_patches((0, 0, 1, 1), 4, 15, 0.25, 3.0, 20)
+    b = gpu.register_bvp(fk.ANISO)
+    gpu.set_stream(9)
+    r64 = gpu.assemble(mesh, b, 4000, 5e-4, fk.FP64)
+    gpu.set_stream(9)
+    r32 = gpu.assemble(mesh, b, 4000, 5e-4, fk.FP32)
+    se = np.sqrt(np.maximum(r64["item_stats"]["phiphi"] - r64["item_stats"]["phi"] ** 2, 1e-30) / 4000)
+    d = np.abs(r32["item_B"] - r64["item_B"])
+    assert np.all(d < 0.5 * se + 1e-6)
+    assert np.allclose(r32["item_G"], r64["item_G"], atol=0.02)
+
+
+def test_step_cap_reports_error(gpu, fk):
+    b = gpu.register_bvp(fk.FRANKE)
+    gpu.set_max_steps(3)
+    try:
+        with pytest.raises(fk.FKError) as e:
+            gpu.solve_points(b, np.array([[0.5, 0.5]]), 1000, 1e-4)
+        assert e.value.code == fk.FK_ERR_STEP_CAP
+        st = gpu.solve_points(b, np.array([[0.5, 0.5]]), 1000, 1e-4, allow=(fk.FK_ERR_STEP_CAP,))
+        assert st["n_capped"][0] > 0
+    finally:
+        gpu.set_max_steps(1 << 24)
+
+
+def test_reproducible_for_a_stream(gpu, fk):
+    mesh = gpu.mesh_square_patches((0, 0, 1, 1), 4, 15, 0.25, 3.0, 20)
+    b = gpu.register_bvp(fk.ANISO)
+    out = []
+    for _ in range(2):
+        gpu.set_stream(5)
+        out.append(gpu.assemble(mesh, b, 1000, 5e-4, fk.FP32))
+    assert np.allclose(out[0]["val"], out[1]["val"], rtol=1e-12, atol=1e-14)
+    assert np.allclose(out[0]["B"], out[1]["B"], rtol=1e-12, atol=1e-14)
