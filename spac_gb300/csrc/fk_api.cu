@@ -272,24 +272,35 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   long long total_paths = 0;
   for (auto& x : it) if (!x.frontera) total_paths += x.paths;
   const int block = ctx->block;
-  const size_t sacc_bytes =
-      static_cast<size_t>(acc_words) * ((precision == FK_FP64 || kind == 1) ? sizeof(double) : sizeof(float));
+  int smem_nodes = 0;
+  if (kind != 0)
+    for (auto& x : it)
+      if (x.stencil >= 0) smem_nodes = std::max(smem_nodes, S->size_of(x.stencil));
+  const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes);
+  if (sacc_bytes > 200 * 1024) return fail(ctx, FK_ERR_CAPACITY, "stencil accumulators exceed shared memory");
   const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes);
   const int grid = std::max(1, ctx->num_sms * occ);
+  // Chunk size: at least 4 chunks per CTA of the persistent grid, at most
+  // 32768 paths; an item is split into equal chunks (no small remainder).
   long long chunk = ctx->chunk;
   if (chunk <= 0) {
     chunk = total_paths / (4LL * grid);
-    chunk = std::max<long long>(block, std::min<long long>(chunk, 16384));
-    chunk = (chunk + block - 1) / block * block;
+    chunk = std::max<long long>(block, std::min<long long>(chunk, 32768));
   }
   std::vector<fk::ChunkDev> chunks;
   for (int i = 0; i < n; ++i) {
     if (it[i].frontera || it[i].paths == 0) continue;
-    for (unsigned p0 = 0; p0 < it[i].paths; p0 += static_cast<unsigned>(chunk)) {
-      const unsigned p1 = static_cast<unsigned>(std::min<long long>(it[i].paths, p0 + chunk));
-      chunks.push_back(fk::ChunkDev{i, p0, p1});
+    const long long np = it[i].paths;
+    const long long pieces = (np + chunk - 1) / chunk;
+    const long long per = (np + pieces - 1) / pieces;
+    for (long long p0 = 0; p0 < np; p0 += per) {
+      const long long p1 = std::min<long long>(np, p0 + per);
+      chunks.push_back(fk::ChunkDev{i, static_cast<unsigned>(p0), static_cast<unsigned>(p1)});
     }
   }
+  // longest chunks first (uneven path counts, as in batched solves)
+  std::stable_sort(chunks.begin(), chunks.end(),
+                   [](const fk::ChunkDev& a, const fk::ChunkDev& b) { return (a.p1 - a.p0) > (b.p1 - b.p0); });
   FK_CUDA(fk::upload(ctx->w_items, it, s));
   FK_CUDA(fk::upload(ctx->w_chunks, chunks, s));
   FK_CUDA(ctx->w_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
@@ -317,6 +328,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   a.cv = (bvp.cv == FK_CV_EXACT) ? 1 : 0;
   a.stencil_kind = kind;
   a.acc_words = acc_words;
+  a.smem_nodes = smem_nodes;
   FK_CUDA(cudaEventRecord(ctx->ev[0], s));
   if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s));
   FK_CUDA(cudaEventRecord(ctx->ev[1], s));

@@ -36,11 +36,16 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& z0, d
   z0 = rad * c;
   z1 = rad * s;
 }
+// FP32 stepping uses the SFU forms (ex2/lg2.approx): relative error ~1e-6,
+// far below the Monte Carlo error of any node estimate.
+__device__ __forceinline__ float fexp(float v) { return __expf(v); }
+__device__ __forceinline__ double fexp(double v) { return exp(v); }
+
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
   const float inv32 = 2.3283064365386962890625e-10f;
   const float u1 = (static_cast<float>(a) + 0.5f) * inv32;  // rounds into (0, 1]
   const float u2 = (static_cast<float>(b) + 0.5f) * inv32;
-  const float rad = sqrtf(-2.0f * logf(u1));
+  const float rad = sqrtf(-2.0f * __logf(u1));
   float s, c;
   sincospif(2.0f * u2, &s, &c);
   z0 = rad * c;
@@ -156,10 +161,10 @@ struct FrankeEval {
     q = R(9) * y - R(3);
     r = R(9) * x - R(4);
     t = R(9) * y - R(7);
-    e1 = exp(R(-0.25) * (a * a + b * b));
-    e2 = exp(R(-1.0 / 49.0) * (c * c) - R(0.1) * d);
-    e3 = exp(R(-0.25) * (p * p + q * q));
-    e4 = exp(R(-1) * (r * r + t * t));
+    e1 = fexp(R(-0.25) * (a * a + b * b));
+    e2 = fexp(R(-1.0 / 49.0) * (c * c) - R(0.1) * d);
+    e3 = fexp(R(-0.25) * (p * p + q * q));
+    e4 = fexp(R(-1) * (r * r + t * t));
   }
   __device__ __forceinline__ R u() const { return R(0.75) * e1 + R(0.75) * e2 + R(0.5) * e3 - R(0.2) * e4; }
   __device__ __forceinline__ R ux() const {
@@ -211,6 +216,9 @@ struct MonegrosEval {
   }
 };
 
+// Problem functors.  state(x, y) is what sigma needs at a point (the
+// anisotropy factor a(x, y) of FK_PROBLEM_ANISO; nothing for constant sigma);
+// the exit rule computes it at the new point and the next step reuses it.
 template <int PROB>
 struct Problem;
 
@@ -218,9 +226,11 @@ struct Problem;
 template <>
 struct Problem<0> {
   template <typename R>
-  __device__ static R sigma(const BvpDev&, R, R) { return R(1.41421356237); }
+  __device__ static R state(const BvpDev&, R, R) { return R(0); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, bool cv, StepCoef<R>& o) {
+  __device__ static R sigma_of(R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
     FrankeEval<R> F(x, y);
     o.s = R(1.41421356237);
     o.f = -F.uxx() - F.uyy();
@@ -240,9 +250,11 @@ struct Problem<0> {
 template <>
 struct Problem<1> {
   template <typename R>
-  __device__ static R sigma(const BvpDev&, R, R) { return R(1.41421356237); }
+  __device__ static R state(const BvpDev&, R, R) { return R(0); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, bool cv, StepCoef<R>& o) {
+  __device__ static R sigma_of(R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
     MonegrosEval<R> M(x, y);
     o.s = R(1.41421356237);
     o.c = R(-1);
@@ -266,16 +278,17 @@ struct Problem<2> {
     return R(1) + R(0.5) * sinpi_(R(2) * x) * sinpi_(R(2) * y);
   }
   template <typename R>
-  __device__ static R sigma(const BvpDev&, R x, R y) { return sqrt(R(2) * coef_a(x, y)); }
+  __device__ static R state(const BvpDev&, R x, R y) { return coef_a(x, y); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, bool cv, StepCoef<R>& o) {
+  __device__ static R sigma_of(R a) { return sqrt(R(2) * a); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, R a, bool cv, StepCoef<R>& o) {
     FrankeEval<R> F(x, y);
     const R q = R(1) + x * y;
     const R Fv = F.u(), Fx = F.ux(), Fy = F.uy();
     const R u = Fv * q;
     const R ux = Fx * q + Fv * y, uy = Fy * q + Fv * x;
     const R lap = (F.uxx() + F.uyy()) * q + R(2) * (Fx * y + Fy * x);
-    const R a = coef_a(x, y);
     o.s = sqrt(R(2) * a);
     o.c = -(R(1) + x * x + y * y);
     o.bx = y - R(0.5);
@@ -294,9 +307,11 @@ struct Problem<2> {
 template <>
 struct Problem<3> {
   template <typename R>
-  __device__ static R sigma(const BvpDev&, R, R) { return R(1.41421356237); }
+  __device__ static R state(const BvpDev&, R, R) { return R(0); }
   template <typename R>
-  __device__ static void step(const BvpDev& b, R x, R y, bool cv, StepCoef<R>& o) {
+  __device__ static R sigma_of(R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev& b, R x, R y, R, bool cv, StepCoef<R>& o) {
     const R inv = R(1) / (R(2) * R(b.prob[2]));
     const R xi = (x - R(b.prob[0])) * inv + R(0.5), eta = (y - R(b.prob[1])) * inv + R(0.5);
     FrankeEval<R> F(xi, eta);

@@ -68,6 +68,7 @@ struct LaunchArgs {
   int cv;
   int stencil_kind;        // 0 none, 1 arc, 2 patch
   int acc_words;           // shared accumulator length (elements) per CTA
+  int smem_nodes;          // patch nodes / arc angles staged in shared memory (max over stencils)
   const void* mlp;         // device MLP parameters (FK_CV_MLP)
 };
 
@@ -92,10 +93,12 @@ struct FinalizeArgs {
   double* B;                // may be null
 };
 
-// host launchers (fk_kernels.cu)
+// host launchers (fk_paths.cu)
+size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes);
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block,
                          size_t smem, cudaStream_t s);
 int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem);
+// host launchers (fk_kernels.cu)
 cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s);
 // batched FP64 full-pivot Gauss-Jordan inverse: matrix b is ns[b] x ns[b],
 // column-major at offset offs[b] of A (input) and inv (output); ns[b] <= 64

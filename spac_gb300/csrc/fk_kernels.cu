@@ -1,15 +1,6 @@
 // GB300 (sm_103a) kernels of the Feynman-Kac hot path.
 //
-//  paths_kernel   persistent grid; each CTA takes chunks of one item's paths
-//                 from a global queue, every thread runs one path at a time and
-//                 pulls the next path index of the chunk as soon as its path
-//                 exits (per-lane regeneration: lanes never wait for the
-//                 longest path of a warp).  The exit is processed in place:
-//                 exit value, B and statistics into per-thread registers,
-//                 stencil weights into shared-memory accumulators, flushed to
-//                 FP64 per-item accumulators at the end of the chunk.
-//                 Replaces Simulacion_OMP + Reduce_Analytic + Interfaz::Update_G
-//                 (Solvers/FeynmanKacSolver.cpp:137-292, Mesh/Interfaz.cpp:219-264).
+//  (the path kernel itself is in fk_paths.cu)
 //  finalize_kernel  per item: applies the stencil inverse to the accumulated
 //                 RBF moments (FP64), averages (Update(Nudo&), :324-334) and
 //                 scatters G into the CSR row and B into the right-hand side
@@ -17,231 +8,10 @@
 //  inverse_kernel FP64 Gauss-Jordan with full pivoting, one CTA per matrix,
 //                 non-contracted arithmetic: the same bits as the CPU
 //                 restatement of Eigen::FullPivLU::inverse (Interfaz.cpp:214).
-#include <cfloat>
-#include <type_traits>
-
 #include "fk_device.cuh"
 #include "fk_internal.h"
 
 namespace fk {
-
-// ------------------------------------------------------------ accumulators --
-struct AccD {
-  double s = 0.0;
-  __device__ __forceinline__ void add(double v) { s += v; }
-  __device__ __forceinline__ double get() const { return s; }
-};
-// Compensated (Kahan) FP32 sum for FP32 stepping: FP64-grade sums of a
-// thread's exits without FP64 arithmetic in the path loop.
-struct AccK {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float v) {
-    const float y = v - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  __device__ __forceinline__ double get() const { return static_cast<double>(s) - static_cast<double>(c); }
-};
-
-constexpr int kNumAcc = 11;  // accumulated per thread: see the exit block
-constexpr int kMaxWarps = 32;
-
-template <typename R, int ST>
-struct SAccType {
-  // arc stencils (kappa(Psi) ~ 1e10) always accumulate in FP64
-  using type = typename std::conditional<std::is_same<R, double>::value || ST == 1, double, float>::type;
-};
-
-// Window (first chain index) of the k nearest patch-boundary nodes to an exit
-// point on the patch boundary.  The k nearest nodes of a point on a convex
-// boundary chain are a contiguous run of the chain; start from the run
-// centred on the nearest node of the exit side and slide while an outside
-// neighbour is closer than the opposite end of the run.
-template <typename R>
-__device__ __forceinline__ int knn_window(const PatchDev& P, const double* __restrict__ nodes, R ex, R ey) {
-  int best_s = -1;
-  R best = R(FLT_MAX);
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    if (P.side_count[s] > 0) {
-      const R dist = fabs((P.side_axis[s] == 0 ? ey : ex) - R(P.side_fixed[s]));
-      if (dist < best) { best = dist; best_s = s; }
-    }
-  }
-  const int m = P.m, k = P.k;
-  int nearest = 0;
-  if (best_s >= 0) {
-    const R coord = P.side_axis[best_s] == 0 ? ex : ey;
-    int j = __double2int_rn((static_cast<double>(coord) - P.side_start[best_s]) / P.side_step[best_s]);
-    j = max(0, min(P.side_count[best_s] - 1, j));
-    nearest = P.side_first[best_s] + j;
-  }
-  auto d2 = [&](int idx) -> R {
-    if (P.closed) { idx %= m; if (idx < 0) idx += m; }
-    const R dx = ex - R(nodes[2 * idx]), dy = ey - R(nodes[2 * idx + 1]);
-    return dx * dx + dy * dy;
-  };
-  int L = nearest - k / 2;
-  if (P.closed) {
-    for (int it = 0; it < m && d2(L - 1) < d2(L + k - 1); ++it) --L;
-    for (int it = 0; it < m && d2(L + k) < d2(L); ++it) ++L;
-    L %= m;
-    if (L < 0) L += m;
-  } else {
-    L = max(0, min(m - k, L));
-    while (L > 0 && d2(L - 1) < d2(L + k - 1)) --L;
-    while (L < m - k && d2(L + k) < d2(L)) ++L;
-  }
-  return L;
-}
-
-template <typename R, int PROB, int ST>
-__global__ void __launch_bounds__(256) paths_kernel(const LaunchArgs a) {
-  using SAcc = typename SAccType<R, ST>::type;
-  using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SAcc* sacc = reinterpret_cast<SAcc*>(smem_raw);
-  __shared__ int s_chunk;
-  __shared__ unsigned s_next;
-  __shared__ double s_red[kNumAcc][kMaxWarps];
-
-  const BvpDev bvp = *a.bvp;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const bool cv = a.cv != 0;
-
-  for (;;) {
-    if (threadIdx.x == 0) s_chunk = atomicAdd(a.queue, 1);
-    __syncthreads();
-    const int c = s_chunk;
-    if (c >= a.n_chunks) break;
-    const ChunkDev ch = a.chunks[c];
-    const ItemDev it = a.items[ch.item];
-    for (int i = threadIdx.x; i < a.acc_words; i += blockDim.x) sacc[i] = SAcc(0);
-    if (threadIdx.x == 0) s_next = ch.p0 + blockDim.x;
-    __syncthreads();
-
-    const R h = R(it.h), sqrth = R(it.sqrth), x0 = R(it.x), y0 = R(it.y);
-    const R s0 = R(it.sub[0]), s1 = R(it.sub[1]), s2 = R(it.sub[2]), s3 = R(it.sub[3]);
-    // stencil metadata
-    ArcDev arc;
-    PatchDev patch;
-    const double* theta = nullptr;
-    if (ST == 1) { arc = a.arcs[it.stencil]; theta = a.arc_theta + arc.theta_off; }
-    if (ST == 2) { patch = a.patches[it.stencil]; }
-    const double* pnodes = (ST == 2) ? a.patch_nodes + patch.node_off : nullptr;
-
-    Acc acc[kNumAcc];
-    R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0);
-    int k = 0;
-    uint32_t w2 = 0, w3 = 0;
-    unsigned p = ch.p0 + threadIdx.x;
-
-    while (p < ch.p1) {
-      // ---- one Euler-Maruyama step (Paso_Absorbente, FeynmanKacSolver.cpp:7-18)
-      StepCoef<R> co;
-      Problem<PROB>::step(bvp, x, y, cv, co);
-      uint32_t wa, wb;
-      if ((k & 1) == 0) {
-        const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k >> 1), p, static_cast<uint32_t>(ch.item), a.stream),
-                                 a.key0, a.key1);
-        wa = r.x; wb = r.y; w2 = r.z; w3 = r.w;
-      } else {
-        wa = w2; wb = w3;
-      }
-      R z0, z1;
-      box_muller(wa, wb, z0, z1);
-      const R dWx = sqrth * z0, dWy = sqrth * z1;
-      Z += co.f * Y * h;
-      if (cv) xi += Y * (co.Fx * dWx + co.Fy * dWy);
-      Y += co.c * Y * h;
-      x += co.bx * h + co.s * dWx;
-      y += co.by * h + co.s * dWy;
-      ++k;
-      // ---- exit rule (Dentro, FeynmanKacSolver.cpp:68-106)
-      Bnd<R> w = (PROB == 3) ? circle_dist<R>(x, y, R(bvp.dom[0]), R(bvp.dom[1]), R(bvp.dom[2]))
-                             : rect_dist<R>(x, y, R(bvp.dom[0]), R(bvp.dom[1]), R(bvp.dom[2]), R(bvp.dom[3]));
-      bool dom_wins = true;
-      if (ST != 0 || it.sub_shape >= 0) {
-        const Bnd<R> sb = (ST == 1 || (ST == 0 && it.sub_shape == 1)) ? circle_dist<R>(x, y, s0, s1, s2)
-                                                                       : rect_dist<R>(x, y, s0, s1, s2, s3);
-        if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
-      }
-      const R sg = (w.d < R(0)) ? Problem<PROB>::sigma(bvp, x, y) : Problem<PROB>::sigma(bvp, w.ex, w.ey);
-      const R nsx = w.nx * sg, nsy = w.ny * sg;
-      const R thr = R(kGobet) * sqrt(nsx * nsx + nsy * nsy) * sqrth;
-      const bool capped = k >= a.max_steps;
-      if (!(w.d < thr) || capped) {
-        // ---- exit: Reduce_Analytic (FeynmanKacSolver.cpp:198-292)
-        const R g = Problem<PROB>::u(bvp, w.ex, w.ey);  // g = u for every registered problem
-        const R score = Z + Y * g;
-        const R vr = score + xi;
-        R bpart = vr;
-        if (ST != 0 && !dom_wins) {
-          bpart = Z + xi;
-          if (ST == 1) {
-            // Interfaz::Update_G moments: s_i += Y phi_i(theta), FP64
-            const double th = arc_theta(arc.interior, static_cast<double>(w.ex) - arc.cx,
-                                        static_cast<double>(w.ey) - arc.cy);
-            const double Yd = static_cast<double>(Y);
-            for (int i = 0; i < arc.n; ++i) {
-              const double d = th - theta[i];
-              atomicAdd(reinterpret_cast<double*>(&sacc[i]), Yd / sqrt(d * d + arc.c2));
-            }
-          } else if (ST == 2) {
-            const int L = knn_window<R>(patch, pnodes, w.ex, w.ey);
-            const int m = patch.m, kk = patch.k;
-            const R e2 = R(patch.eps2);
-            for (int q = 0; q < kk; ++q) {
-              int idx = L + q;
-              if (idx >= m) idx -= m;
-              const R dx = w.ex - R(pnodes[2 * idx]), dy = w.ey - R(pnodes[2 * idx + 1]);
-              atomicAdd(&sacc[L * kk + q], static_cast<SAcc>(Y * exp(-e2 * (dx * dx + dy * dy))));
-            }
-          }
-        }
-        acc[0].add(score);
-        acc[1].add(score * score);
-        acc[2].add(xi + xi * xi);
-        acc[3].add(vr);
-        acc[4].add(vr * vr);
-        acc[5].add(xi * score);
-        acc[6].add(R(k));
-        acc[7].add(bpart);
-        acc[8].add(dom_wins ? R(1) : R(0));
-        acc[9].add(capped ? R(1) : R(0));
-        acc[10].add(xi * xi);
-        // regenerate: next path of this chunk
-        p = atomicAdd(&s_next, 1u);
-        x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0;
-      }
-    }
-    // xi (plain sum) is recovered at finalize from slots 2 and 10
-    __syncthreads();
-    // ---- chunk flush: block reduction of the thread sums, FP64 atomics per item
-#pragma unroll
-    for (int j = 0; j < kNumAcc; ++j) {
-      double v = acc[j].get();
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) s_red[j][warp] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kNumAcc) {
-      double v = 0.0;
-      for (int w = 0; w < nwarps; ++w) v += s_red[threadIdx.x][w];
-      if (v != 0.0) atomicAdd(&a.stats[static_cast<long long>(ch.item) * kNumStats + threadIdx.x], v);
-    }
-    if (ST != 0) {
-      double* gacc = a.acc + it.acc_off;
-      for (int i = threadIdx.x; i < a.acc_words; i += blockDim.x) {
-        const double v = static_cast<double>(sacc[i]);
-        if (v != 0.0) atomicAdd(&gacc[i], v);
-      }
-    }
-    __syncthreads();
-  }
-}
 
 // ------------------------------------------------------------- finalize -----
 // fk_stats layout (16 doubles): phi, phiphi, phi_VR, phiphi_VR, xi, xixi,
@@ -451,47 +221,7 @@ __global__ void inverse_kernel(const double* A, double* inv, const int* ns, cons
   for (int e = threadIdx.x; e < nn; e += blockDim.x) Vg[e] = v[e];
 }
 
-// --------------------------------------------------------------- dispatch ---
-template <typename R, int PROB>
-static const void* paths_fn(int st) {
-  switch (st) {
-    case 1: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 1>);
-    case 2: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2>);
-    default: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 0>);
-  }
-}
-template <typename R>
-static const void* paths_fn_r(int problem, int st) {
-  switch (problem) {
-    case 1: return paths_fn<R, 1>(st);
-    case 2: return paths_fn<R, 2>(st);
-    case 3: return paths_fn<R, 3>(st);
-    default: return paths_fn<R, 0>(st);
-  }
-}
-static const void* select_paths(int problem, int precision, int st) {
-  return precision == 1 ? paths_fn_r<float>(problem, st) : paths_fn_r<double>(problem, st);
-}
-
-cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block, size_t smem,
-                         cudaStream_t s) {
-  const void* fn = select_paths(problem, precision, a.stencil_kind);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-  }
-  void* args[] = {const_cast<LaunchArgs*>(&a)};
-  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, s);
-}
-
-int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int, int block, size_t smem) {
-  const void* fn = select_paths(problem, precision, stencil_kind);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 1;
-  return n > 0 ? n : 1;
-}
-
+// --------------------------------------------------------------- launchers --
 cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s) {
   if (a.n_items <= 0) return cudaSuccess;
   const dim3 grid(a.n_items), block(128);

@@ -1,0 +1,362 @@
+// GB300 (sm_103a) path kernel of the Feynman-Kac hot path.
+//
+// Persistent grid.  Each CTA takes chunks of one item's paths from a global
+// queue; every thread runs one path at a time and pulls the next path index
+// of the chunk as soon as its path exits (per-lane regeneration: a lane never
+// waits for the longest path of its warp).  The exit is processed in place:
+//  - scalar part by the exiting lane: exit value u(X_tau), B and the
+//    statistics into per-thread registers (compensated FP32 sums for FP32
+//    stepping, FP64 for FP64 stepping);
+//  - stencil part by the whole warp: each exit is broadcast and the lanes
+//    evaluate the stencil's RBF terms in parallel, adding Y phi into the
+//    chunk's shared-memory moments (FP64 for the arc stencil, whose inverse
+//    has condition ~1e10; FP32 chunk partials for the Gaussian stencil).
+// At the end of a chunk the thread sums are block-reduced and the moments
+// flushed into FP64 per-item accumulators.  On the FP32 path no FP64
+// instruction runs inside the step loop.
+// Replaces Simulacion_OMP + Reduce_Analytic + Interfaz::Update_G
+// (Solvers/FeynmanKacSolver.cpp:137-292, Mesh/Interfaz.cpp:219-264).
+#include <cfloat>
+#include <type_traits>
+
+#include "fk_device.cuh"
+#include "fk_internal.h"
+
+namespace fk {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxWarps = 32;
+constexpr int kNumAcc = 8;   // floating-point sums per thread
+
+struct AccD {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+// Compensated (Kahan) FP32 sum: FP64-grade thread sums without FP64 work.
+struct AccK {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double get() const { return static_cast<double>(s) - static_cast<double>(c); }
+};
+
+template <typename R, int ST>
+struct SAccType {
+  using type = typename std::conditional<std::is_same<R, double>::value || ST == 1, double, float>::type;
+};
+
+// Per-chunk copy of the exit patch in shared memory (stepping precision).
+template <typename R>
+struct PatchSh {
+  int m, k, closed;
+  int side_first[4], side_count[4], side_axis[4];
+  R side_fixed[4], side_start[4], side_inv_step[4];
+  R e2;
+};
+
+// Window (first chain index) of the k nearest patch-boundary nodes to an exit
+// point on the patch boundary.  The k nearest nodes of a point of a convex
+// boundary chain form a contiguous run of the chain: start from the run
+// centred on the nearest node of the exit side, slide while an outside
+// neighbour is closer than the opposite end of the run.
+template <typename R>
+__device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restrict__ nx, const R* __restrict__ ny,
+                                          R ex, R ey) {
+  int best_s = -1;
+  R best = R(FLT_MAX);
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    if (P.side_count[s] > 0) {
+      const R dist = fabs((P.side_axis[s] == 0 ? ey : ex) - P.side_fixed[s]);
+      if (dist < best) { best = dist; best_s = s; }
+    }
+  }
+  const int m = P.m, k = P.k;
+  int nearest = 0;
+  if (best_s >= 0) {
+    const R coord = P.side_axis[best_s] == 0 ? ex : ey;
+    int j = static_cast<int>(rint((coord - P.side_start[best_s]) * P.side_inv_step[best_s]));
+    j = max(0, min(P.side_count[best_s] - 1, j));
+    nearest = P.side_first[best_s] + j;
+  }
+  auto d2 = [&](int idx) -> R {
+    if (idx >= m) idx -= m;
+    if (idx < 0) idx += m;
+    const R dx = ex - nx[idx], dy = ey - ny[idx];
+    return dx * dx + dy * dy;
+  };
+  int L = nearest - k / 2;
+  if (P.closed) {
+    if (L < 0) L += m;
+    for (int it = 0; it < m && d2(L - 1) < d2(L + k - 1); ++it) { --L; if (L < 0) L += m; }
+    for (int it = 0; it < m && d2(L + k) < d2(L); ++it) { ++L; if (L >= m) L -= m; }
+  } else {
+    L = max(0, min(m - k, L));
+    while (L > 0 && d2(L - 1) < d2(L + k - 1)) --L;
+    while (L < m - k && d2(L + k) < d2(L)) ++L;
+  }
+  return L;
+}
+
+template <typename R, int PROB, int ST>
+__global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
+  using SAcc = typename SAccType<R, ST>::type;
+  using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SAcc* sacc = reinterpret_cast<SAcc*>(smem_raw);
+  // after the accumulators: patch nodes (x[], y[]) or arc angles
+  R* snx = reinterpret_cast<R*>(smem_raw + static_cast<size_t>(a.acc_words) * sizeof(SAcc));
+  R* sny = snx + a.smem_nodes;
+  double* sth = reinterpret_cast<double*>(smem_raw + static_cast<size_t>(a.acc_words) * sizeof(SAcc));
+  __shared__ int s_chunk;
+  __shared__ unsigned s_next;
+  __shared__ double s_red[kNumAcc + 3][kMaxWarps];
+  __shared__ PatchSh<R> sp;
+  __shared__ ArcDev sarc;
+
+  const BvpDev& bvp = *a.bvp;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const bool cv = a.cv != 0;
+  const R d0 = R(bvp.dom[0]), d1 = R(bvp.dom[1]), d2 = R(bvp.dom[2]), d3 = R(bvp.dom[3]);
+
+  for (;;) {
+    if (threadIdx.x == 0) s_chunk = atomicAdd(a.queue, 1);
+    __syncthreads();
+    const int c = s_chunk;
+    if (c >= a.n_chunks) break;
+    const ChunkDev ch = a.chunks[c];
+    const ItemDev& itg = a.items[ch.item];
+    for (int i = threadIdx.x; i < a.acc_words; i += blockDim.x) sacc[i] = SAcc(0);
+    if (ST == 2) {
+      const PatchDev& P = a.patches[itg.stencil];
+      const double* nd = a.patch_nodes + P.node_off;
+      for (int i = threadIdx.x; i < P.m; i += blockDim.x) { snx[i] = R(nd[2 * i]); sny[i] = R(nd[2 * i + 1]); }
+      if (threadIdx.x == 0) {
+        sp.m = P.m; sp.k = P.k; sp.closed = P.closed; sp.e2 = R(P.eps2);
+        for (int s = 0; s < 4; ++s) {
+          sp.side_first[s] = P.side_first[s]; sp.side_count[s] = P.side_count[s]; sp.side_axis[s] = P.side_axis[s];
+          sp.side_fixed[s] = R(P.side_fixed[s]); sp.side_start[s] = R(P.side_start[s]);
+          sp.side_inv_step[s] = R(1.0 / P.side_step[s]);
+        }
+      }
+    }
+    if (ST == 1) {
+      const ArcDev& A = a.arcs[itg.stencil];
+      for (int i = threadIdx.x; i < A.n; i += blockDim.x) sth[i] = a.arc_theta[A.theta_off + i];
+      if (threadIdx.x == 0) sarc = A;
+    }
+    if (threadIdx.x == 0) s_next = ch.p0 + blockDim.x;
+    __syncthreads();
+
+    const R h = R(itg.h), sqrth = R(itg.sqrth), x0 = R(itg.x), y0 = R(itg.y);
+    const R s0 = R(itg.sub[0]), s1 = R(itg.sub[1]), s2 = R(itg.sub[2]), s3 = R(itg.sub[3]);
+    const bool has_sub = (ST != 0) || itg.sub_shape >= 0;
+    const bool sub_circle = (ST == 1) || (ST == 0 && itg.sub_shape == 1);
+    const R st0 = Problem<PROB>::template state<R>(bvp, x0, y0);  // sigma state at the start point
+    const uint32_t item = static_cast<uint32_t>(ch.item);
+
+    Acc acc[kNumAcc];
+    unsigned n_steps = 0, n_dom = 0, n_cap = 0;
+    R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0;
+    int k = 0;
+    uint32_t w2 = 0, w3 = 0;
+    unsigned p = ch.p0 + threadIdx.x;
+    bool active = p < ch.p1;
+
+    while (__any_sync(kFull, active)) {
+      bool exits = false, dom_wins = true;
+      R ex = R(0), ey = R(0);
+      if (active) {
+        // ---- one Euler-Maruyama step (Paso_Absorbente, FeynmanKacSolver.cpp:7-18)
+        StepCoef<R> co;
+        Problem<PROB>::step(bvp, x, y, st, cv, co);
+        uint32_t wa, wb;
+        if ((k & 1) == 0) {
+          const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k >> 1), p, item, a.stream), a.key0, a.key1);
+          wa = r.x; wb = r.y; w2 = r.z; w3 = r.w;
+        } else {
+          wa = w2; wb = w3;
+        }
+        R z0, z1;
+        box_muller(wa, wb, z0, z1);
+        const R dWx = sqrth * z0, dWy = sqrth * z1;
+        Z += co.f * Y * h;
+        if (cv) xi += Y * (co.Fx * dWx + co.Fy * dWy);
+        Y += co.c * Y * h;
+        x += co.bx * h + co.s * dWx;
+        y += co.by * h + co.s * dWy;
+        ++k;
+        // ---- exit rule (Dentro, FeynmanKacSolver.cpp:68-106)
+        Bnd<R> w = (PROB == 3) ? circle_dist<R>(x, y, d0, d1, d2) : rect_dist<R>(x, y, d0, d1, d2, d3);
+        if (has_sub) {
+          const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
+          if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
+        }
+        // sigma at the new point (kept for the next step) or at the projection
+        R sg;
+        if (w.d < R(0)) {
+          st = Problem<PROB>::template state<R>(bvp, x, y);
+          sg = Problem<PROB>::template sigma_of<R>(st);
+        } else {
+          sg = Problem<PROB>::template sigma_of<R>(Problem<PROB>::template state<R>(bvp, w.ex, w.ey));
+        }
+        const R nsx = w.nx * sg, nsy = w.ny * sg;
+        const R thr = R(kGobet) * sqrt(nsx * nsx + nsy * nsy) * sqrth;
+        const bool capped = k >= a.max_steps;
+        exits = !(w.d < thr) || capped;
+        if (exits) {
+          // ---- exit value and statistics (Reduce_Analytic, FeynmanKacSolver.cpp:198-292)
+          ex = w.ex;
+          ey = w.ey;
+          const R g = Problem<PROB>::u(bvp, ex, ey);  // g = u for every registered problem
+          const R score = Z + Y * g;
+          const R vr = score + xi;
+          const R bpart = (ST != 0 && !dom_wins) ? Z + xi : vr;
+          acc[0].add(score);
+          acc[1].add(score * score);
+          acc[2].add(xi + xi * xi);
+          acc[3].add(vr);
+          acc[4].add(vr * vr);
+          acc[5].add(xi * score);
+          acc[6].add(bpart);
+          acc[7].add(xi * xi);
+          n_steps += static_cast<unsigned>(k);
+          n_dom += dom_wins ? 1u : 0u;
+          n_cap += capped ? 1u : 0u;
+        }
+      }
+      // ---- stencil moments, one exit at a time across the warp
+      if (ST != 0) {
+        unsigned em = __ballot_sync(kFull, exits && !dom_wins);
+        if (ST == 2) {
+          const int kk = sp.k, m = sp.m;
+          int L = 0;
+          if (exits && !dom_wins) L = knn_window<R>(sp, snx, sny, ex, ey);
+          while (em) {
+            const int src = __ffs(em) - 1;
+            em &= em - 1;
+            const int Lb = __shfl_sync(kFull, L, src);
+            const R xb = __shfl_sync(kFull, ex, src), yb = __shfl_sync(kFull, ey, src), Yb = __shfl_sync(kFull, Y, src);
+            if (lane < kk) {
+              int idx = Lb + lane;
+              if (idx >= m) idx -= m;
+              const R dx = xb - snx[idx], dy = yb - sny[idx];
+              atomicAdd(&sacc[Lb * kk + lane], static_cast<SAcc>(Yb * fexp(-sp.e2 * (dx * dx + dy * dy))));
+            }
+          }
+        } else {
+          // Interfaz::Update_G moments s_i += Y phi_i(theta), FP64
+          double th = 0.0;
+          if (exits && !dom_wins)
+            th = arc_theta(sarc.interior, static_cast<double>(ex) - sarc.cx, static_cast<double>(ey) - sarc.cy);
+          const int n = sarc.n;
+          const double c2 = sarc.c2;
+          while (em) {
+            const int src = __ffs(em) - 1;
+            em &= em - 1;
+            const double tb = __shfl_sync(kFull, th, src);
+            const double Yb = static_cast<double>(__shfl_sync(kFull, Y, src));
+            for (int i = lane; i < n; i += 32) {
+              const double d = tb - sth[i];
+              atomicAdd(reinterpret_cast<double*>(&sacc[i]), Yb / sqrt(d * d + c2));
+            }
+          }
+        }
+      }
+      if (exits) {
+        // regenerate: next path of this chunk
+        p = atomicAdd(&s_next, 1u);
+        active = p < ch.p1;
+        x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0; st = st0;
+      }
+    }
+    __syncthreads();
+    // ---- chunk flush: block reduction of the thread sums, FP64 atomics per item
+    double v[kNumAcc + 3];
+#pragma unroll
+    for (int j = 0; j < kNumAcc; ++j) v[j] = acc[j].get();
+    v[kNumAcc] = static_cast<double>(n_steps);
+    v[kNumAcc + 1] = static_cast<double>(n_dom);
+    v[kNumAcc + 2] = static_cast<double>(n_cap);
+#pragma unroll
+    for (int j = 0; j < kNumAcc + 3; ++j) {
+      double t = v[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+      if (lane == 0) s_red[j][warp] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumAcc + 3) {
+      double t = 0.0;
+      for (int w = 0; w < nwarps; ++w) t += s_red[threadIdx.x][w];
+      // slot layout of kStat*: score, score^2, xi+xi^2, vr, vr^2, xi score, steps, B, dom, cap, xi^2
+      const int slot_of[kNumAcc + 3] = {kStatScore, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScore,
+                                        kStatB, kStatXi2, kStatSteps, kStatDom, kStatCap};
+      if (t != 0.0) atomicAdd(&a.stats[static_cast<long long>(ch.item) * kNumStats + slot_of[threadIdx.x]], t);
+    }
+    if (ST != 0) {
+      double* gacc = a.acc + itg.acc_off;
+      for (int i = threadIdx.x; i < a.acc_words; i += blockDim.x) {
+        const double t = static_cast<double>(sacc[i]);
+        if (t != 0.0) atomicAdd(&gacc[i], t);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename R, int PROB>
+const void* paths_fn(int st) {
+  switch (st) {
+    case 1: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 1>);
+    case 2: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2>);
+    default: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 0>);
+  }
+}
+template <typename R>
+const void* paths_fn_r(int problem, int st) {
+  switch (problem) {
+    case 1: return paths_fn<R, 1>(st);
+    case 2: return paths_fn<R, 2>(st);
+    case 3: return paths_fn<R, 3>(st);
+    default: return paths_fn<R, 0>(st);
+  }
+}
+const void* select_paths(int problem, int precision, int st) {
+  return precision == 1 ? paths_fn_r<float>(problem, st) : paths_fn_r<double>(problem, st);
+}
+
+}  // namespace
+
+size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes) {
+  const size_t acc = static_cast<size_t>(acc_words) * ((precision == 0 || stencil_kind == 1) ? 8 : 4);
+  if (stencil_kind == 2) return acc + 2ull * smem_nodes * (precision == 0 ? 8 : 4);
+  if (stencil_kind == 1) return acc + static_cast<size_t>(smem_nodes) * 8;
+  return acc;
+}
+
+cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block, size_t smem,
+                         cudaStream_t s) {
+  const void* fn = select_paths(problem, precision, a.stencil_kind);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<LaunchArgs*>(&a)};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, s);
+}
+
+int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int, int block, size_t smem) {
+  const void* fn = select_paths(problem, precision, stencil_kind);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+}  // namespace fk
