@@ -434,7 +434,7 @@ const char* fk_last_error(const fk_ctx* ctx) { return ctx ? ctx->err.c_str() : "
 int fk_set_stream(fk_ctx* ctx, unsigned id) { if (!ctx) return FK_ERR_ARG; ctx->stream_id = id; return FK_OK; }
 int fk_get_stream(const fk_ctx* ctx, unsigned* id) { if (!ctx || !id) return FK_ERR_ARG; *id = ctx->stream_id; return FK_OK; }
 int fk_set_max_steps(fk_ctx* ctx, int m) {
-  if (!ctx || m < 1) return fail(ctx, FK_ERR_ARG, "max_steps must be >= 1");
+  if (!ctx || m < 1 || m > (1 << 30)) return fail(ctx, FK_ERR_ARG, "max_steps must be in [1, 2^30]");
   ctx->max_steps = m;
   return FK_OK;
 }

@@ -47,7 +47,7 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, fl
   const float u2 = (static_cast<float>(b) + 0.5f) * inv32;
   const float rad = sqrtf(-2.0f * __logf(u1));
   float s, c;
-  sincospif(2.0f * u2, &s, &c);
+  __sincosf(6.28318530717958647692f * u2, &s, &c);
   z0 = rad * c;
   z1 = rad * s;
 }
@@ -184,7 +184,8 @@ struct FrankeEval {
   }
 };
 
-__device__ __forceinline__ float sinpi_(float v) { return sinpif(v); }
+// sin(pi v): SFU form for FP32 stepping (|v| <= 2 here), accurate for FP64
+__device__ __forceinline__ float sinpi_(float v) { return __sinf(3.14159265358979323846f * v); }
 __device__ __forceinline__ double sinpi_(double v) { return sinpi(v); }
 
 // Monegros with c = -1 (BVPs/Monegros_Revamped.hpp:4-75).

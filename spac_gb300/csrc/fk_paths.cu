@@ -3,14 +3,16 @@
 // Persistent grid.  Each CTA takes chunks of one item's paths from a global
 // queue; every thread runs one path at a time and pulls the next path index
 // of the chunk as soon as its path exits (per-lane regeneration: a lane never
-// waits for the longest path of its warp).  The exit is processed in place:
-//  - scalar part by the exiting lane: exit value u(X_tau), B and the
-//    statistics into per-thread registers (compensated FP32 sums for FP32
-//    stepping, FP64 for FP64 stepping);
-//  - stencil part by the whole warp: each exit is broadcast and the lanes
-//    evaluate the stencil's RBF terms in parallel, adding Y phi into the
-//    chunk's shared-memory moments (FP64 for the arc stencil, whose inverse
-//    has condition ~1e10; FP32 chunk partials for the Gaussian stencil).
+// waits for the longest path of its warp).  An exiting lane only pushes its
+// exit (X_tau, Y, Z, xi, steps, flags) onto its warp's shared-memory queue and
+// starts the next path; once 32 exits are queued the whole warp processes
+// them, one exit per lane, so the exit work runs at full SIMD width:
+//  - exit value u(X_tau), B and the statistics into per-thread registers
+//    (compensated FP32 sums for FP32 stepping, FP64 for FP64 stepping);
+//  - the stencil moments Y phi of subdomain exits into the chunk's
+//    shared-memory accumulators (FP64 for the arc stencil, whose inverse has
+//    condition ~1e10, with lanes over the arc nodes; FP32 chunk partials for
+//    the Gaussian k-nearest stencil, one exit and its window per lane).
 // At the end of a chunk the thread sums are block-reduced and the moments
 // flushed into FP64 per-item accumulators.  On the FP32 path no FP64
 // instruction runs inside the step loop.
@@ -50,6 +52,15 @@ struct AccK {
 template <typename R, int ST>
 struct SAccType {
   using type = typename std::conditional<std::is_same<R, double>::value || ST == 1, double, float>::type;
+};
+
+// Per-warp queue of exits awaiting processing (exit point, Y, Z, xi, and
+// steps | domain-exit << 30 | capped << 31); at most 31 + 32 entries.
+constexpr int kMaxBlockWarps = 8;
+template <typename R>
+struct ExitQueue {
+  R x[64], y[64], Y[64], Z[64], xi[64];
+  unsigned kf[64];
 };
 
 // Per-chunk copy of the exit patch in shared memory (stepping precision).
@@ -120,6 +131,7 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
   __shared__ double s_red[kNumAcc + 3][kMaxWarps];
   __shared__ PatchSh<R> sp;
   __shared__ ArcDev sarc;
+  __shared__ ExitQueue<R> sq[kMaxBlockWarps];
 
   const BvpDev& bvp = *a.bvp;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -169,9 +181,76 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
     uint32_t w2 = 0, w3 = 0;
     unsigned p = ch.p0 + threadIdx.x;
     bool active = p < ch.p1;
+    ExitQueue<R>& q = sq[warp];
+    int qn = 0;  // queued exits of this warp (warp-uniform)
+
+    // Processes the top `cnt` (<= 32) queued exits, one per lane: exit value
+    // and statistics (Reduce_Analytic, FeynmanKacSolver.cpp:198-292) and the
+    // stencil moments of subdomain exits.
+    auto process = [&](int cnt) {
+      const int base = qn - cnt;
+      const bool mine = lane < cnt;
+      R ex = R(0), ey = R(0), Yv = R(0);
+      bool sub_exit = false;
+      if (mine) {
+        const int e = base + lane;
+        ex = q.x[e]; ey = q.y[e]; Yv = q.Y[e];
+        const R Zv = q.Z[e], xv = q.xi[e];
+        const unsigned kf = q.kf[e];
+        const bool dw = (kf >> 30) & 1u, cp = (kf >> 31) & 1u;
+        sub_exit = (ST != 0) && !dw;
+        const R g = Problem<PROB>::u(bvp, ex, ey);  // g = u for every registered problem
+        const R score = Zv + Yv * g;
+        const R vr = score + xv;
+        acc[0].add(score);
+        acc[1].add(score * score);
+        acc[2].add(xv + xv * xv);
+        acc[3].add(vr);
+        acc[4].add(vr * vr);
+        acc[5].add(xv * score);
+        acc[6].add(sub_exit ? Zv + xv : vr);
+        acc[7].add(xv * xv);
+        n_steps += kf & 0x3fffffffu;
+        n_dom += dw ? 1u : 0u;
+        n_cap += cp ? 1u : 0u;
+      }
+      if (ST == 2) {
+        if (sub_exit) {
+          // Gaussian k-nearest moments t_W[j] += Y phi_j, one exit per lane
+          const int L = knn_window<R>(sp, snx, sny, ex, ey);
+          const int kk = sp.k, m = sp.m;
+          const R e2 = sp.e2;
+          for (int j = 0; j < kk; ++j) {
+            int idx = L + j;
+            if (idx >= m) idx -= m;
+            const R dx = ex - snx[idx], dy = ey - sny[idx];
+            atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(Yv * fexp(-e2 * (dx * dx + dy * dy))));
+          }
+        }
+      } else if (ST == 1) {
+        // Interfaz::Update_G moments s_i += Y phi_i(theta), FP64, lanes over i
+        double th = 0.0;
+        if (sub_exit)
+          th = arc_theta(sarc.interior, static_cast<double>(ex) - sarc.cx, static_cast<double>(ey) - sarc.cy);
+        unsigned em = __ballot_sync(kFull, sub_exit);
+        const int n = sarc.n;
+        const double c2 = sarc.c2;
+        while (em) {
+          const int src = __ffs(em) - 1;
+          em &= em - 1;
+          const double tb = __shfl_sync(kFull, th, src);
+          const double Yb = static_cast<double>(__shfl_sync(kFull, Yv, src));
+          for (int i = lane; i < n; i += 32) {
+            const double d = tb - sth[i];
+            atomicAdd(reinterpret_cast<double*>(&sacc[i]), Yb / sqrt(d * d + c2));
+          }
+        }
+      }
+      qn = base;
+    };
 
     while (__any_sync(kFull, active)) {
-      bool exits = false, dom_wins = true;
+      bool exits = false, dom_wins = true, capped = false;
       R ex = R(0), ey = R(0);
       if (active) {
         // ---- one Euler-Maruyama step (Paso_Absorbente, FeynmanKacSolver.cpp:7-18)
@@ -209,74 +288,29 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
         }
         const R nsx = w.nx * sg, nsy = w.ny * sg;
         const R thr = R(kGobet) * sqrt(nsx * nsx + nsy * nsy) * sqrth;
-        const bool capped = k >= a.max_steps;
+        capped = k >= a.max_steps;
         exits = !(w.d < thr) || capped;
-        if (exits) {
-          // ---- exit value and statistics (Reduce_Analytic, FeynmanKacSolver.cpp:198-292)
-          ex = w.ex;
-          ey = w.ey;
-          const R g = Problem<PROB>::u(bvp, ex, ey);  // g = u for every registered problem
-          const R score = Z + Y * g;
-          const R vr = score + xi;
-          const R bpart = (ST != 0 && !dom_wins) ? Z + xi : vr;
-          acc[0].add(score);
-          acc[1].add(score * score);
-          acc[2].add(xi + xi * xi);
-          acc[3].add(vr);
-          acc[4].add(vr * vr);
-          acc[5].add(xi * score);
-          acc[6].add(bpart);
-          acc[7].add(xi * xi);
-          n_steps += static_cast<unsigned>(k);
-          n_dom += dom_wins ? 1u : 0u;
-          n_cap += capped ? 1u : 0u;
-        }
+        ex = w.ex;
+        ey = w.ey;
       }
-      // ---- stencil moments, one exit at a time across the warp
-      if (ST != 0) {
-        unsigned em = __ballot_sync(kFull, exits && !dom_wins);
-        if (ST == 2) {
-          const int kk = sp.k, m = sp.m;
-          int L = 0;
-          if (exits && !dom_wins) L = knn_window<R>(sp, snx, sny, ex, ey);
-          while (em) {
-            const int src = __ffs(em) - 1;
-            em &= em - 1;
-            const int Lb = __shfl_sync(kFull, L, src);
-            const R xb = __shfl_sync(kFull, ex, src), yb = __shfl_sync(kFull, ey, src), Yb = __shfl_sync(kFull, Y, src);
-            if (lane < kk) {
-              int idx = Lb + lane;
-              if (idx >= m) idx -= m;
-              const R dx = xb - snx[idx], dy = yb - sny[idx];
-              atomicAdd(&sacc[Lb * kk + lane], static_cast<SAcc>(Yb * fexp(-sp.e2 * (dx * dx + dy * dy))));
-            }
-          }
-        } else {
-          // Interfaz::Update_G moments s_i += Y phi_i(theta), FP64
-          double th = 0.0;
-          if (exits && !dom_wins)
-            th = arc_theta(sarc.interior, static_cast<double>(ex) - sarc.cx, static_cast<double>(ey) - sarc.cy);
-          const int n = sarc.n;
-          const double c2 = sarc.c2;
-          while (em) {
-            const int src = __ffs(em) - 1;
-            em &= em - 1;
-            const double tb = __shfl_sync(kFull, th, src);
-            const double Yb = static_cast<double>(__shfl_sync(kFull, Y, src));
-            for (int i = lane; i < n; i += 32) {
-              const double d = tb - sth[i];
-              atomicAdd(reinterpret_cast<double*>(&sacc[i]), Yb / sqrt(d * d + c2));
-            }
-          }
-        }
-      }
+      // ---- queue the exits; the exiting lanes start their next path at once
+      const unsigned em = __ballot_sync(kFull, exits);
       if (exits) {
-        // regenerate: next path of this chunk
+        const int e = qn + __popc(em & ((1u << lane) - 1u));
+        q.x[e] = ex; q.y[e] = ey; q.Y[e] = Y; q.Z[e] = Z; q.xi[e] = xi;
+        q.kf[e] = static_cast<unsigned>(k) | (dom_wins ? 1u << 30 : 0u) | (capped ? 1u << 31 : 0u);
         p = atomicAdd(&s_next, 1u);
         active = p < ch.p1;
         x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0; st = st0;
       }
+      qn += __popc(em);
+      __syncwarp();
+      if (qn >= 32) {
+        process(32);
+        __syncwarp();
+      }
     }
+    if (qn > 0) process(qn);
     __syncthreads();
     // ---- chunk flush: block reduction of the thread sums, FP64 atomics per item
     double v[kNumAcc + 3];
