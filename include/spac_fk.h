@@ -129,6 +129,27 @@ int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsi
                     const double* h, const int* sub_shape, const double* sub_params,
                     int precision, fk_stats* out);
 
+/* ---- point solves without any allocation ----------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they solve: code running during CUDA stream capture, embedders
+ * that reserve all device memory up front and forbid later allocations, and
+ * real-time hosts that cannot afford an allocation's latency.  Same kernels
+ * and random stream as fk_solve_points (point i, path p uses the Philox
+ * counter (step/2, p, i, stream_id) under key seed); no fk_ctx is needed.
+ * d_xy (2n doubles), d_paths (n), d_h (n) and d_out (n fk_stats) are device
+ * buffers owned by the caller; launches go on `cuda_stream` (a cudaStream_t,
+ * NULL = default stream) of the current device and are not synchronised.
+ * Scratch memory is one 4 MiB static device array per GPU that loads the
+ * library, held until the process exits; n > FK_NOALLOC_MAX_POINTS returns
+ * FK_ERR_CAPACITY.  The first call on a device looks up the array's device
+ * address (make it before any stream capture).  All calls share the array:
+ * calls whose kernels overlap on the GPU race and give wrong results.
+ * Capped paths are reported in d_out[i].n_capped (no error code). */
+#define FK_NOALLOC_MAX_POINTS 16384
+int fk_solve_points_noalloc(const fk_bvp_desc* bvp, unsigned long long seed, unsigned stream_id, int n,
+                            const double* d_xy, const unsigned* d_paths, const double* d_h, int precision,
+                            int max_steps, void* cuda_stream, fk_stats* d_out);
+
 /* ---- node solves on reference arcs --------------------------------------- */
 int fk_register_arc(fk_ctx* ctx, const fk_arc_desc* arc, int* arc_id);
 /* the arc's iPsi as used by the kernels (n*n column-major) */

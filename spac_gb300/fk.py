@@ -93,6 +93,8 @@ _SIGS = {
                                C.c_ulonglong, _fp]),
     "fk_mlp_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
     "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
+    "fk_solve_points_noalloc": (C.c_int, [C.POINTER(BvpDesc), C.c_ulonglong, C.c_uint, C.c_int, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
 }
 
 
