@@ -196,23 +196,36 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
                 double h, int precision, double* val, double* B, double* item_G, double* item_B,
                 fk_stats* item_stats);
 
-/* ---- learned control variate: MLP 2 -> W -> W -> W -> 1 (SiLU), BF16 weights,
- *      FP32 master copy, trained by the library's own kernels ------------- */
-int fk_mlp_create(fk_ctx* ctx, int width, const double in_lo[2], const double in_scale[2],
-                  unsigned long long init_seed, int* mlp_id);
-/* parameters packed W1(Wx2),b1,W2(WxW),b2,W3(WxW),b3,W4(1xW),b4 (row-major, FP32 master) */
+/* ---- learned control variate ---------------------------------------------
+ * No counterpart in the reference (its control-variate hook is the field F of
+ * the BVP, Coeficiente_Vectorial F, set to -sigma^T grad u by hand).  One MLP
+ * 2 -> 64 -> 64 -> 64 -> 1 (SiLU) per region, input mapped from the region's
+ * rectangle to [-1,1]^2; BF16 weights on the tensor cores, FP32 accumulate,
+ * FP32 master copy updated by Adam.  A BVP registered with cv = FK_CV_MLP and
+ * mlp_id uses F = -sigma^T grad u_hat, where grad u_hat is tabulated on a
+ * grid per region (fk_mlp_build_table) and interpolated bilinearly at every
+ * step; paths of mesh items use the region of their stencil when the network
+ * has one region per stencil, region 0 otherwise. */
+int fk_mlp_create(fk_ctx* ctx, int n_regions, const double* region_rects, unsigned long long init_seed,
+                  int* mlp_id);
+/* parameters per region, packed W1(64x2),b1,W2(64x64),b2,W3(64x64),b3,W4(1x64),b4, row-major FP32;
+ * get/set move all regions ([n_regions][n]) */
 int fk_mlp_num_params(fk_ctx* ctx, int mlp_id, int* n);
 int fk_mlp_get_params(fk_ctx* ctx, int mlp_id, float* params);
 int fk_mlp_set_params(fk_ctx* ctx, int mlp_id, const float* params);
-/* Adam training on (xy, target): steps, batch, learning rate; loss history
- * (may be NULL, length steps). */
-int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, int steps,
-                 int batch, double lr, unsigned long long shuffle_seed, float* loss_history);
+/* Adam on mean((u_hat - target)^2): every step draws `batch` samples (a
+ * multiple of 128) per region with replacement (Philox, shuffle_seed) from
+ * the samples of that region (region[i], NULL = region 0).  loss_history
+ * (length steps, may be NULL) receives the mean batch loss of each step. */
+int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, const int* region,
+                 int steps, int batch, double lr, unsigned long long shuffle_seed, float* loss_history);
 /* forward + input gradient at n points: out[3*n] = (u_hat, du/dx, du/dy) */
-int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, double* out);
-/* loss and parameter gradient of mean((u_hat - target)^2) on a batch (FP32 grad) */
+int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, const int* region, double* out);
+/* loss and parameter gradient of mean((u_hat - target)^2) over all n samples, region 0 (FP32 grad) */
 int fk_mlp_loss_grad(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target,
                      double* loss, float* grad);
+/* tabulates grad u_hat on a grid x grid lattice of every region (used by FK_CV_MLP solves) */
+int fk_mlp_build_table(fk_ctx* ctx, int mlp_id, int grid);
 
 #ifdef __cplusplus
 }

@@ -260,7 +260,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   std::vector<fk::ItemDev> it = items;
   long long acc_total = 0;
   int acc_words = 0;
+  // learned control variate: one network region per stencil, or region 0
+  int n_stencils = 0;
+  if (S) n_stencils = static_cast<int>(S->kind == 1 ? S->arcs.size() : S->patches.size());
+  const bool per_stencil = bvp.cv == FK_CV_MLP && n_stencils > 0 && ctx->mlps[bvp.mlp]->n_regions == n_stencils;
   for (auto& x : it) {
+    x.cv_region = (per_stencil && x.stencil >= 0) ? x.stencil : 0;
     x.acc_off = acc_total;
     if (kind != 0 && x.stencil >= 0) {
       const long long w = S->acc_of(x.stencil);
@@ -326,6 +331,14 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   a.stream = ctx->stream_id;
   a.max_steps = ctx->max_steps;
   a.cv = (bvp.cv == FK_CV_EXACT) ? 1 : 0;
+  if (bvp.cv == FK_CV_MLP) {
+    const fk::Mlp& M = *ctx->mlps[bvp.mlp];
+    if (M.table_grid < 2 || !M.d_table) return fail(ctx, FK_ERR_ARG, "learned control variate: build its table first");
+    a.cv = 2;
+    a.cv_tab = M.d_table;
+    a.cv_rect = M.d_rect;
+    a.cv_grid = M.table_grid;
+  }
   a.stencil_kind = kind;
   a.acc_words = acc_words;
   a.smem_nodes = smem_nodes;
@@ -782,4 +795,83 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   return FK_OK;
 }
 
+// ---- learned control variate ------------------------------------------------
+static fk::Mlp* get_mlp(fk_ctx* ctx, int id) {
+  if (!ctx || id < 0 || id >= static_cast<int>(ctx->mlps.size())) return nullptr;
+  return ctx->mlps[id].get();
+}
+
+int fk_mlp_create(fk_ctx* ctx, int n_regions, const double* rects, unsigned long long seed, int* mlp_id) {
+  if (!ctx || !rects || !mlp_id || n_regions < 1) return fail(ctx, FK_ERR_ARG, "mlp: need >= 1 region rectangle");
+  int rc = need_device(ctx);
+  if (rc) return rc;
+  std::unique_ptr<fk::Mlp> M(new fk::Mlp());
+  rc = fk::mlp_init(*M, n_regions, rects, seed, ctx->err);
+  if (rc) return rc;
+  ctx->mlps.push_back(std::move(M));
+  *mlp_id = static_cast<int>(ctx->mlps.size()) - 1;
+  return FK_OK;
+}
+
+int fk_mlp_num_params(fk_ctx* ctx, int mlp_id, int* n) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M || !n) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  *n = fk::mlp_nparam();
+  return FK_OK;
+}
+
+int fk_mlp_get_params(fk_ctx* ctx, int mlp_id, float* params) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M || !params) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  cudaSetDevice(ctx->device);
+  FK_CUDA(cudaMemcpy(params, M->d_master, sizeof(float) * M->n_regions * fk::mlp_nparam(), cudaMemcpyDeviceToHost));
+  return FK_OK;
+}
+
+int fk_mlp_set_params(fk_ctx* ctx, int mlp_id, const float* params) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M || !params) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  cudaSetDevice(ctx->device);
+  const int rc = fk::mlp_set_params(*M, params);
+  if (rc) return fail(ctx, rc, "mlp: set params failed");
+  M->table_grid = 0;  // the gradient table is stale
+  return FK_OK;
+}
+
+int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, const int* region,
+                 int steps, int batch, double lr, unsigned long long seed, float* loss_history) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  if (n < 1 || !xy || !target || !(lr > 0)) return fail(ctx, FK_ERR_ARG, "mlp train: need samples and lr > 0");
+  cudaSetDevice(ctx->device);
+  const int rc = fk::mlp_train(*M, n, xy, target, region, steps, batch, lr, seed, loss_history, ctx->stream, ctx->err);
+  if (rc == FK_OK) M->table_grid = 0;
+  return rc;
+}
+
+int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, const int* region, double* out) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  if (n < 0 || (n > 0 && (!xy || !out))) return fail(ctx, FK_ERR_ARG, "null argument");
+  cudaSetDevice(ctx->device);
+  return fk::mlp_eval_host(*M, n, xy, region, out, ctx->stream, ctx->err);
+}
+
+int fk_mlp_loss_grad(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, double* loss,
+                     float* grad) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  if (n < 1 || !xy || !target || !loss || !grad) return fail(ctx, FK_ERR_ARG, "null argument");
+  cudaSetDevice(ctx->device);
+  return fk::mlp_loss_grad(*M, n, xy, target, loss, grad, ctx->stream, ctx->err);
+}
+
+int fk_mlp_build_table(fk_ctx* ctx, int mlp_id, int grid) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  cudaSetDevice(ctx->device);
+  return fk::mlp_build_table(*M, grid, ctx->stream, ctx->err);
+}
+
 }  // extern "C"
+

@@ -17,6 +17,8 @@ struct ItemDev {
   int stencil;            // arc / patch index, -1 for point solves
   int frontera;           // B = g(x), no paths
   int sub_shape;          // point solves: 0 rect, 1 circle, -1 = domain
+  int cv_region;          // learned control variate: region of the grad table
+  int pad_;
   long long acc_off;      // first double of this item's stencil accumulator
 };
 
@@ -65,7 +67,10 @@ struct LaunchArgs {
   double* acc;             // stencil accumulators
   uint32_t key0, key1, stream;
   int max_steps;
-  int cv;
+  int cv;                  // 0 none, 1 exact gradient functor, 2 learned (gradient table)
+  const float2* cv_tab;    // [regions][grid][grid] grad u_hat
+  const double* cv_rect;   // 4 per region
+  int cv_grid;
   int stencil_kind;        // 0 none, 1 arc, 2 patch
   int acc_words;           // shared accumulator length (elements) per CTA
   int smem_nodes;          // patch nodes / arc angles staged in shared memory (max over stencils)

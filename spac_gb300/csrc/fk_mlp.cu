@@ -1,24 +1,746 @@
-// Learned control variate (MLP) -- C ABI entry points.
+// Learned control variate: MLP 2 -> 64 -> 64 -> 64 -> 1 (SiLU), one network
+// per region (a patch or the whole domain), trained by the library's own
+// kernels:
+//  mlp_pass_kernel  128 rows per CTA (4 warps): forward and backward through
+//                   the two 64x64 layers on the tensor cores (mma.sync
+//                   m16n8k16 BF16, FP32 accumulate), activations staged in
+//                   shared memory.  Modes: training-gradient partials on a
+//                   Philox-sampled batch, full-data loss gradient, and the
+//                   input gradient du_hat/dx (value + gradient at points).
+//  mlp_adam_kernel  sums the per-CTA gradient partials in a fixed order,
+//                   Adam update of the FP32 master weights, refresh of the
+//                   BF16 copies (row-major and transposed) used by the GEMMs.
+//  mlp_table        grad u_hat on a grid per region (the inference pass),
+//                   read by the path kernel with bilinear interpolation to
+//                   form the control term F = -sigma^T grad u_hat of every step.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
 #include "../../include/spac_fk.h"
+#include "fk_device.cuh"
 #include "fk_mlp.h"
+#include "fk_mma.cuh"
 
 namespace fk {
+
 Mlp::~Mlp() {
-  if (d_master) cudaFree(d_master);
-  if (d_bf16) cudaFree(d_bf16);
-  if (d_m) cudaFree(d_m);
-  if (d_v) cudaFree(d_v);
+  for (void* p : {static_cast<void*>(d_master), d_bf16, static_cast<void*>(d_m), static_cast<void*>(d_v),
+                  static_cast<void*>(d_norm), static_cast<void*>(d_partial), static_cast<void*>(d_loss),
+                  static_cast<void*>(d_rect), static_cast<void*>(d_table), static_cast<void*>(d_samples),
+                  static_cast<void*>(d_hist)})
+    if (p) cudaFree(p);
 }
+
+namespace {
+
+constexpr int W = 64;
+constexpr int kRows = 128;      // rows per CTA pass
+constexpr int kThreads = 128;
+constexpr int LD = 72;          // bf16 leading dimension of [rows][64] tiles (144 B rows)
+constexpr int LDT = 136;        // bf16 leading dimension of [64][128] transposed tiles (272 B rows)
+constexpr int OFF_W1 = 0, OFF_B1 = 128, OFF_W2 = 192, OFF_B2 = OFF_W2 + W * W, OFF_W3 = OFF_B2 + W,
+              OFF_B3 = OFF_W3 + W * W, OFF_W4 = OFF_B3 + W, OFF_B4 = OFF_W4 + W, NPARAM = OFF_B4 + 1;
+constexpr int BF_PER_REGION = 4 * W * W;  // W2, W2^T, W3, W3^T
+
+enum { MODE_TRAIN = 0, MODE_LOSSGRAD = 1, MODE_GRADX = 2 };
+
+__device__ __forceinline__ float silu_f(float z, float& dsilu) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  dsilu = s * (1.0f + z * (1.0f - s));
+  return z * s;
+}
+
+struct PassArgs {
+  int mode, n_regions, ctas_per_region, rows_per_cta;
+  const float* params;          // [R][NPARAM]
+  const __nv_bfloat16* wbf;     // [R][4][W*W]
+  const float4* norm;           // per region: (lo_x, lo_y, scale_x, scale_y)
+  // samples (TRAIN / LOSSGRAD): region r owns [sample_off[r], sample_off[r+1])
+  const float4* samples;        // (x, y, target, -)
+  const int* sample_off;
+  uint32_t seed0, seed1, step;
+  float inv_batch;              // 1 / rows per region that contribute to the loss
+  float* partial;               // [R][C][NPARAM]
+  float* loss;                  // [R][C]
+  // GRADX
+  int n_points;
+  const float2* points;
+  const int* point_region;      // may be null (region 0)
+  float* out;                   // [n][3]
+};
+
+struct Smem {
+  __nv_bfloat16 w2[W * LD], w2t[W * LD], w3[W * LD], w3t[W * LD];
+  __nv_bfloat16 h1[kRows * LD], h2[kRows * LD], s1[kRows * LD], s2[kRows * LD];
+  // h3 and s3 are adjacent: after the layer-3 backward they hold dp1 in FP32
+  __nv_bfloat16 h3[kRows * LD], s3[kRows * LD];
+  __nv_bfloat16 h1t[W * LDT], h2t[W * LDT];
+  __nv_bfloat16 dp[kRows * LD], dpt[W * LDT];
+  float w1[2 * W], b1[W], b2[W], b3[W], w4[W], b4;
+  float z[kRows][2], tgt[kRows], dO[kRows], o[kRows];
+  int valid[kRows];
+};
+
+__global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t4 = lane & 3;
+  const int region = blockIdx.y, cta = blockIdx.x;
+  const float* P = a.params + static_cast<long long>(region) * NPARAM;
+  const __nv_bfloat16* WB = a.wbf + static_cast<long long>(region) * BF_PER_REGION;
+  // weights into shared memory
+  for (int e = tid; e < W * W; e += kThreads) {
+    const int r = e / W, c = e % W;
+    S.w2[r * LD + c] = WB[e];
+    S.w2t[r * LD + c] = WB[W * W + e];
+    S.w3[r * LD + c] = WB[2 * W * W + e];
+    S.w3t[r * LD + c] = WB[3 * W * W + e];
+  }
+  for (int e = tid; e < 2 * W; e += kThreads) S.w1[e] = P[OFF_W1 + e];
+  for (int e = tid; e < W; e += kThreads) {
+    S.b1[e] = P[OFF_B1 + e]; S.b2[e] = P[OFF_B2 + e]; S.b3[e] = P[OFF_B3 + e]; S.w4[e] = P[OFF_W4 + e];
+  }
+  if (tid == 0) S.b4 = P[OFF_B4];
+  const float4 nm = a.norm[region];
+  const bool train = a.mode != MODE_GRADX;
+
+  // persistent gradient accumulators: this warp owns rows 16*warp.. of dW2 / dW3
+  float cW2[1][8][4], cW3[1][8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cW2[0][j][q] = cW3[0][j][q] = 0.f;
+  float gW4 = 0.f, gB3 = 0.f, gB2 = 0.f, gB1 = 0.f, gW10 = 0.f, gW11 = 0.f, gB4 = 0.f, lsum = 0.f;
+
+  int n_tiles, row0;
+  if (a.mode == MODE_GRADX) {
+    n_tiles = 1;
+    row0 = (blockIdx.x + blockIdx.y * gridDim.x) * kRows;
+  } else {
+    n_tiles = a.rows_per_cta / kRows;
+    row0 = cta * a.rows_per_cta;
+  }
+  __syncthreads();
+
+  for (int tile = 0; tile < n_tiles; ++tile) {
+    // ---- samples: row tid of this tile
+    {
+      const int r = tid;
+      float x = 0.f, y = 0.f, tg = 0.f;
+      int valid = 0;
+      if (a.mode == MODE_GRADX) {
+        const int pi = row0 + r;
+        if (pi < a.n_points) {
+          const float2 p = a.points[pi];
+          x = p.x; y = p.y; valid = 1;
+        }
+      } else {
+        const int lo = a.sample_off[region], cnt = a.sample_off[region + 1] - lo;
+        const int gr = row0 + tile * kRows + r;  // row of the region's batch
+        if (cnt > 0) {
+          int si;
+          if (a.mode == MODE_TRAIN) {
+            const uint4 rr = philox10(make_uint4(a.step, static_cast<uint32_t>(gr), static_cast<uint32_t>(region), 0x6d6c70u),
+                                      a.seed0, a.seed1);
+            si = lo + static_cast<int>(rr.x % static_cast<uint32_t>(cnt));
+            valid = 1;
+          } else {
+            si = lo + gr;
+            valid = gr < cnt;
+            if (!valid) si = lo;
+          }
+          const float4 s = a.samples[si];
+          x = s.x; y = s.y; tg = s.z;
+        }
+      }
+      float z0 = (x - nm.x) * nm.z, z1 = (y - nm.y) * nm.w;
+      S.z[r][0] = z0; S.z[r][1] = z1; S.tgt[r] = tg; S.valid[r] = valid;
+      // layer 1 (K = 2) in FP32
+      for (int j = 0; j < W; ++j) {
+        const float p = S.w1[2 * j] * z0 + S.w1[2 * j + 1] * z1 + S.b1[j];
+        float ds;
+        const float hv = silu_f(p, ds);
+        S.h1[r * LD + j] = __float2bfloat16_rn(hv);
+        S.s1[r * LD + j] = __float2bfloat16_rn(ds);
+        if (train) S.h1t[j * LDT + r] = __float2bfloat16_rn(hv);
+      }
+    }
+    __syncthreads();
+    // ---- layers 2 and 3 on the tensor cores, warp w owns rows 32w..32w+31
+    for (int layer = 0; layer < 2; ++layer) {
+      const __nv_bfloat16* Ain = layer == 0 ? S.h1 : S.h2;
+      const __nv_bfloat16* Bw = layer == 0 ? S.w2 : S.w3;
+      const float* bias = layer == 0 ? S.b2 : S.b3;
+      __nv_bfloat16* Hout = layer == 0 ? S.h2 : S.h3;
+      __nv_bfloat16* Sout = layer == 0 ? S.s2 : S.s3;
+      float c[2][8][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
+      warp_gemm_tn<2, 8, W>(c, Ain, LD, warp * 32, Bw, LD, 0, lane);
+      float orow[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int r = warp * 32 + mt * 16 + g + ((q >> 1) << 3);
+            const int col = nt * 8 + 2 * t4 + (q & 1);
+            float ds;
+            const float hv = silu_f(c[mt][nt][q] + bias[col], ds);
+            Hout[r * LD + col] = __float2bfloat16_rn(hv);
+            Sout[r * LD + col] = __float2bfloat16_rn(ds);
+            if (layer == 0 && train) S.h2t[col * LDT + r] = __float2bfloat16_rn(hv);
+            if (layer == 1) orow[mt][q >> 1] += S.w4[col] * hv;
+          }
+      if (layer == 1) {
+        // output unit: reduce the row partial sums over the quad
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            float v = orow[mt][hh];
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            if (t4 == 0) S.o[warp * 32 + mt * 16 + g + hh * 8] = v + S.b4;
+          }
+      }
+      __syncthreads();
+    }
+    // ---- output gradient and dp3 = dO * w4 * silu'(p3)
+    {
+      const int r = tid;
+      const float o = S.o[r];
+      float d;
+      if (a.mode == MODE_GRADX) {
+        d = 1.f;
+      } else {
+        const float e = S.valid[r] ? (o - S.tgt[r]) : 0.f;
+        lsum += e * e;
+        d = 2.f * e * a.inv_batch;
+      }
+      S.dO[r] = d;
+      for (int j = 0; j < W; ++j) {
+        const float v = d * S.w4[j] * __bfloat162float(S.s3[r * LD + j]);
+        const __nv_bfloat16 vb = __float2bfloat16_rn(v);
+        S.dp[r * LD + j] = vb;
+        if (train) S.dpt[j * LDT + r] = vb;
+      }
+    }
+    __syncthreads();
+    // layer-3 backward: dW3 += dp3^T h2, db3, dW4, db4; dh2 = dp3 W3
+    if (train) {
+      warp_gemm_tn<1, 8, kRows>(cW3, S.dpt, LDT, warp * 16, S.h2t, LDT, 0, lane);
+      if (tid < W) {
+        const int j = tid;
+        for (int r = 0; r < kRows; ++r) {
+          gW4 += S.dO[r] * __bfloat162float(S.h3[r * LD + j]);
+          gB3 += __bfloat162float(S.dp[r * LD + j]);
+        }
+        if (j == 0)
+          for (int r = 0; r < kRows; ++r) gB4 += S.dO[r];
+      }
+    }
+    {
+      float c[2][8][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
+      warp_gemm_tn<2, 8, W>(c, S.dp, LD, warp * 32, S.w3t, LD, 0, lane);
+      __syncthreads();  // everyone is done reading dp / dpt of layer 3
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int r = warp * 32 + mt * 16 + g + ((q >> 1) << 3);
+            const int col = nt * 8 + 2 * t4 + (q & 1);
+            const __nv_bfloat16 vb = __float2bfloat16_rn(c[mt][nt][q] * __bfloat162float(S.s2[r * LD + col]));
+            S.dp[r * LD + col] = vb;
+            if (train) S.dpt[col * LDT + r] = vb;
+          }
+    }
+    __syncthreads();
+    // layer-2 backward: dW2 += dp2^T h1, db2; dh1 = dp2 W2
+    if (train) {
+      warp_gemm_tn<1, 8, kRows>(cW2, S.dpt, LDT, warp * 16, S.h1t, LDT, 0, lane);
+      if (tid < W)
+        for (int r = 0; r < kRows; ++r) gB2 += __bfloat162float(S.dp[r * LD + tid]);
+    }
+    {
+      float c[2][8][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
+      warp_gemm_tn<2, 8, W>(c, S.dp, LD, warp * 32, S.w2t, LD, 0, lane);
+      __syncthreads();
+      // dp1 = dh1 * silu'(p1), kept in FP32 in the (now free) h3 / s3 area as pairs
+      static_assert(sizeof(float) * kRows * W <= 2 * sizeof(__nv_bfloat16) * kRows * LD, "dp1 overlay");
+      float* dp1 = reinterpret_cast<float*>(S.h3);  // [kRows][W] FP32 over h3 + s3
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int r = warp * 32 + mt * 16 + g + ((q >> 1) << 3);
+            const int col = nt * 8 + 2 * t4 + (q & 1);
+            dp1[r * W + col] = c[mt][nt][q] * __bfloat162float(S.s1[r * LD + col]);
+          }
+    }
+    __syncthreads();
+    {
+      const float* dp1 = reinterpret_cast<const float*>(S.h3);
+      if (a.mode == MODE_GRADX) {
+        const int r = tid, pi = row0 + r;
+        float gx = 0.f, gy = 0.f;
+        for (int j = 0; j < W; ++j) {
+          gx += dp1[r * W + j] * S.w1[2 * j];
+          gy += dp1[r * W + j] * S.w1[2 * j + 1];
+        }
+        if (pi < a.n_points) {
+          a.out[3 * pi] = S.o[r];
+          a.out[3 * pi + 1] = gx * nm.z;
+          a.out[3 * pi + 2] = gy * nm.w;
+        }
+      } else if (tid < W) {
+        const int j = tid;
+        for (int r = 0; r < kRows; ++r) {
+          const float d = dp1[r * W + j];
+          gB1 += d;
+          gW10 += d * S.z[r][0];
+          gW11 += d * S.z[r][1];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (a.mode == MODE_GRADX) return;
+  // ---- write this CTA's gradient partial
+  float* out = a.partial + (static_cast<long long>(region) * a.ctas_per_region + cta) * NPARAM;
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = warp * 16 + g + ((q >> 1) << 3);
+      const int col = nt * 8 + 2 * t4 + (q & 1);
+      out[OFF_W2 + r * W + col] = cW2[0][nt][q];
+      out[OFF_W3 + r * W + col] = cW3[0][nt][q];
+    }
+  if (tid < W) {
+    const int j = tid;
+    out[OFF_W4 + j] = gW4;
+    out[OFF_B3 + j] = gB3;
+    out[OFF_B2 + j] = gB2;
+    out[OFF_B1 + j] = gB1;
+    out[OFF_W1 + 2 * j] = gW10;
+    out[OFF_W1 + 2 * j + 1] = gW11;
+    if (j == 0) out[OFF_B4] = gB4;
+  }
+  // loss partial (sum of squared errors of this CTA)
+  __shared__ float red[kThreads];
+  red[tid] = lsum;
+  __syncthreads();
+  for (int o = kThreads / 2; o > 0; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0) a.loss[region * a.ctas_per_region + cta] = red[0];
+}
+
+// Sum of partials (fixed order) and Adam update; refreshes the BF16 copies.
+__global__ void mlp_adam_kernel(float* params, __nv_bfloat16* wbf, float* m, float* v, const float* partial,
+                                const float* loss, int n_regions, int ctas, float lr, float b1, float b2, float eps,
+                                float bc1, float bc2, int apply, float* grad_out, float* hist, float loss_scale) {
+  const long long total = static_cast<long long>(n_regions) * NPARAM;
+  for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int r = static_cast<int>(e / NPARAM), p = static_cast<int>(e % NPARAM);
+    float gsum = 0.f;
+    for (int c = 0; c < ctas; ++c) gsum += partial[(static_cast<long long>(r) * ctas + c) * NPARAM + p];
+    if (grad_out) grad_out[e] = gsum;
+    if (!apply) continue;
+    const float mm = b1 * m[e] + (1.f - b1) * gsum;
+    const float vv = b2 * v[e] + (1.f - b2) * gsum * gsum;
+    m[e] = mm;
+    v[e] = vv;
+    const float th = params[e] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+    params[e] = th;
+    __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
+    const __nv_bfloat16 tb = __float2bfloat16_rn(th);
+    if (p >= OFF_W2 && p < OFF_W2 + W * W) {
+      const int q = p - OFF_W2, o = q / W, i = q % W;
+      B[q] = tb;
+      B[W * W + i * W + o] = tb;
+    } else if (p >= OFF_W3 && p < OFF_W3 + W * W) {
+      const int q = p - OFF_W3, o = q / W, i = q % W;
+      B[2 * W * W + q] = tb;
+      B[3 * W * W + i * W + o] = tb;
+    }
+  }
+  if (hist && blockIdx.x == 0 && threadIdx.x == 0) {
+    float s = 0.f;
+    for (int i = 0; i < n_regions * ctas; ++i) s += loss[i];
+    *hist = s * loss_scale;
+  }
+}
+
+__global__ void mlp_refresh_bf16(const float* params, __nv_bfloat16* wbf, int n_regions) {
+  const long long total = static_cast<long long>(n_regions) * W * W;
+  for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int r = static_cast<int>(e / (W * W)), q = static_cast<int>(e % (W * W)), o = q / W, i = q % W;
+    const float* P = params + static_cast<long long>(r) * NPARAM;
+    __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
+    B[q] = __float2bfloat16_rn(P[OFF_W2 + q]);
+    B[W * W + i * W + o] = __float2bfloat16_rn(P[OFF_W2 + q]);
+    B[2 * W * W + q] = __float2bfloat16_rn(P[OFF_W3 + q]);
+    B[3 * W * W + i * W + o] = __float2bfloat16_rn(P[OFF_W3 + q]);
+  }
+}
+
+// grid point (i, j) of region r: out table[r][j][i] = (du/dx, du/dy)
+__global__ void mlp_grid_points(const double* rects, int n_regions, int G, float2* pts, int* reg) {
+  const long long total = static_cast<long long>(n_regions) * G * G;
+  for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int r = static_cast<int>(e / (G * G)), q = static_cast<int>(e % (G * G)), j = q / G, i = q % G;
+    const double* R = rects + 4 * r;
+    pts[e] = make_float2(static_cast<float>(R[0] + (R[2] - R[0]) * i / (G - 1)),
+                         static_cast<float>(R[1] + (R[3] - R[1]) * j / (G - 1)));
+    reg[e] = r;
+  }
+}
+
+__global__ void mlp_pack_table(const float* eval, long long n, float2* table) {
+  for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < n;
+       e += static_cast<long long>(gridDim.x) * blockDim.x)
+    table[e] = make_float2(eval[3 * e + 1], eval[3 * e + 2]);
+}
+
+}  // namespace
+
+size_t mlp_pass_smem() { return sizeof(Smem); }
+int mlp_nparam() { return NPARAM; }
+
+// Evaluates (u_hat, du/dx, du/dy) at n device points of one region.
+cudaError_t mlp_eval_device(const float* params, const void* wbf, const float4* norm, int n, const float2* d_pts,
+                            float* d_out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.mode = MODE_GRADX;
+  a.n_regions = 1;
+  a.params = params;
+  a.wbf = static_cast<const __nv_bfloat16*>(wbf);
+  a.norm = norm;
+  a.n_points = n;
+  a.points = d_pts;
+  a.out = d_out;
+  cudaError_t e = cudaFuncSetAttribute(mlp_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(Smem)));
+  if (e != cudaSuccess) return e;
+  const int tiles = (n + kRows - 1) / kRows;
+  mlp_pass_kernel<<<dim3(tiles, 1), kThreads, sizeof(Smem), s>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace fk
 
-extern "C" {
-int fk_mlp_create(fk_ctx*, int, const double*, const double*, unsigned long long, int*) { return FK_ERR_ARG; }
-int fk_mlp_num_params(fk_ctx*, int, int*) { return FK_ERR_ARG; }
-int fk_mlp_get_params(fk_ctx*, int, float*) { return FK_ERR_ARG; }
-int fk_mlp_set_params(fk_ctx*, int, const float*) { return FK_ERR_ARG; }
-int fk_mlp_train(fk_ctx*, int, int, const double*, const double*, int, int, double, unsigned long long, float*) {
-  return FK_ERR_ARG;
+// ============================================================== C ABI =======
+// (the context-side parts live in fk_api.cu; these helpers are called there)
+namespace fk {
+
+int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed, std::string& err) {
+  M.n_regions = n_regions;
+  M.n_params = NPARAM;
+  M.rects.assign(rects, rects + 4 * n_regions);
+  std::vector<float4> norm(n_regions);
+  for (int r = 0; r < n_regions; ++r) {
+    const double* R = rects + 4 * r;
+    if (!(R[2] > R[0] && R[3] > R[1])) { err = "mlp region rectangles must be non-empty"; return FK_ERR_ARG; }
+    // (x - lo) * scale maps the rectangle to [-1, 1]^2
+    norm[r] = make_float4(static_cast<float>(0.5 * (R[0] + R[2])), static_cast<float>(0.5 * (R[1] + R[3])),
+                          static_cast<float>(2.0 / (R[2] - R[0])), static_cast<float>(2.0 / (R[3] - R[1])));
+  }
+  std::vector<float> p(static_cast<size_t>(n_regions) * NPARAM, 0.f);
+  std::mt19937_64 rng(seed);
+  auto uni = [&](float a) { return std::uniform_real_distribution<float>(-a, a)(rng); };
+  for (int r = 0; r < n_regions; ++r) {
+    float* P = p.data() + static_cast<size_t>(r) * NPARAM;
+    const float a1 = std::sqrt(6.f / (2 + W)), a2 = std::sqrt(6.f / (2 * W)), a4 = std::sqrt(6.f / (W + 1));
+    for (int e = 0; e < 2 * W; ++e) P[OFF_W1 + e] = uni(a1);
+    for (int e = 0; e < W * W; ++e) { P[OFF_W2 + e] = uni(a2); P[OFF_W3 + e] = uni(a2); }
+    for (int e = 0; e < W; ++e) P[OFF_W4 + e] = uni(a4);
+  }
+  const size_t np = p.size();
+  if (cudaMalloc(&M.d_master, np * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&M.d_m, np * sizeof(float)) != cudaSuccess || cudaMalloc(&M.d_v, np * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&M.d_bf16, static_cast<size_t>(n_regions) * BF_PER_REGION * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&M.d_norm, n_regions * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&M.d_rect, 4 * n_regions * sizeof(double)) != cudaSuccess) {
+    err = "mlp: device allocation failed";
+    return FK_ERR_CUDA;
+  }
+  cudaMemcpy(M.d_master, p.data(), np * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(M.d_m, 0, np * sizeof(float));
+  cudaMemset(M.d_v, 0, np * sizeof(float));
+  cudaMemcpy(M.d_norm, norm.data(), n_regions * sizeof(float4), cudaMemcpyHostToDevice);
+  cudaMemcpy(M.d_rect, rects, 4 * n_regions * sizeof(double), cudaMemcpyHostToDevice);
+  mlp_refresh_bf16<<<64, 256>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), n_regions);
+  if (cudaDeviceSynchronize() != cudaSuccess) { err = "mlp: init kernels failed"; return FK_ERR_CUDA; }
+  return FK_OK;
 }
-int fk_mlp_eval(fk_ctx*, int, int, const double*, double*) { return FK_ERR_ARG; }
-int fk_mlp_loss_grad(fk_ctx*, int, int, const double*, const double*, double*, float*) { return FK_ERR_ARG; }
+
+int mlp_set_params(Mlp& M, const float* host) {
+  const size_t np = static_cast<size_t>(M.n_regions) * NPARAM;
+  if (cudaMemcpy(M.d_master, host, np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return FK_ERR_CUDA;
+  cudaMemset(M.d_m, 0, np * sizeof(float));
+  cudaMemset(M.d_v, 0, np * sizeof(float));
+  M.adam_t = 0;
+  mlp_refresh_bf16<<<64, 256>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), M.n_regions);
+  return cudaDeviceSynchronize() == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
+
+// Uploads (x, y, target) samples grouped by region.
+static int upload_samples(Mlp& M, int n, const double* xy, const double* target, const int* region,
+                          std::vector<int>& off, std::string& err) {
+  std::vector<std::vector<float4>> by(M.n_regions);
+  for (int i = 0; i < n; ++i) {
+    const int r = region ? region[i] : 0;
+    if (r < 0 || r >= M.n_regions) { err = "sample region out of range"; return FK_ERR_ARG; }
+    by[r].push_back(make_float4(static_cast<float>(xy[2 * i]), static_cast<float>(xy[2 * i + 1]),
+                                static_cast<float>(target[i]), 0.f));
+  }
+  std::vector<float4> flat;
+  off.assign(M.n_regions + 1, 0);
+  for (int r = 0; r < M.n_regions; ++r) {
+    off[r] = static_cast<int>(flat.size());
+    flat.insert(flat.end(), by[r].begin(), by[r].end());
+  }
+  off[M.n_regions] = static_cast<int>(flat.size());
+  if (M.d_samples) cudaFree(M.d_samples);
+  M.d_samples = nullptr;
+  if (cudaMalloc(&M.d_samples, std::max<size_t>(flat.size(), 1) * sizeof(float4) + (M.n_regions + 1) * sizeof(int)) !=
+      cudaSuccess) {
+    err = "mlp: sample allocation failed";
+    return FK_ERR_CUDA;
+  }
+  cudaMemcpy(M.d_samples, flat.data(), flat.size() * sizeof(float4), cudaMemcpyHostToDevice);
+  int* d_off = reinterpret_cast<int*>(M.d_samples + std::max<size_t>(flat.size(), 1));
+  cudaMemcpy(d_off, off.data(), (M.n_regions + 1) * sizeof(int), cudaMemcpyHostToDevice);
+  M.d_sample_off = d_off;
+  return FK_OK;
+}
+
+int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* region, int steps, int batch,
+              double lr, unsigned long long seed, float* loss_hist, cudaStream_t s, std::string& err) {
+  if (steps < 0 || batch < kRows || batch % kRows) { err = "batch must be a positive multiple of 128"; return FK_ERR_ARG; }
+  std::vector<int> off;
+  int rc = upload_samples(M, n, xy, target, region, off, err);
+  if (rc) return rc;
+  // one 128-row tile per CTA (the step is latency-bound: more CTAs, shorter
+  // step); larger tiles per CTA only when the grid would exceed ~4 waves
+  int rows_per_cta = kRows;
+  while (rows_per_cta < 1024 && batch % (2 * rows_per_cta) == 0 &&
+         static_cast<long long>(batch / rows_per_cta) * M.n_regions > 4 * 152)
+    rows_per_cta *= 2;
+  const int ctas = batch / rows_per_cta;
+  const size_t np = static_cast<size_t>(M.n_regions) * NPARAM;
+  if (M.d_partial) cudaFree(M.d_partial);
+  if (M.d_loss) cudaFree(M.d_loss);
+  if (M.d_hist) cudaFree(M.d_hist);
+  if (cudaMalloc(&M.d_partial, np * ctas * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&M.d_loss, static_cast<size_t>(M.n_regions) * ctas * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&M.d_hist, std::max(steps, 1) * sizeof(float)) != cudaSuccess) {
+    err = "mlp: training buffers";
+    return FK_ERR_CUDA;
+  }
+  cudaError_t e = cudaFuncSetAttribute(mlp_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(Smem)));
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.mode = MODE_TRAIN;
+  a.n_regions = M.n_regions;
+  a.ctas_per_region = ctas;
+  a.rows_per_cta = rows_per_cta;
+  a.params = M.d_master;
+  a.wbf = static_cast<const __nv_bfloat16*>(M.d_bf16);
+  a.norm = M.d_norm;
+  a.samples = M.d_samples;
+  a.sample_off = M.d_sample_off;
+  a.seed0 = static_cast<uint32_t>(seed);
+  a.seed1 = static_cast<uint32_t>(seed >> 32);
+  a.inv_batch = 1.f / batch;
+  a.partial = M.d_partial;
+  a.loss = M.d_loss;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  // capture the whole loop in one CUDA graph: 2 kernels per step
+  cudaGraph_t graph;
+  e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  const int adam_blocks = static_cast<int>(std::min<size_t>((np + 255) / 256, 1024));
+  for (int st = 0; st < steps; ++st) {
+    a.step = static_cast<uint32_t>(M.adam_t + st);
+    mlp_pass_kernel<<<dim3(ctas, M.n_regions), kThreads, sizeof(Smem), s>>>(a);
+    const double t = static_cast<double>(M.adam_t + st + 1);
+    const float bc1 = static_cast<float>(1.0 - std::pow(0.9, t)), bc2 = static_cast<float>(1.0 - std::pow(0.999, t));
+    // cosine decay of the learning rate from lr to lr/100 over this training call
+    const double lr_t = lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(M_PI * st / std::max(1, steps))));
+    mlp_adam_kernel<<<adam_blocks, 256, 0, s>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), M.d_m, M.d_v,
+                                                M.d_partial, M.d_loss, M.n_regions, ctas, static_cast<float>(lr_t), b1,
+                                                b2, eps, bc1, bc2, 1, nullptr, M.d_hist + st,
+                                                1.f / (static_cast<float>(batch) * M.n_regions));
+  }
+  e = cudaStreamEndCapture(s, &graph);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  cudaGraphExec_t exec;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  e = cudaGraphLaunch(exec, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaGraphExecDestroy(exec);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  M.adam_t += steps;
+  if (loss_hist && steps > 0) cudaMemcpy(loss_hist, M.d_hist, steps * sizeof(float), cudaMemcpyDeviceToHost);
+  return FK_OK;
+}
+
+int mlp_loss_grad(Mlp& M, int n, const double* xy, const double* target, double* loss, float* grad, cudaStream_t s,
+                  std::string& err) {
+  // region 0, all n samples, no sampling
+  std::vector<int> off;
+  std::vector<int> reg(n, 0);
+  int rc = upload_samples(M, n, xy, target, reg.data(), off, err);
+  if (rc) return rc;
+  const int rows = (n + kRows - 1) / kRows * kRows;
+  const int ctas = rows / kRows;
+  float *d_partial = nullptr, *d_loss = nullptr, *d_grad = nullptr;
+  const size_t np = static_cast<size_t>(M.n_regions) * NPARAM;
+  if (cudaMalloc(&d_partial, np * ctas * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&d_loss, static_cast<size_t>(M.n_regions) * ctas * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&d_grad, np * sizeof(float)) != cudaSuccess) {
+    err = "mlp: loss-grad buffers";
+    return FK_ERR_CUDA;
+  }
+  cudaMemset(d_partial, 0, np * ctas * sizeof(float));
+  cudaMemset(d_loss, 0, static_cast<size_t>(M.n_regions) * ctas * sizeof(float));
+  cudaFuncSetAttribute(mlp_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(Smem)));
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.mode = MODE_LOSSGRAD;
+  a.n_regions = 1;
+  a.ctas_per_region = ctas;
+  a.rows_per_cta = kRows;
+  a.params = M.d_master;
+  a.wbf = static_cast<const __nv_bfloat16*>(M.d_bf16);
+  a.norm = M.d_norm;
+  a.samples = M.d_samples;
+  a.sample_off = M.d_sample_off;
+  a.inv_batch = 1.f / n;
+  a.partial = d_partial;
+  a.loss = d_loss;
+  mlp_pass_kernel<<<dim3(ctas, 1), kThreads, sizeof(Smem), s>>>(a);
+  mlp_adam_kernel<<<64, 256, 0, s>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), M.d_m, M.d_v, d_partial,
+                                     d_loss, 1, ctas, 0.f, 0.f, 0.f, 0.f, 1.f, 1.f, 0, d_grad, nullptr, 0.f);
+  std::vector<float> l(ctas);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMemcpy(grad, d_grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(l.data(), d_loss, ctas * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d_partial);
+  cudaFree(d_loss);
+  cudaFree(d_grad);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  double sum = 0;
+  for (float v : l) sum += v;
+  *loss = sum / n;
+  return FK_OK;
+}
+
+int mlp_eval_host(Mlp& M, int n, const double* xy, const int* region, double* out, cudaStream_t s,
+                  std::string& err) {
+  // group by region: evaluate each region's points in one launch
+  std::vector<float> res(3 * static_cast<size_t>(n));
+  for (int r = 0; r < M.n_regions; ++r) {
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i)
+      if ((region ? region[i] : 0) == r) idx.push_back(i);
+    if (idx.empty()) continue;
+    std::vector<float2> pts(idx.size());
+    for (size_t k = 0; k < idx.size(); ++k)
+      pts[k] = make_float2(static_cast<float>(xy[2 * idx[k]]), static_cast<float>(xy[2 * idx[k] + 1]));
+    float2* d_pts = nullptr;
+    float* d_out = nullptr;
+    if (cudaMalloc(&d_pts, pts.size() * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&d_out, 3 * pts.size() * sizeof(float)) != cudaSuccess) {
+      err = "mlp eval buffers";
+      return FK_ERR_CUDA;
+    }
+    cudaMemcpy(d_pts, pts.data(), pts.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    cudaError_t e = mlp_eval_device(M.d_master + static_cast<size_t>(r) * NPARAM,
+                                    static_cast<__nv_bfloat16*>(M.d_bf16) + static_cast<size_t>(r) * BF_PER_REGION,
+                                    M.d_norm + r, static_cast<int>(pts.size()), d_pts, d_out, s);
+    std::vector<float> o(3 * pts.size());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpy(o.data(), d_out, o.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d_pts);
+    cudaFree(d_out);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+    for (size_t k = 0; k < idx.size(); ++k)
+      for (int q = 0; q < 3; ++q) res[3 * idx[k] + q] = o[3 * k + q];
+  }
+  for (size_t i = 0; i < res.size(); ++i) out[i] = res[i];
+  return FK_OK;
+}
+
+int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err) {
+  if (G < 2 || G > 2048) { err = "table grid must be 2..2048"; return FK_ERR_ARG; }
+  const long long npts = static_cast<long long>(M.n_regions) * G * G;
+  if (M.d_table) cudaFree(M.d_table);
+  M.d_table = nullptr;
+  float2* d_pts = nullptr;
+  int* d_reg = nullptr;
+  float* d_eval = nullptr;
+  if (cudaMalloc(&M.d_table, npts * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc(&d_pts, npts * sizeof(float2)) != cudaSuccess || cudaMalloc(&d_reg, npts * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&d_eval, 3 * npts * sizeof(float)) != cudaSuccess) {
+    err = "mlp table buffers";
+    return FK_ERR_CUDA;
+  }
+  mlp_grid_points<<<256, 256, 0, s>>>(M.d_rect, M.n_regions, G, d_pts, d_reg);
+  cudaError_t e = cudaSuccess;
+  for (int r = 0; r < M.n_regions && e == cudaSuccess; ++r)
+    e = mlp_eval_device(M.d_master + static_cast<size_t>(r) * NPARAM,
+                        static_cast<__nv_bfloat16*>(M.d_bf16) + static_cast<size_t>(r) * BF_PER_REGION, M.d_norm + r,
+                        G * G, d_pts + static_cast<long long>(r) * G * G, d_eval + 3LL * r * G * G, s);
+  if (e == cudaSuccess) {
+    mlp_pack_table<<<256, 256, 0, s>>>(d_eval, npts, M.d_table);
+    e = cudaStreamSynchronize(s);
+  }
+  cudaFree(d_pts);
+  cudaFree(d_reg);
+  cudaFree(d_eval);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  M.table_grid = G;
+  return FK_OK;
+}
+
+}  // namespace fk

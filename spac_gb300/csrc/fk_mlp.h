@@ -1,21 +1,45 @@
-// Learned control variate: MLP 2 -> W -> W -> W -> 1 (SiLU) with BF16 weights
-// for the tensor-core kernels and an FP32 master copy for Adam.
+// Learned control variate: MLP 2 -> 64 -> 64 -> 64 -> 1 (SiLU) per region,
+// BF16 weights for the tensor-core kernels, FP32 master copy for Adam.
 #pragma once
 #include <cuda_runtime.h>
+#include <string>
 #include <vector>
 
 namespace fk {
 
 struct Mlp {
-  int width = 64;
-  double in_lo[2] = {0, 0}, in_scale[2] = {1, 1};
-  int n_params = 0;
-  float* d_master = nullptr;    // FP32 master parameters (packed)
-  void* d_bf16 = nullptr;       // BF16 copy used by the kernels
-  float* d_m = nullptr;         // Adam moments
+  int n_regions = 0;
+  int n_params = 0;                 // per region
+  std::vector<double> rects;        // 4 per region
+  float* d_master = nullptr;        // FP32 master parameters [R][P]
+  void* d_bf16 = nullptr;           // BF16 W2, W2^T, W3, W3^T per region
+  float* d_m = nullptr;             // Adam moments
   float* d_v = nullptr;
+  float4* d_norm = nullptr;         // input normalisation per region
+  double* d_rect = nullptr;
+  float* d_partial = nullptr;       // per-CTA gradient partials
+  float* d_loss = nullptr;
+  float* d_hist = nullptr;
+  float4* d_samples = nullptr;      // training samples (x, y, target) grouped by region
+  int* d_sample_off = nullptr;      // inside the d_samples allocation
+  float2* d_table = nullptr;        // grad u_hat on a G x G grid per region
+  int table_grid = 0;
   long long adam_t = 0;
+  Mlp() = default;
+  Mlp(const Mlp&) = delete;
+  Mlp& operator=(const Mlp&) = delete;
   ~Mlp();
 };
+
+size_t mlp_pass_smem();
+int mlp_nparam();
+int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed, std::string& err);
+int mlp_set_params(Mlp& M, const float* host);
+int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* region, int steps, int batch,
+              double lr, unsigned long long seed, float* loss_hist, cudaStream_t s, std::string& err);
+int mlp_loss_grad(Mlp& M, int n, const double* xy, const double* target, double* loss, float* grad, cudaStream_t s,
+                  std::string& err);
+int mlp_eval_host(Mlp& M, int n, const double* xy, const int* region, double* out, cudaStream_t s, std::string& err);
+int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err);
 
 }  // namespace fk

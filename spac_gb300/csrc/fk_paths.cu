@@ -135,7 +135,9 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
 
   const BvpDev& bvp = *a.bvp;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const bool cv = a.cv != 0;
+  const bool cv = a.cv != 0;         // any control term
+  const bool cv_exact = a.cv == 1;   // F from the problem functor
+  const bool cv_table = a.cv == 2;   // F from the learned gradient table
   const R d0 = R(bvp.dom[0]), d1 = R(bvp.dom[1]), d2 = R(bvp.dom[2]), d3 = R(bvp.dom[3]);
 
   for (;;) {
@@ -173,6 +175,19 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
     const bool sub_circle = (ST == 1) || (ST == 0 && itg.sub_shape == 1);
     const R st0 = Problem<PROB>::template state<R>(bvp, x0, y0);  // sigma state at the start point
     const uint32_t item = static_cast<uint32_t>(ch.item);
+    // learned control variate: grad u_hat table of this item's region
+    const float2* ctab = nullptr;
+    R cx0 = R(0), cy0 = R(0), csx = R(0), csy = R(0);
+    const int G = a.cv_grid;
+    if (cv_table) {
+      const int r = itg.cv_region;
+      const double* rc = a.cv_rect + 4 * r;
+      ctab = a.cv_tab + static_cast<long long>(r) * G * G;
+      cx0 = R(rc[0]);
+      cy0 = R(rc[1]);
+      csx = R((G - 1) / (rc[2] - rc[0]));
+      csy = R((G - 1) / (rc[3] - rc[1]));
+    }
 
     Acc acc[kNumAcc];
     unsigned n_steps = 0, n_dom = 0, n_cap = 0;
@@ -255,7 +270,21 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
       if (active) {
         // ---- one Euler-Maruyama step (Paso_Absorbente, FeynmanKacSolver.cpp:7-18)
         StepCoef<R> co;
-        Problem<PROB>::step(bvp, x, y, st, cv, co);
+        Problem<PROB>::step(bvp, x, y, st, cv_exact, co);
+        if (cv_table) {
+          // F = -sigma^T grad u_hat, bilinear in the region's table
+          R u = (x - cx0) * csx, v = (y - cy0) * csy;
+          u = fmin(fmax(u, R(0)), R(G - 1) - R(1e-3));
+          v = fmin(fmax(v, R(0)), R(G - 1) - R(1e-3));
+          const int i = static_cast<int>(u), j = static_cast<int>(v);
+          const R fu = u - R(i), fv = v - R(j);
+          const float2* T = ctab + j * G + i;
+          const float2 t00 = __ldg(T), t10 = __ldg(T + 1), t01 = __ldg(T + G), t11 = __ldg(T + G + 1);
+          const R gx = (R(1) - fv) * ((R(1) - fu) * R(t00.x) + fu * R(t10.x)) + fv * ((R(1) - fu) * R(t01.x) + fu * R(t11.x));
+          const R gy = (R(1) - fv) * ((R(1) - fu) * R(t00.y) + fu * R(t10.y)) + fv * ((R(1) - fu) * R(t01.y) + fu * R(t11.y));
+          co.Fx = -co.s * gx;
+          co.Fy = -co.s * gy;
+        }
         uint32_t wa, wb;
         if ((k & 1) == 0) {
           const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k >> 1), p, item, a.stream), a.key0, a.key1);

@@ -85,13 +85,14 @@ _SIGS = {
     "fk_mesh_csr": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp]),
     "fk_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint, _up, C.c_double, C.c_int, _dp, _dp, _dp,
                               _dp, C.POINTER(Stats)]),
-    "fk_mlp_create": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.c_ulonglong, _ip]),
+    "fk_mlp_create": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_ulonglong, _ip]),
     "fk_mlp_num_params": (C.c_int, [C.c_void_p, C.c_int, _ip]),
     "fk_mlp_get_params": (C.c_int, [C.c_void_p, C.c_int, _fp]),
     "fk_mlp_set_params": (C.c_int, [C.c_void_p, C.c_int, _fp]),
-    "fk_mlp_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double,
+    "fk_mlp_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int, C.c_int, C.c_double,
                                C.c_ulonglong, _fp]),
-    "fk_mlp_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
+    "fk_mlp_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp]),
+    "fk_mlp_build_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
     "fk_solve_points_noalloc": (C.c_int, [C.POINTER(BvpDesc), C.c_ulonglong, C.c_uint, C.c_int, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
