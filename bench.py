@@ -193,6 +193,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--paths", type=int, default=CFG["paths_per_item"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-metric", action="store_true", help="skip the time-to-1e-3 comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -292,6 +293,9 @@ def main():
     fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12  # TFLOP/s, nominal at the maximum SM clock
     achieved = flops / (k_ms / 1000.0) / 1e12
     traffic = _read_traffic()
+    ttt = None
+    if rank == 0 and not args.no_metric:
+        ttt = time_to_target_all(ctx, mesh)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -309,12 +313,121 @@ def main():
                                             f"(sm_max_mhz of MEASURED_PEAKS.json, {src}); no FP32 figure is measured",
                              "flops_per_step": FLOPS_PER_STEP},
                 "clocks": clocks,
+                "time_to_1e-3": ttt,
                 "cpu_baseline": base}
         print(json.dumps(line))
     ctx.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def _franke_np(x, y):
+    return (0.75 * np.exp(-0.25 * ((9 * x - 2) ** 2 + (9 * y - 2) ** 2)) +
+            0.75 * np.exp(-((9 * x + 1) ** 2) / 49 - 0.1 * (9 * y + 1)) +
+            0.5 * np.exp(-0.25 * ((9 * x - 7) ** 2 + (9 * y - 3) ** 2)) -
+            0.2 * np.exp(-((9 * x - 4) ** 2) - (9 * y - 7) ** 2))
+
+
+def _u_aniso(xy):
+    return _franke_np(xy[:, 0], xy[:, 1]) * (1 + xy[:, 0] * xy[:, 1])
+
+
+def _assemble_stats(ctx, mesh, bvp, paths, prec, h):
+    """One fk_assemble call into host buffers; returns (seconds, per-item stats)."""
+    from spac_gb300 import fk
+    info = ctx.mesh_info(mesh)
+    st = (fk.Stats * info["n_items"])()
+    val = np.empty(info["nnz"])
+    B = np.empty(info["n_rows"])
+    t0 = time.perf_counter()
+    ctx.check(ctx.L.fk_assemble(ctx.h, mesh, bvp, int(paths), None, h, prec, val.ctypes.data_as(fk._dp),
+                                B.ctypes.data_as(fk._dp), None, None, st))
+    return time.perf_counter() - t0, fk.stats_array(st)
+
+
+def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
+    """time_to_target at the configured h and at smaller steps (the bias floor
+    of the configured h can exceed the target)."""
+    res = {}
+    for h in hs:
+        res["h=%g" % h] = time_to_target(ctx, mesh, target=target, h=h)
+    return res
+
+
+def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=1000, pilot_h=5e-4, train_steps=2000,
+                   table=512):
+    """Time to `target` RMS node error on the assembly, plain FK vs the learned
+    control variate (both FP32 stepping, same h).
+
+    Node error of an item = its FK estimate of u at the node (exit value taken
+    exactly, so the figure does not depend on the exit stencil) minus the exact
+    u.  RMS^2 = bias^2 + mean(var)/N: each method's N comes from an untimed
+    calibration run.  The learned-CV time includes its pilot (whole-domain
+    point solves at pilot_grid^2 collocation points: boundary data only),
+    training (train_steps Adam steps, batch 4096), the gradient table and the
+    assembly with the control term."""
+    from spac_gb300 import fk
+    info = ctx.mesh_info(mesh)
+    row, ixy, stn, fr = ctx.mesh_items(mesh)
+    u_exact = _u_aniso(ixy)
+    prec = fk.FP32
+    b_plain = ctx.register_bvp(fk.ANISO)
+
+    def rms_of(st):
+        return float(np.sqrt(np.mean((st["phi_VR"] - u_exact) ** 2)))
+
+    # calibration of the plain method
+    n_cal = 4000
+    _, st = _assemble_stats(ctx, mesh, b_plain, n_cal, prec, h)
+    var_p = np.maximum(st["phiphi_VR"] - st["phi_VR"] ** 2, 0)
+    bias2 = max(rms_of(st) ** 2 - var_p.mean() / n_cal, 0.0)
+    out = {"target": target, "bias_rms_est": float(np.sqrt(bias2)), "plain_var_mean": float(var_p.mean())}
+    if bias2 >= 0.8 * target ** 2:
+        out["unreachable"] = "bias floor at h=%g is above 0.9 x target" % h
+        return out
+    budget = target ** 2 - bias2
+    n_plain = int(np.ceil(1.05 * var_p.mean() / budget))
+    t_plain, st = _assemble_stats(ctx, mesh, b_plain, n_plain, prec, h)
+    out["plain"] = {"paths_per_item": n_plain, "seconds": t_plain, "rms": rms_of(st)}
+
+    # learned control variate: pilot from boundary data only
+    t0 = time.perf_counter()
+    g = (np.arange(pilot_grid) + 0.5) / pilot_grid
+    pxy = np.array([(x, y) for x in g for y in g])
+    # the pilot only has to approximate u (any u_hat keeps the estimator
+    # unbiased), so it runs at the coarse step pilot_h
+    pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec)
+    t_pilot = time.perf_counter() - t0
+    rects = np.array([[0.0, 0.0, 1.0, 1.0]])
+    mid = fk.C.c_int()
+    ctx.check(ctx.L.fk_mlp_create(ctx.h, 1, rects.ctypes.data_as(fk._dp), 12345, fk.C.byref(mid)))
+    mid = mid.value
+    tgt = np.ascontiguousarray(pst["phi"])
+    pxy = np.ascontiguousarray(pxy)
+    hist = np.zeros(train_steps, dtype=np.float32)
+    t1 = time.perf_counter()
+    ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp), None,
+                                 train_steps, 4096, 1e-2, 777, hist.ctypes.data_as(fk._fp)))
+    t_train = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
+    t_table = time.perf_counter() - t2
+    b_cv = ctx.register_bvp(fk.ANISO, cv=fk.CV_MLP, mlp_id=mid)
+    # calibration of the control-variate run (untimed, as for plain)
+    _, stc = _assemble_stats(ctx, mesh, b_cv, n_cal, prec, h)
+    var_c = np.maximum(stc["phiphi_VR"] - stc["phi_VR"] ** 2, 0)
+    n_cv = max(32, int(np.ceil(1.05 * var_c.mean() / budget)))
+    t_run, stc = _assemble_stats(ctx, mesh, b_cv, n_cv, prec, h)
+    t_cv = t_pilot + t_train + t_table + t_run
+    out["learned_cv"] = {"paths_per_item": n_cv, "seconds": t_cv, "rms": rms_of(stc), "pilot_s": t_pilot,
+                         "train_s": t_train, "table_s": t_table, "run_s": t_run,
+                         "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
+                         "train_loss_first_last": [float(hist[0]), float(hist[-1])]}
+    out["variance_reduction"] = float(var_p.mean() / max(var_c.mean(), 1e-300))
+    out["speedup_cv_over_plain"] = t_plain / t_cv
+    out["speedup_cv_run_only"] = t_plain / t_run
+    return out
 
 
 def _mean_steps(ctx, mesh, bvp, prec, paths):

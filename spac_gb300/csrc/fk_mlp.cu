@@ -38,18 +38,29 @@ Mlp::~Mlp() {
 namespace {
 
 constexpr int W = 64;
-constexpr int kRows = 128;      // rows per CTA pass
-constexpr int kThreads = 128;
+constexpr int kRows = 64;       // rows per CTA pass (the step is latency-bound: short chains)
+constexpr int kThreads = 128;   // 4 warps
+constexpr int kWarpRows = kRows / 4;
+constexpr int kMT = kWarpRows / 16;  // m16 tiles per warp
 constexpr int LD = 72;          // bf16 leading dimension of [rows][64] tiles (144 B rows)
-constexpr int LDT = 136;        // bf16 leading dimension of [64][128] transposed tiles (272 B rows)
+constexpr int LDT = kRows + 8;  // bf16 leading dimension of [64][rows] transposed tiles (16 B multiple)
+static_assert(kMT >= 1 && kWarpRows % 16 == 0, "rows per warp");
 constexpr int OFF_W1 = 0, OFF_B1 = 128, OFF_W2 = 192, OFF_B2 = OFF_W2 + W * W, OFF_W3 = OFF_B2 + W,
               OFF_B3 = OFF_W3 + W * W, OFF_W4 = OFF_B3 + W, OFF_B4 = OFF_W4 + W, NPARAM = OFF_B4 + 1;
 constexpr int BF_PER_REGION = 4 * W * W;  // W2, W2^T, W3, W3^T
 
 enum { MODE_TRAIN = 0, MODE_LOSSGRAD = 1, MODE_GRADX = 2 };
 
+// SiLU and its derivative with the logistic function from the SFU tanh:
+// sigmoid(z) = 1/2 + tanh(z/2)/2 (tanh.approx.f32, max rel. error ~2^-11,
+// below the BF16 rounding these values go through).
+__device__ __forceinline__ float tanh_approx(float v) {
+  float r;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
 __device__ __forceinline__ float silu_f(float z, float& dsilu) {
-  const float s = 1.0f / (1.0f + __expf(-z));
+  const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
   dsilu = s * (1.0f + z * (1.0f - s));
   return z * s;
 }
@@ -93,13 +104,14 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
   const int region = blockIdx.y, cta = blockIdx.x;
   const float* P = a.params + static_cast<long long>(region) * NPARAM;
   const __nv_bfloat16* WB = a.wbf + static_cast<long long>(region) * BF_PER_REGION;
-  // weights into shared memory
-  for (int e = tid; e < W * W; e += kThreads) {
-    const int r = e / W, c = e % W;
-    S.w2[r * LD + c] = WB[e];
-    S.w2t[r * LD + c] = WB[W * W + e];
-    S.w3[r * LD + c] = WB[2 * W * W + e];
-    S.w3t[r * LD + c] = WB[3 * W * W + e];
+  // weights into shared memory, 8 bf16 (16 bytes) per load
+  for (int e8 = tid; e8 < W * W / 8; e8 += kThreads) {
+    const int r = (e8 * 8) / W, c = (e8 * 8) % W;
+    const uint4* src = reinterpret_cast<const uint4*>(WB) + e8;
+    *reinterpret_cast<uint4*>(&S.w2[r * LD + c]) = __ldg(src);
+    *reinterpret_cast<uint4*>(&S.w2t[r * LD + c]) = __ldg(src + W * W / 8);
+    *reinterpret_cast<uint4*>(&S.w3[r * LD + c]) = __ldg(src + 2 * W * W / 8);
+    *reinterpret_cast<uint4*>(&S.w3t[r * LD + c]) = __ldg(src + 3 * W * W / 8);
   }
   for (int e = tid; e < 2 * W; e += kThreads) S.w1[e] = P[OFF_W1 + e];
   for (int e = tid; e < W; e += kThreads) {
@@ -129,7 +141,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
 
   for (int tile = 0; tile < n_tiles; ++tile) {
     // ---- samples: row tid of this tile
-    {
+    if (tid < kRows) {
       const int r = tid;
       float x = 0.f, y = 0.f, tg = 0.f;
       int valid = 0;
@@ -158,17 +170,19 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
           x = s.x; y = s.y; tg = s.z;
         }
       }
-      float z0 = (x - nm.x) * nm.z, z1 = (y - nm.y) * nm.w;
+      const float z0 = (x - nm.x) * nm.z, z1 = (y - nm.y) * nm.w;
       S.z[r][0] = z0; S.z[r][1] = z1; S.tgt[r] = tg; S.valid[r] = valid;
-      // layer 1 (K = 2) in FP32
-      for (int j = 0; j < W; ++j) {
-        const float p = S.w1[2 * j] * z0 + S.w1[2 * j + 1] * z1 + S.b1[j];
-        float ds;
-        const float hv = silu_f(p, ds);
-        S.h1[r * LD + j] = __float2bfloat16_rn(hv);
-        S.s1[r * LD + j] = __float2bfloat16_rn(ds);
-        if (train) S.h1t[j * LDT + r] = __float2bfloat16_rn(hv);
-      }
+    }
+    __syncthreads();
+    // layer 1 (K = 2) in FP32; thread <-> (row, unit), unit-contiguous stores
+    for (int e = tid; e < kRows * W; e += kThreads) {
+      const int r = e >> 6, j = e & (W - 1);
+      const float p = fmaf(S.w1[2 * j], S.z[r][0], fmaf(S.w1[2 * j + 1], S.z[r][1], S.b1[j]));
+      float ds;
+      const float hv = silu_f(p, ds);
+      S.h1[r * LD + j] = __float2bfloat16_rn(hv);
+      S.s1[r * LD + j] = __float2bfloat16_rn(ds);
+      if (train) S.h1t[j * LDT + r] = __float2bfloat16_rn(hv);
     }
     __syncthreads();
     // ---- layers 2 and 3 on the tensor cores, warp w owns rows 32w..32w+31
@@ -178,22 +192,22 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
       const float* bias = layer == 0 ? S.b2 : S.b3;
       __nv_bfloat16* Hout = layer == 0 ? S.h2 : S.h3;
       __nv_bfloat16* Sout = layer == 0 ? S.s2 : S.s3;
-      float c[2][8][4];
+      float c[kMT][8][4];
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<2, 8, W>(c, Ain, LD, warp * 32, Bw, LD, 0, lane);
-      float orow[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+      warp_gemm_tn<kMT, 8, W>(c,Ain, LD, warp * kWarpRows,Bw, LD, 0, lane);
+      float orow[kMT][2] = {};
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int r = warp * 32 + mt * 16 + g + ((q >> 1) << 3);
+            const int r = warp * kWarpRows + mt * 16 + g + ((q >> 1) << 3);
             const int col = nt * 8 + 2 * t4 + (q & 1);
             float ds;
             const float hv = silu_f(c[mt][nt][q] + bias[col], ds);
@@ -205,19 +219,19 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
       if (layer == 1) {
         // output unit: reduce the row partial sums over the quad
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
+        for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
           for (int hh = 0; hh < 2; ++hh) {
             float v = orow[mt][hh];
             v += __shfl_xor_sync(0xffffffffu, v, 1);
             v += __shfl_xor_sync(0xffffffffu, v, 2);
-            if (t4 == 0) S.o[warp * 32 + mt * 16 + g + hh * 8] = v + S.b4;
+            if (t4 == 0) S.o[warp * kWarpRows + mt * 16 + g + hh * 8] = v + S.b4;
           }
       }
       __syncthreads();
     }
     // ---- output gradient and dp3 = dO * w4 * silu'(p3)
-    {
+    if (tid < kRows) {
       const int r = tid;
       const float o = S.o[r];
       float d;
@@ -229,12 +243,13 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
         d = 2.f * e * a.inv_batch;
       }
       S.dO[r] = d;
-      for (int j = 0; j < W; ++j) {
-        const float v = d * S.w4[j] * __bfloat162float(S.s3[r * LD + j]);
-        const __nv_bfloat16 vb = __float2bfloat16_rn(v);
-        S.dp[r * LD + j] = vb;
-        if (train) S.dpt[j * LDT + r] = vb;
-      }
+    }
+    __syncthreads();
+    for (int e = tid; e < kRows * W; e += kThreads) {
+      const int r = e >> 6, j = e & (W - 1);
+      const __nv_bfloat16 vb = __float2bfloat16_rn(S.dO[r] * S.w4[j] * __bfloat162float(S.s3[r * LD + j]));
+      S.dp[r * LD + j] = vb;
+      if (train) S.dpt[j * LDT + r] = vb;
     }
     __syncthreads();
     // layer-3 backward: dW3 += dp3^T h2, db3, dW4, db4; dh2 = dp3 W3
@@ -251,22 +266,22 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
       }
     }
     {
-      float c[2][8][4];
+      float c[kMT][8][4];
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<2, 8, W>(c, S.dp, LD, warp * 32, S.w3t, LD, 0, lane);
+      warp_gemm_tn<kMT, 8, W>(c,S.dp, LD, warp * kWarpRows,S.w3t, LD, 0, lane);
       __syncthreads();  // everyone is done reading dp / dpt of layer 3
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int r = warp * 32 + mt * 16 + g + ((q >> 1) << 3);
+            const int r = warp * kWarpRows + mt * 16 + g + ((q >> 1) << 3);
             const int col = nt * 8 + 2 * t4 + (q & 1);
             const __nv_bfloat16 vb = __float2bfloat16_rn(c[mt][nt][q] * __bfloat162float(S.s2[r * LD + col]));
             S.dp[r * LD + col] = vb;
@@ -281,25 +296,25 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
         for (int r = 0; r < kRows; ++r) gB2 += __bfloat162float(S.dp[r * LD + tid]);
     }
     {
-      float c[2][8][4];
+      float c[kMT][8][4];
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<2, 8, W>(c, S.dp, LD, warp * 32, S.w2t, LD, 0, lane);
+      warp_gemm_tn<kMT, 8, W>(c,S.dp, LD, warp * kWarpRows,S.w2t, LD, 0, lane);
       __syncthreads();
       // dp1 = dh1 * silu'(p1), kept in FP32 in the (now free) h3 / s3 area as pairs
       static_assert(sizeof(float) * kRows * W <= 2 * sizeof(__nv_bfloat16) * kRows * LD, "dp1 overlay");
       float* dp1 = reinterpret_cast<float*>(S.h3);  // [kRows][W] FP32 over h3 + s3
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt)
+      for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int r = warp * 32 + mt * 16 + g + ((q >> 1) << 3);
+            const int r = warp * kWarpRows + mt * 16 + g + ((q >> 1) << 3);
             const int col = nt * 8 + 2 * t4 + (q & 1);
             dp1[r * W + col] = c[mt][nt][q] * __bfloat162float(S.s1[r * LD + col]);
           }
@@ -307,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
     __syncthreads();
     {
       const float* dp1 = reinterpret_cast<const float*>(S.h3);
-      if (a.mode == MODE_GRADX) {
+      if (a.mode == MODE_GRADX && tid < kRows) {
         const int r = tid, pi = row0 + r;
         float gx = 0.f, gy = 0.f;
         for (int j = 0; j < W; ++j) {
@@ -319,7 +334,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
           a.out[3 * pi + 1] = gx * nm.z;
           a.out[3 * pi + 2] = gy * nm.w;
         }
-      } else if (tid < W) {
+      } else if (a.mode != MODE_GRADX && tid < W) {
         const int j = tid;
         for (int r = 0; r < kRows; ++r) {
           const float d = dp1[r * W + j];
@@ -368,12 +383,35 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
 __global__ void mlp_adam_kernel(float* params, __nv_bfloat16* wbf, float* m, float* v, const float* partial,
                                 const float* loss, int n_regions, int ctas, float lr, float b1, float b2, float eps,
                                 float bc1, float bc2, int apply, float* grad_out, float* hist, float loss_scale) {
+  // 8 lanes per parameter: lane q sums the partials c = q, q+8, ... (fixed
+  // order), then a fixed shuffle tree combines the 8 lane sums
   const long long total = static_cast<long long>(n_regions) * NPARAM;
-  for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
-       e += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const int r = static_cast<int>(e / NPARAM), p = static_cast<int>(e % NPARAM);
-    float gsum = 0.f;
-    for (int c = 0; c < ctas; ++c) gsum += partial[(static_cast<long long>(r) * ctas + c) * NPARAM + p];
+  const int sub = threadIdx.x & 7;
+  const long long lanes = static_cast<long long>(gridDim.x) * blockDim.x;
+  const long long rounds = (total * 8 + lanes - 1) / lanes;
+  for (long long it = 0; it < rounds; ++it) {
+    const long long e = (it * lanes + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 3;
+    const bool live = e < total;
+    float part = 0.f;
+    int r = 0, p = 0;
+    if (live) {
+      r = static_cast<int>(e / NPARAM);
+      p = static_cast<int>(e % NPARAM);
+      const float* src = partial + static_cast<long long>(r) * ctas * NPARAM + p;
+      float a0 = 0.f, a1 = 0.f;
+      int c = sub;
+      for (; c + 8 < ctas; c += 16) {
+        a0 += __ldg(src + static_cast<long long>(c) * NPARAM);
+        a1 += __ldg(src + static_cast<long long>(c + 8) * NPARAM);
+      }
+      if (c < ctas) a0 += __ldg(src + static_cast<long long>(c) * NPARAM);
+      part = a0 + a1;
+    }
+    part += __shfl_xor_sync(0xffffffffu, part, 1);
+    part += __shfl_xor_sync(0xffffffffu, part, 2);
+    part += __shfl_xor_sync(0xffffffffu, part, 4);
+    if (!live || sub != 0) continue;
+    const float gsum = part;
     if (grad_out) grad_out[e] = gsum;
     if (!apply) continue;
     const float mm = b1 * m[e] + (1.f - b1) * gsum;
@@ -551,7 +589,7 @@ static int upload_samples(Mlp& M, int n, const double* xy, const double* target,
 
 int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* region, int steps, int batch,
               double lr, unsigned long long seed, float* loss_hist, cudaStream_t s, std::string& err) {
-  if (steps < 0 || batch < kRows || batch % kRows) { err = "batch must be a positive multiple of 128"; return FK_ERR_ARG; }
+  if (steps < 0 || batch < kRows || batch % kRows) { err = "batch must be a positive multiple of 64"; return FK_ERR_ARG; }
   std::vector<int> off;
   int rc = upload_samples(M, n, xy, target, region, off, err);
   if (rc) return rc;
@@ -596,7 +634,7 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
   cudaGraph_t graph;
   e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
-  const int adam_blocks = static_cast<int>(std::min<size_t>((np + 255) / 256, 1024));
+  const int adam_blocks = static_cast<int>(std::min<size_t>((8 * np + 255) / 256, 4096));
   for (int st = 0; st < steps; ++st) {
     a.step = static_cast<uint32_t>(M.adam_t + st);
     mlp_pass_kernel<<<dim3(ctas, M.n_regions), kThreads, sizeof(Smem), s>>>(a);
