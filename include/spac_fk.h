@@ -129,6 +129,23 @@ int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsi
                     const double* h, const int* sub_shape, const double* sub_params,
                     int precision, fk_stats* out);
 
+/* Batched uneven point solves: n points, each of its own registered BVP
+ * (all of one problem functor and control mode), path count and step size,
+ * in ONE persistent launch: chunks of every point's paths are handed to the
+ * CTAs longest-first and finished paths are regenerated at once, so points
+ * with 1e3 and 1e5 paths and different h share the grid without idling.
+ * No reference counterpart beyond Solve_OMP_Analytic(X0,...) called per point. */
+int fk_solve_points_multi(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy, const unsigned* paths,
+                          const double* h, int precision, fk_stats* out);
+/* Autotuner of the persistent launch: times the path kernel (CUDA events) on
+ * the given batched solve with every path count scaled by sample_fraction,
+ * for block sizes {64, 128, 256} x chunk sizes {512, 2048, 8192, 32768}, and
+ * keeps the fastest pair in the context (as fk_set_launch).  The tuning runs
+ * do not advance the context's random stream id. */
+int fk_autotune_points(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy, const unsigned* paths,
+                       const double* h, int precision, double sample_fraction, int* best_block, int* best_chunk,
+                       double* best_ms);
+
 /* ---- point solves without any allocation ----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory while they solve: code running during CUDA stream capture, embedders

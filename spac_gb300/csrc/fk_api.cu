@@ -250,7 +250,9 @@ struct RunOut {
 
 int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::ItemDev>& items, fk::StencilSet* S,
               const std::vector<long long>* g_off, long long g_total, const int* d_csr_idx, double* d_csr_val,
-              const int* d_row, double* d_B, RunOut& out) {
+              const int* d_row, double* d_B, RunOut& out, bool multi_bvp = false) {
+  // multi_bvp: items carry their own BVP index (same functor and control mode
+  // as bvp_id); otherwise every item uses bvp_id
   cudaStream_t s = ctx->stream;
   const int n = static_cast<int>(items.size());
   const int kind = S ? S->kind : 0;
@@ -265,6 +267,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   if (S) n_stencils = static_cast<int>(S->kind == 1 ? S->arcs.size() : S->patches.size());
   const bool per_stencil = bvp.cv == FK_CV_MLP && n_stencils > 0 && ctx->mlps[bvp.mlp]->n_regions == n_stencils;
   for (auto& x : it) {
+    if (!multi_bvp) x.bvp = bvp_id;
     x.cv_region = (per_stencil && x.stencil >= 0) ? x.stencil : 0;
     x.acc_off = acc_total;
     if (kind != 0 && x.stencil >= 0) {
@@ -317,7 +320,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
 
   fk::LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.bvp = ctx->d_bvps.as<fk::BvpDev>() + bvp_id;
+  a.bvp = ctx->d_bvps.as<fk::BvpDev>();
   a.items = ctx->w_items.as<fk::ItemDev>();
   a.chunks = ctx->w_chunks.as<fk::ChunkDev>();
   a.n_chunks = static_cast<int>(chunks.size());
@@ -529,6 +532,88 @@ int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsi
   FK_CUDA(cudaMemcpy(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
   for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &out[i]);
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+// Points of several registered BVPs (one problem functor and control mode) in
+// one persistent launch.
+static int build_multi(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy, const unsigned* paths,
+                       const double* h, double paths_scale, std::vector<fk::ItemDev>& items) {
+  items.assign(n, fk::ItemDev());
+  const fk::BvpDev& b0 = ctx->bvps[bvp_ids[0]];
+  for (int i = 0; i < n; ++i) {
+    if (check_bvp(ctx, bvp_ids[i])) return FK_ERR_REGISTRY;
+    const fk::BvpDev& b = ctx->bvps[bvp_ids[i]];
+    if (b.problem != b0.problem || b.cv != b0.cv || b.mlp != b0.mlp)
+      return fail(ctx, FK_ERR_ARG, "one launch needs BVPs of one problem functor and control mode");
+    if (!(h[i] > 0) || !std::isfinite(xy[2 * i]) || !std::isfinite(xy[2 * i + 1]))
+      return fail(ctx, FK_ERR_ARG, "point solve: h must be > 0 and coordinates finite");
+    fk::ItemDev& it = items[i];
+    std::memset(&it, 0, sizeof(it));
+    it.x = xy[2 * i]; it.y = xy[2 * i + 1]; it.h = h[i]; it.sqrth = std::sqrt(h[i]);
+    it.paths = std::max(1u, static_cast<unsigned>(std::ceil(paths[i] * paths_scale)));
+    it.stencil = -1; it.sub_shape = -1; it.bvp = bvp_ids[i];
+  }
+  return FK_OK;
+}
+
+int fk_solve_points_multi(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy, const unsigned* paths,
+                          const double* h, int precision, fk_stats* out) {
+  if (!ctx) return FK_ERR_ARG;
+  if (n < 0 || (n > 0 && (!bvp_ids || !xy || !paths || !h || !out))) return fail(ctx, FK_ERR_ARG, "null argument");
+  if (n == 0) return FK_OK;
+  int rc = need_device(ctx);
+  if (rc) return rc;
+  std::vector<fk::ItemDev> items;
+  if ((rc = build_multi(ctx, n, bvp_ids, xy, paths, h, 1.0, items))) return rc;
+  RunOut ro;
+  rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro, true);
+  if (rc) return rc;
+  std::vector<double> st(static_cast<size_t>(n) * 16);
+  FK_CUDA(cudaMemcpy(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &out[i]);
+  if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+int fk_autotune_points(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy, const unsigned* paths,
+                       const double* h, int precision, double sample_fraction, int* best_block, int* best_chunk,
+                       double* best_ms) {
+  if (!ctx || n < 1 || !bvp_ids || !xy || !paths || !h) return fail(ctx, FK_ERR_ARG, "null argument");
+  if (!(sample_fraction > 0 && sample_fraction <= 1)) return fail(ctx, FK_ERR_ARG, "sample_fraction in (0, 1]");
+  int rc = need_device(ctx);
+  if (rc) return rc;
+  std::vector<fk::ItemDev> items;
+  if ((rc = build_multi(ctx, n, bvp_ids, xy, paths, h, sample_fraction, items))) return rc;
+  const unsigned saved_stream = ctx->stream_id;
+  const int blocks[] = {64, 128, 256};
+  const int chunks[] = {512, 2048, 8192, 32768};
+  int bb = 256, bc = 0;
+  double best = 1e300;
+  for (int b : blocks)
+    for (int c : chunks) {
+      if (c % b) continue;
+      ctx->block = b;
+      ctx->chunk = c;
+      double t = 1e300;
+      for (int rep = 0; rep < 2; ++rep) {
+        RunOut ro;
+        rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro,
+                       true);
+        if (rc && rc != FK_ERR_STEP_CAP) {
+          ctx->stream_id = saved_stream;
+          return rc;
+        }
+        t = std::min(t, ctx->timing[0]);
+      }
+      if (t < best) { best = t; bb = b; bc = c; }
+    }
+  ctx->block = bb;
+  ctx->chunk = bc;
+  ctx->stream_id = saved_stream;  // tuning runs do not advance the random stream
+  if (best_block) *best_block = bb;
+  if (best_chunk) *best_chunk = bc;
+  if (best_ms) *best_ms = best;
   return FK_OK;
 }
 

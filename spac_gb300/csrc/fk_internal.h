@@ -18,7 +18,7 @@ struct ItemDev {
   int frontera;           // B = g(x), no paths
   int sub_shape;          // point solves: 0 rect, 1 circle, -1 = domain
   int cv_region;          // learned control variate: region of the grad table
-  int pad_;
+  int bvp;                // index into the launch's BVP records
   long long acc_off;      // first double of this item's stencil accumulator
 };
 

@@ -22,19 +22,21 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
   const int item = blockIdx.x;
   if (item >= a.n_items) return;
   const ItemDev it = a.items[item];
-  const BvpDev bvp = *a.bvp;
+  const BvpDev bvp = a.bvp[it.bvp];
   const double N = static_cast<double>(it.paths);
   const double* S = a.stats + static_cast<long long>(item) * kNumStats;
   double Bv;
+  // an item given no paths contributes nothing (G = 0, B = 0)
+  const bool live = !it.frontera && it.paths > 0;
   if (it.frontera) {
     Bv = Problem<PROB>::u(bvp, it.x, it.y);  // Solve_OMP_Analytic :346-347
   } else {
-    Bv = S[7] / N;
+    Bv = live ? S[7] / N : 0.0;
   }
   if (threadIdx.x == 0) {
     if (a.item_stats) {
       double* o = a.item_stats + static_cast<long long>(item) * 16;
-      if (it.frontera) {
+      if (!live) {
         for (int j = 0; j < 16; ++j) o[j] = 0.0;
         o[9] = Bv;
       } else {
@@ -56,12 +58,12 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
     const double* iPsi = a.arc_ipsi + arc.ipsi_off;
     for (int j = threadIdx.x; j < arc.n; j += blockDim.x) {
       double g = 0.0;
-      if (!it.frontera) {
+      if (live) {
         for (int i = 0; i < arc.n; ++i) g += iPsi[i + j * arc.n] * acc[i];
         g = -g / N;
       }
       if (a.item_G) a.item_G[goff + j] = g;
-      if (a.csr_val && !it.frontera) a.csr_val[a.csr_idx[goff + j]] += g;
+      if (a.csr_val && live) a.csr_val[a.csr_idx[goff + j]] += g;
     }
   } else {
     const PatchDev P = a.patches[it.stencil];
@@ -69,7 +71,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
     const int m = P.m, k = P.k;
     for (int gi = threadIdx.x; gi < m; gi += blockDim.x) {
       double g = 0.0;
-      if (!it.frontera) {
+      if (live) {
         if (P.closed) {
           for (int t = 0; t < k; ++t) {
             int W = gi - t;
@@ -90,7 +92,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
         g = -g / N;
       }
       if (a.item_G) a.item_G[goff + gi] = g;
-      if (a.csr_val && !it.frontera) a.csr_val[a.csr_idx[goff + gi]] += g;
+      if (a.csr_val && live) a.csr_val[a.csr_idx[goff + gi]] += g;
     }
   }
 }

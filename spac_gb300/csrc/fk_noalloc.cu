@@ -78,7 +78,7 @@ __global__ void noalloc_prepare(BvpDev bvp, int n, const double* xy, const unsig
   it.frontera = 0;
   it.sub_shape = -1;
   it.cv_region = 0;
-  it.pad_ = 0;
+  it.bvp = 0;
   it.acc_off = 0;
   items[i] = it;
   chunks[i] = ChunkDev{i, 0u, paths[i]};

@@ -133,12 +133,10 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
   __shared__ ArcDev sarc;
   __shared__ ExitQueue<R> sq[kMaxBlockWarps];
 
-  const BvpDev& bvp = *a.bvp;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const bool cv = a.cv != 0;         // any control term
   const bool cv_exact = a.cv == 1;   // F from the problem functor
   const bool cv_table = a.cv == 2;   // F from the learned gradient table
-  const R d0 = R(bvp.dom[0]), d1 = R(bvp.dom[1]), d2 = R(bvp.dom[2]), d3 = R(bvp.dom[3]);
 
   for (;;) {
     if (threadIdx.x == 0) s_chunk = atomicAdd(a.queue, 1);
@@ -169,6 +167,9 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
     if (threadIdx.x == 0) s_next = ch.p0 + blockDim.x;
     __syncthreads();
 
+    // the item's BVP (independent problems of one functor share a launch)
+    const BvpDev& bvp = a.bvp[itg.bvp];
+    const R d0 = R(bvp.dom[0]), d1 = R(bvp.dom[1]), d2 = R(bvp.dom[2]), d3 = R(bvp.dom[3]);
     const R h = R(itg.h), sqrth = R(itg.sqrth), x0 = R(itg.x), y0 = R(itg.y);
     const R s0 = R(itg.sub[0]), s1 = R(itg.sub[1]), s2 = R(itg.sub[2]), s3 = R(itg.sub[3]);
     const bool has_sub = (ST != 0) || itg.sub_shape >= 0;

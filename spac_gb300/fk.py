@@ -70,6 +70,8 @@ _SIGS = {
     "fk_register_bvp": (C.c_int, [C.c_void_p, C.POINTER(BvpDesc), _ip]),
     "fk_solve_points": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _up, _dp, _ip, _dp, C.c_int,
                                   C.POINTER(Stats)]),
+    "fk_solve_points_multi": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _up, _dp, C.c_int, C.POINTER(Stats)]),
+    "fk_autotune_points": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _up, _dp, C.c_int, C.c_double, _ip, _ip, _dp]),
     "fk_register_arc": (C.c_int, [C.c_void_p, C.POINTER(ArcDesc), _ip]),
     "fk_arc_ipsi": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "fk_solve_nodes_arc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(NodeItem), C.c_int, _dp, _dp,
@@ -220,6 +222,27 @@ class Context:
         self.check(rc, allow)
         return stats_array(out)
 
+    def solve_points_multi(self, bvp_ids, xy, paths, h, precision=FP64, allow=()):
+        xy, pxy = _d(np.reshape(xy, (-1, 2)))
+        n = xy.shape[0]
+        ids, pid = _i(np.broadcast_to(bvp_ids, (n,)))
+        paths, pp = _u(np.broadcast_to(paths, (n,)))
+        h, ph = _d(np.broadcast_to(h, (n,)))
+        out = (Stats * n)()
+        self.check(self.L.fk_solve_points_multi(self.h, n, pid, pxy, pp, ph, precision, out), allow)
+        return stats_array(out)
+
+    def autotune_points(self, bvp_ids, xy, paths, h, precision=FP64, sample_fraction=0.1):
+        xy, pxy = _d(np.reshape(xy, (-1, 2)))
+        n = xy.shape[0]
+        ids, pid = _i(np.broadcast_to(bvp_ids, (n,)))
+        paths, pp = _u(np.broadcast_to(paths, (n,)))
+        h, ph = _d(np.broadcast_to(h, (n,)))
+        b, c, t = C.c_int(), C.c_int(), C.c_double()
+        self.check(self.L.fk_autotune_points(self.h, n, pid, pxy, pp, ph, precision, sample_fraction, C.byref(b),
+                                             C.byref(c), C.byref(t)))
+        return b.value, c.value, t.value
+
     # -- arcs / node solves
     def register_arc(self, cx, cy, radius, c2, interior, theta, gids, iPsi=None):
         theta, pt = _d(theta)
@@ -302,22 +325,27 @@ class Context:
                                       v0.ctypes.data_as(_dp)))
         return rp, col, v0
 
-    def assemble(self, mesh, bvp, paths, h, precision=FP64, paths_per_item=None, items=True, allow=()):
+    def assemble(self, mesh, bvp, paths, h, precision=FP64, paths_per_item=None, items=True, item_G=True, csr=True,
+                 allow=()):
+        """fk_assemble into numpy arrays.  items: per-item B and statistics;
+        item_G: per-item G rows too; csr: the CSR values and B."""
         info = self.mesh_info(mesh)
-        val = np.zeros(info["nnz"])
-        B = np.zeros(info["n_rows"])
+        val = np.zeros(info["nnz"]) if csr else None
+        B = np.zeros(info["n_rows"]) if csr else None
         pp = None
         if paths_per_item is not None:
             ppi, pp = _u(paths_per_item)
         G = iB = st = None
         if items:
-            sizes = [len(self.mesh_stencil_nodes(mesh, s)) for s in range(info["n_stencils"])]
-            _, _, stn, _ = self.mesh_items(mesh)
-            G = np.zeros(int(sum(sizes[s] for s in stn)))
+            if item_G:
+                sizes = [len(self.mesh_stencil_nodes(mesh, s)) for s in range(info["n_stencils"])]
+                _, _, stn, _ = self.mesh_items(mesh)
+                G = np.zeros(int(sum(sizes[s] for s in stn)))
             iB = np.zeros(info["n_items"])
             st = (Stats * info["n_items"])()
-        rc = self.L.fk_assemble(self.h, mesh, bvp, int(paths), pp, h, precision, val.ctypes.data_as(_dp),
-                                B.ctypes.data_as(_dp), G.ctypes.data_as(_dp) if items else None,
+        rc = self.L.fk_assemble(self.h, mesh, bvp, int(paths), pp, h, precision,
+                                val.ctypes.data_as(_dp) if csr else None, B.ctypes.data_as(_dp) if csr else None,
+                                G.ctypes.data_as(_dp) if G is not None else None,
                                 iB.ctypes.data_as(_dp) if items else None, st if items else None)
         self.check(rc, allow)
         return dict(val=val, B=B, item_G=G, item_B=iB, item_stats=stats_array(st) if items else None)

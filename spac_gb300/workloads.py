@@ -1,0 +1,204 @@
+"""Named synthetic workloads of the Feynman-Kac hot path and their runners.
+
+  point_solves  32 x 32 grid nodes (i/33, j/33) of the Franke Poisson problem
+                on [0,1]^2, 1e4 paths per node, h = 1e-3 (FP64 and FP32)
+  assembly      square-patch G/B assembly (see bench.py for the 8 x 8 preset)
+  uneven        16 independent disk BVPs, radius ~ U[0.25, 1], 2^14 nodes
+                (1024 per disk, uniform in area), paths log-uniform in
+                [1e3, 1e5], h in {1e-3, 5e-4}, one persistent launch with the
+                autotuned block/chunk
+  large         32 x 32 subdomains, 63 nodes per patch side, h = 2.5e-4,
+                paths added per item until its standard error is below 1e-4,
+                learned control variate with plain FK as the per-item fallback
+
+  python -m spac_gb300.workloads point_solves|uneven|large [--scale s]
+
+All inputs are seeded synthetic data; nothing is read from disk.
+"""
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import fk
+
+
+def franke(x, y):
+    return (0.75 * np.exp(-0.25 * ((9 * x - 2) ** 2 + (9 * y - 2) ** 2)) +
+            0.75 * np.exp(-((9 * x + 1) ** 2) / 49 - 0.1 * (9 * y + 1)) +
+            0.5 * np.exp(-0.25 * ((9 * x - 7) ** 2 + (9 * y - 3) ** 2)) -
+            0.2 * np.exp(-((9 * x - 4) ** 2) - (9 * y - 7) ** 2))
+
+
+def _sync_time(fn):
+    t0 = time.perf_counter()
+    r = fn()
+    return r, time.perf_counter() - t0
+
+
+def point_solves(ctx, paths=10000, h=1e-3, precisions=(fk.FP64, fk.FP32)):
+    g = np.arange(1, 33) / 33.0
+    xy = np.array([(x, y) for x in g for y in g])
+    u = franke(xy[:, 0], xy[:, 1])
+    b = ctx.register_bvp(fk.FRANKE)
+    out = {"nodes": len(xy), "paths_per_node": paths, "h": h}
+    for prec in precisions:
+        ctx.solve_points(b, xy[:8], 64, h, prec)  # warm-up
+        st, t = _sync_time(lambda: ctx.solve_points(b, xy, paths, h, prec))
+        k_ms = ctx.last_timing()[0]
+        err = st["phi"] - u
+        se = np.sqrt(np.maximum(st["phiphi"] - st["phi"] ** 2, 0) / paths)
+        name = "fp64" if prec == fk.FP64 else "fp32"
+        out[name] = {"seconds": t, "kernel_ms": k_ms, "paths_per_s": len(xy) * paths / t,
+                     "node_solves_per_s": len(xy) / t, "path_steps_per_s": len(xy) * paths * st["mean_steps"].mean() / t,
+                     "mean_steps": float(st["mean_steps"].mean()), "rms_error": float(np.sqrt(np.mean(err ** 2))),
+                     "mean_se": float(se.mean()), "max_abs_z": float(np.max(np.abs(err) / se)),
+                     "bias_rms_est": float(np.sqrt(max(np.mean(err ** 2) - np.mean(se ** 2), 0.0)))}
+    return out
+
+
+def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp64_fraction=0.05):
+    rng = np.random.default_rng(seed)
+    R = rng.uniform(0.25, 1.0, n_bvp)
+    centers = np.stack([2.5 * np.arange(n_bvp), np.zeros(n_bvp)], axis=1)
+    per = nodes // n_bvp
+    ids, xy, bvp_of = [], [], []
+    for k in range(n_bvp):
+        bid = ctx.register_bvp(fk.DISK, dom=(R[k], centers[k, 0], centers[k, 1]),
+                               prob=(centers[k, 0], centers[k, 1], R[k], 0.0))
+        ids.append(bid)
+        r = R[k] * np.sqrt(rng.uniform(0, 1, per))
+        th = rng.uniform(0, 2 * np.pi, per)
+        xy.append(np.stack([centers[k, 0] + r * np.cos(th), centers[k, 1] + r * np.sin(th)], axis=1))
+        bvp_of += [k] * per
+    xy = np.concatenate(xy)
+    bvp_of = np.array(bvp_of)
+    bvp_ids = np.array(ids, dtype=np.int32)[bvp_of]
+    paths = np.exp(rng.uniform(np.log(1e3), np.log(1e5), len(xy)))
+    paths = np.maximum(1, np.round(paths * scale)).astype(np.uint32)
+    h = rng.choice([1e-3, 5e-4], len(xy))
+    xi = (xy[:, 0] - centers[bvp_of, 0]) / (2 * R[bvp_of]) + 0.5
+    eta = (xy[:, 1] - centers[bvp_of, 1]) / (2 * R[bvp_of]) + 0.5
+    u = franke(xi, eta)
+    out = {"bvps": n_bvp, "nodes": len(xy), "total_paths": int(paths.sum()), "radius": R.tolist()}
+    if autotune:
+        bb, bc, tms = ctx.autotune_points(bvp_ids, xy, paths, h, fk.FP32, sample_fraction=0.05)
+        out["autotune"] = {"block": bb, "chunk": bc, "sample_kernel_ms": tms}
+    ctx.solve_points_multi(bvp_ids[:64], xy[:64], 100, h[:64], fk.FP32)  # warm-up
+    st, t = _sync_time(lambda: ctx.solve_points_multi(bvp_ids, xy, paths, h, fk.FP32))
+    steps = float((st["mean_steps"] * paths).sum())
+    out["fp32"] = {"seconds": t, "kernel_ms": ctx.last_timing()[0], "paths_per_s": paths.sum() / t,
+                   "path_steps_per_s": steps / t, "mean_steps": steps / paths.sum()}
+    err32 = st["phi"] - u
+    se32 = np.sqrt(np.maximum(st["phiphi"] - st["phi"] ** 2, 0) / paths)
+    # FP64 on a subsample of the same nodes (paths scaled) for the precision comparison
+    sub = rng.choice(len(xy), size=max(64, int(fp64_fraction * len(xy))), replace=False)
+    p64 = np.maximum(1000, paths[sub] // 4).astype(np.uint32)
+    s64, t64 = _sync_time(lambda: ctx.solve_points_multi(bvp_ids[sub], xy[sub], p64, h[sub], fk.FP64))
+    s32 = ctx.solve_points_multi(bvp_ids[sub], xy[sub], p64, h[sub], fk.FP32)
+    out["fp64_vs_fp32"] = {"nodes": len(sub), "paths": int(p64.sum()), "fp64_seconds": t64,
+                           "fp64_paths_per_s": p64.sum() / t64,
+                           "rms_error_fp64": float(np.sqrt(np.mean((s64["phi"] - u[sub]) ** 2))),
+                           "rms_error_fp32": float(np.sqrt(np.mean((s32["phi"] - u[sub]) ** 2))),
+                           "rms_fp32_minus_fp64": float(np.sqrt(np.mean((s32["phi"] - s64["phi"]) ** 2)))}
+    per_bvp = []
+    for k in range(n_bvp):
+        sel = bvp_of == k
+        _, tk = _sync_time(lambda: ctx.solve_points_multi(bvp_ids[sel], xy[sel], paths[sel], h[sel], fk.FP32))
+        per_bvp.append({"radius": float(R[k]), "paths": int(paths[sel].sum()),
+                        "paths_per_s_alone": float(paths[sel].sum() / tk),
+                        "rms_error_fp32": float(np.sqrt(np.mean(err32[sel] ** 2))),
+                        "mean_se_fp32": float(se32[sel].mean())})
+    out["per_bvp"] = per_bvp
+    out["sum_of_separate_seconds"] = float(sum(p["paths"] / p["paths_per_s_alone"] for p in per_bvp))
+    return out
+
+
+def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_paths=256, max_rounds=6,
+          max_paths=4_000_000, train_steps=2000, table=256):
+    """Adaptive assembly: per item, paths until SE < se_target, learned control
+    variate where it lowers the variance, plain FK otherwise."""
+    mesh, t_mesh = _sync_time(lambda: ctx.mesh_square_patches((0, 0, 1, 1), n_sub, nodes_per_side, 0.25, 3.0, 20))
+    info = ctx.mesh_info(mesh)
+    n = info["n_items"]
+    row, ixy, stn, fr = ctx.mesh_items(mesh)
+    u = franke(ixy[:, 0], ixy[:, 1])
+    b_plain = ctx.register_bvp(fk.FRANKE)
+    t0 = time.perf_counter()
+    # pilot: plain assembly with few paths; its node estimates train the network
+    p0 = np.full(n, pilot_paths, dtype=np.uint32)
+    r0 = ctx.assemble(mesh, b_plain, 0, h, fk.FP32, paths_per_item=p0, item_G=False, csr=False)
+    nodes_xy, _ = ctx.mesh_nodes(mesh)
+    # node estimates: mean over the items of each row (the row's FK value estimates)
+    est = np.bincount(row, weights=r0["item_stats"]["phi_VR"], minlength=info["n_rows"]) / \
+        np.maximum(np.bincount(row, minlength=info["n_rows"]), 1)
+    rects = np.array([[0.0, 0.0, 1.0, 1.0]])
+    mid = fk.C.c_int()
+    ctx.check(ctx.L.fk_mlp_create(ctx.h, 1, rects.ctypes.data_as(fk._dp), 99, fk.C.byref(mid)))
+    mid = mid.value
+    nx = np.ascontiguousarray(nodes_xy)
+    tg = np.ascontiguousarray(est)
+    ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tg), nx.ctypes.data_as(fk._dp), tg.ctypes.data_as(fk._dp), None,
+                                 train_steps, 4096, 1e-2, 5, None))
+    ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
+    b_cv = ctx.register_bvp(fk.FRANKE, cv=fk.CV_MLP, mlp_id=mid)
+    rc = ctx.assemble(mesh, b_cv, 0, h, fk.FP32, paths_per_item=p0, item_G=False, csr=False)
+    v_plain = np.maximum(r0["item_stats"]["phiphi_VR"] - r0["item_stats"]["phi_VR"] ** 2, 1e-30)
+    v_cv = np.maximum(rc["item_stats"]["phiphi_VR"] - rc["item_stats"]["phi_VR"] ** 2, 1e-30)
+    use_cv = v_cv < v_plain  # plain FK is the fallback where the control variate does not help
+    var = np.where(use_cv, v_cv, v_plain)
+    # running sums per item (B, G rows and the estimate), weighted by paths
+    done = np.full(n, pilot_paths, dtype=np.int64)
+    sum_phi = np.where(use_cv, rc["item_stats"]["phi_VR"], r0["item_stats"]["phi_VR"]) * pilot_paths
+    sum_B = np.where(use_cv, rc["item_B"], r0["item_B"]) * pilot_paths
+    rounds, total_paths = 0, int(2 * pilot_paths * n)
+    while rounds < max_rounds:
+        need = np.ceil(var / se_target ** 2).astype(np.int64) - done
+        need = np.clip(need, 0, max_paths)
+        if need.max() <= 0:
+            break
+        for bvp_id, mask in ((b_cv, use_cv), (b_plain, ~use_cv)):
+            pp = np.where(mask, need, 0).astype(np.uint32)
+            if pp.max() == 0:
+                continue
+            r = ctx.assemble(mesh, bvp_id, 0, h, fk.FP32, paths_per_item=pp, item_G=False, csr=False)
+            m = pp > 0
+            sum_phi[m] += r["item_stats"]["phi_VR"][m] * pp[m]
+            sum_B[m] += r["item_B"][m] * pp[m]
+            vr = np.maximum(r["item_stats"]["phiphi_VR"] - r["item_stats"]["phi_VR"] ** 2, 1e-30)
+            var[m] = vr[m]
+            done[m] += pp[m]
+            total_paths += int(pp.sum())
+        rounds += 1
+    t_total = time.perf_counter() - t0
+    phi = sum_phi / done
+    se = np.sqrt(var / done)
+    return {"items": n, "rows": info["n_rows"], "nnz": info["nnz"], "mesh_seconds": t_mesh,
+            "assembly_seconds": t_total, "rounds": rounds, "total_paths": total_paths,
+            "paths_per_s": total_paths / t_total, "cv_items": int(use_cv.sum()),
+            "variance_reduction_median": float(np.median(v_plain / v_cv)),
+            "se_max": float(se.max()), "se_median": float(np.median(se)),
+            "items_below_target": float(np.mean(se <= se_target * 1.001)),
+            "rms_node_error": float(np.sqrt(np.mean((phi - u) ** 2))),
+            "paths_per_item_median": float(np.median(done))}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("workload", choices=["point_solves", "uneven", "large"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=2026)
+    a = ap.parse_args()
+    ctx = fk.Context(0, seed=a.seed)
+    if a.workload == "point_solves":
+        r = point_solves(ctx, paths=max(64, int(10000 * a.scale)))
+    elif a.workload == "uneven":
+        r = uneven(ctx, scale=a.scale)
+    else:
+        r = large(ctx, n_sub=max(2, int(round(32 * a.scale))), nodes_per_side=63 if a.scale >= 1 else 31)
+    print(json.dumps({"workload": a.workload, **r}))
+
+
+if __name__ == "__main__":
+    main()
