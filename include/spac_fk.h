@@ -213,6 +213,28 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
                 double h, int precision, double* val, double* B, double* item_G, double* item_B,
                 fk_stats* item_stats);
 
+/* ---- host-side consumers of the assembled system (no GPU needed) -----------
+ * Restarted GMRES(restart) with right Jacobi preconditioning on a CSR system,
+ * to check an assembled solution on the host.  Replaces, for checking only,
+ * SistemaLinealSolverGMRES::Resuelve (Solvers/SistemaLinealSolverGMRES.hpp:157-597,
+ * METIS + MUMPS Schwarz preconditioner over MPI).  x holds the initial guess.
+ * Returns FK_ERR_NOT_FOUND if the relative residual stays above 10 tol. */
+int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x, double tol,
+                 int max_iter, int restart, int* iters, double* rel_resid);
+/* The reference's text formats (values in C++ general format, as its
+ * setf(fixed, scientific) leaves them): dir/G.txt "row col value" (%.8g) and
+ * dir/B.txt (%.8g) -- SistemaLineal::Escribe_GB_COO (Mesh/SistemaLineal.cpp:96-110);
+ * dir/G_i.txt, G_j.txt, G_ij.txt and B.txt (%.10g) -- Escribe_GB_CSR (:124-138). */
+int fk_write_gb_coo(const char* dir, int n_rows, const int* rowptr, const int* col, const double* val,
+                    const double* B);
+int fk_write_gb_csr(const char* dir, int n_rows, const int* rowptr, const int* col, const double* val,
+                    const double* B);
+/* SistemaLineal::Lee_GB_COO (Mesh/SistemaLineal.cpp:139-164): header "nnz n_rows" then
+ * row-sorted "row col value" lines; call with NULL arrays for the sizes. */
+int fk_read_gb_coo(const char* path, int* n_rows, int* nnz, int* rowptr, int* col, double* val);
+/* Malla::Escribe_Posiciones (Mesh/Malla.cpp:99-112): "gid x y u" (%.12g) */
+int fk_write_positions(const char* path, int n, const int* gids, const double* xy, const double* u);
+
 /* ---- learned control variate ---------------------------------------------
  * No counterpart in the reference (its control-variate hook is the field F of
  * the BVP, Coeficiente_Vectorial F, set to -sigma^T grad u by hand).  One MLP

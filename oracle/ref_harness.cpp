@@ -13,6 +13,7 @@
 //       defined below with the reference's typedefs; u = Franke * (1+xy))
 #include <cstdio>
 #include <cstring>
+#include <unistd.h>
 #include <vector>
 #include <map>
 #include <string>
@@ -134,6 +135,8 @@ struct Last {
   std::vector<MeshNode> nodes;
   std::vector<MeshIface> ifaces;
 } g_last;
+
+std::string g_out_dir;
 
 void stats_of(const FeynmanKacSolver& s, double out[9]) {
   out[0] = s.phi;
@@ -306,8 +309,22 @@ int ref_assemble_circles(void* session, int problem, int use_F, const double dom
   }
   g_last.val.assign(S.G_ij, S.G_ij + S.nnz);
   g_last.B.assign(S.B, S.B + S.n_filas);
+  if (!g_out_dir.empty()) {
+    // the reference writes into ./Output/ (SistemaLineal.cpp:96-138, Malla.cpp:99-112)
+    char cwd[4096];
+    if (getcwd(cwd, sizeof(cwd)) && chdir(g_out_dir.c_str()) == 0) {
+      S.Escribe_GB_COO();
+      S.Escribe_GB_CSR();
+      mesh.Escribe_Posiciones(bvp);
+      if (chdir(cwd) != 0) return -1;
+    }
+  }
   return 0;
 }
+
+// Directory (containing Output/) where the next assembly writes the
+// reference's text outputs; empty = none.
+void ref_set_output_dir(const char* dir) { g_out_dir = dir ? dir : ""; }
 
 int ref_last_sizes(int* n_rows, int* nnz, int* n_items, int* n_nodes, int* n_ifaces) {
   *n_rows = g_last.n_rows; *nnz = g_last.nnz;

@@ -96,6 +96,11 @@ _SIGS = {
     "fk_mlp_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp]),
     "fk_mlp_build_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
+    "fk_gmres_csr": (C.c_int, [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, _ip, _dp]),
+    "fk_write_gb_coo": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _dp, _dp]),
+    "fk_write_gb_csr": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _dp, _dp]),
+    "fk_read_gb_coo": (C.c_int, [C.c_char_p, _ip, _ip, _ip, _ip, _dp]),
+    "fk_write_positions": (C.c_int, [C.c_char_p, C.c_int, _ip, _dp, _dp]),
     "fk_solve_points_noalloc": (C.c_int, [C.POINTER(BvpDesc), C.c_ulonglong, C.c_uint, C.c_int, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
 }
@@ -373,3 +378,52 @@ class FeynmanKacSolverGPU:
         for k in ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL", "RNGC"):
             setattr(self, k, float(st[k][0]))
         return self
+
+
+# ---- host-side consumers of the assembled system ------------------------------
+def gmres(rowptr, col, val, b, x0=None, tol=1e-10, max_iter=2000, restart=50):
+    """fk_gmres_csr: returns (x, iterations, relative residual, status)."""
+    L = load()
+    rp, prp = _i(rowptr)
+    cl, pcl = _i(col)
+    v, pv = _d(val)
+    bb, pb = _d(b)
+    x = np.array(np.zeros(len(bb)) if x0 is None else x0, dtype=np.float64)
+    it, res = C.c_int(), C.c_double()
+    rc = L.fk_gmres_csr(len(bb), prp, pcl, pv, pb, x.ctypes.data_as(_dp), tol, max_iter, restart, C.byref(it),
+                        C.byref(res))
+    return x, it.value, res.value, rc
+
+
+def write_gb(dir_, rowptr, col, val, B, fmt="coo"):
+    L = load()
+    rp, prp = _i(rowptr)
+    cl, pcl = _i(col)
+    v, pv = _d(val)
+    bb, pb = _d(B)
+    f = L.fk_write_gb_coo if fmt == "coo" else L.fk_write_gb_csr
+    return f(str(dir_).encode(), len(bb), prp, pcl, pv, pb)
+
+
+def read_gb_coo(path):
+    L = load()
+    nr, nz = C.c_int(), C.c_int()
+    rc = L.fk_read_gb_coo(str(path).encode(), C.byref(nr), C.byref(nz), None, None, None)
+    if rc != FK_OK:
+        raise FKError(rc, "fk_read_gb_coo: cannot read " + str(path))
+    rp = np.zeros(nr.value + 1, dtype=np.int32)
+    col = np.zeros(nz.value, dtype=np.int32)
+    val = np.zeros(nz.value)
+    rc = L.fk_read_gb_coo(str(path).encode(), C.byref(nr), C.byref(nz), rp.ctypes.data_as(_ip),
+                          col.ctypes.data_as(_ip), val.ctypes.data_as(_dp))
+    if rc != FK_OK:
+        raise FKError(rc, "fk_read_gb_coo: malformed " + str(path))
+    return rp, col, val
+
+
+def write_positions(path, gids, xy, u):
+    L = load()
+    g, pg = _i(gids)
+    p, pp = _d(np.reshape(xy, (-1, 2)))
+    uu, pu = _d(u)
+    return L.fk_write_positions(str(path).encode(), len(g), pg, pp, pu)

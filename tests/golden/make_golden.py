@@ -139,6 +139,22 @@ def main():
     for name, problem, use_F, N, h in ASSEMBLIES:
         a = mesh_and_assembly(L, name, problem, use_F, N, h, True)
         np.savez_compressed(os.path.join(HERE, f"assembly_{name}_p{problem}_f{use_F}.npz"), **a)
+    # the reference's text outputs of the first assembly (Escribe_GB_COO, then
+    # Escribe_GB_CSR, which rewrites B.txt with 10 decimals; Escribe_Posiciones)
+    import shutil
+    import tempfile
+    tmp = tempfile.mkdtemp()
+    os.makedirs(os.path.join(tmp, "Output"))
+    L.ref_set_output_dir.argtypes = [C.c_char_p]
+    L.ref_set_output_dir(tmp.encode())
+    name, problem, use_F, N, h = ASSEMBLIES[0]
+    mesh_and_assembly(L, name, problem, use_F, N, h, True)
+    L.ref_set_output_dir(b"")
+    out = os.path.join(HERE, "text_unit3")
+    os.makedirs(out, exist_ok=True)
+    for f in ("G.txt", "B.txt", "G_i.txt", "G_j.txt", "G_ij.txt", "knot_position.txt"):
+        shutil.copy(os.path.join(tmp, "Output", f), os.path.join(out, f))
+    shutil.rmtree(tmp)
     # point solves: each on a fresh session (sequential stream from the start)
     pts = []
     for problem, use_F, dom, (x, y), sk, sub, N, h in POINTS:
