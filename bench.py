@@ -442,13 +442,13 @@ def _mean_steps(ctx, mesh, bvp, prec, paths):
 
 def _read_traffic():
     """DRAM bytes per path-kernel launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
     if os.path.exists(p):
-        try:
-            with open(p) as f:
-                return json.load(f).get("paths_kernel_dram_bytes_per_launch")
-        except Exception:
-            return None
+        with open(p) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and parts[0] == "paths_kernel_dram_bytes_per_launch":
+                    return float(parts[1])
     return None
 
 

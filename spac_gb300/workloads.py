@@ -95,7 +95,9 @@ def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp
     # FP64 on a subsample of the same nodes (paths scaled) for the precision comparison
     sub = rng.choice(len(xy), size=max(64, int(fp64_fraction * len(xy))), replace=False)
     p64 = np.maximum(1000, paths[sub] // 4).astype(np.uint32)
+    stream = ctx.get_stream()  # both precisions on the same Philox stream: paired paths
     s64, t64 = _sync_time(lambda: ctx.solve_points_multi(bvp_ids[sub], xy[sub], p64, h[sub], fk.FP64))
+    ctx.set_stream(stream)
     s32 = ctx.solve_points_multi(bvp_ids[sub], xy[sub], p64, h[sub], fk.FP32)
     out["fp64_vs_fp32"] = {"nodes": len(sub), "paths": int(p64.sum()), "fp64_seconds": t64,
                            "fp64_paths_per_s": p64.sum() / t64,
