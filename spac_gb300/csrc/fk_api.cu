@@ -316,7 +316,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
   if (acc_total > 0) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
   FK_CUDA(ctx->w_queue.ensure(16));
-  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, sizeof(int), s));
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 2 * sizeof(int), s));
 
   fk::LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -385,11 +385,17 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   out.item_G = f.item_G;
   out.item_B = f.item_B;
   out.item_stats = f.item_stats;
-  // capped paths?
-  std::vector<double> cap(n);
+  // every requested path completed?  capped paths?
+  int qerr[2] = {0, 0};
+  FK_CUDA(cudaMemcpy(qerr, ctx->w_queue.p, sizeof(qerr), cudaMemcpyDeviceToHost));
+  if (qerr[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
   std::vector<double> st(static_cast<size_t>(n) * 16);
   FK_CUDA(cudaMemcpy(st.data(), f.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < n; ++i) if (st[static_cast<size_t>(i) * 16 + 12] > 0) out.capped = true;
+  for (int i = 0; i < n; ++i) {
+    if (st[static_cast<size_t>(i) * 16 + 12] > 0) out.capped = true;
+    if (!it[i].frontera && it[i].paths > 0 && st[static_cast<size_t>(i) * 16 + 10] != static_cast<double>(it[i].paths))
+      return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
+  }
   return FK_OK;
 }
 

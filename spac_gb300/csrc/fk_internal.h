@@ -49,9 +49,28 @@ struct PatchDev {
 
 // Per-item FP64 sums written by the path kernel: score, score^2, xi + xi^2
 // (the reference's aliased xi slot), score + xi, (score + xi)^2, xi score,
-// steps, B, domain exits, capped paths, xi^2.
+// steps, B, domain exits, capped paths, xi^2, paths completed.
 enum { kStatScore = 0, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScore, kStatSteps, kStatB, kStatDom,
-       kStatCap, kStatXi2, kNumStats = 12 };
+       kStatCap, kStatXi2, kStatPaths, kNumStats = 12 };
+
+// Path-kernel shared memory: each CTA keeps paths_slots() chunks in flight
+// (3 for FP32 stepping, 2 for FP64), so that its warps move on to the next
+// chunk while the last paths of the previous one finish.  A slot holds the
+// chunk's stencil accumulators followed by its stencil nodes (patch node
+// coordinates in the stepping precision, or arc angles in FP64), each part
+// padded to 16 bytes.
+__host__ __device__ inline int paths_slots(int precision) { return precision == 0 ? 2 : 3; }
+__host__ __device__ inline size_t paths_slot_acc_bytes(int precision, int stencil_kind, int acc_words) {
+  const size_t w = (precision == 0 || stencil_kind == 1) ? 8 : 4;
+  return (static_cast<size_t>(acc_words) * w + 15) & ~static_cast<size_t>(15);
+}
+__host__ __device__ inline size_t paths_slot_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes) {
+  size_t nodes = 0;
+  if (stencil_kind == 2) nodes = 2ull * smem_nodes * (precision == 0 ? 8 : 4);
+  if (stencil_kind == 1) nodes = static_cast<size_t>(smem_nodes) * 8;
+  nodes = (nodes + 15) & ~static_cast<size_t>(15);
+  return paths_slot_acc_bytes(precision, stencil_kind, acc_words) + nodes;
+}
 
 struct LaunchArgs {
   const BvpDev* bvp;
@@ -62,7 +81,7 @@ struct LaunchArgs {
   const double* arc_theta;
   const PatchDev* patches;
   const double* patch_nodes;
-  int* queue;              // chunk counter (zeroed before launch)
+  int* queue;              // [0] chunk counter, [1] error word (both zeroed before launch)
   double* stats;           // n_items * kNumStats
   double* acc;             // stencil accumulators
   uint32_t key0, key1, stream;

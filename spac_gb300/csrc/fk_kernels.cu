@@ -43,7 +43,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
         // slot 2 holds sum(xi + xi^2); the reference adds it twice (xi/xixi aliasing)
         o[0] = S[0] / N; o[1] = S[1] / N; o[2] = S[3] / N; o[3] = S[4] / N;
         o[4] = (S[2] + S[2]) / N; o[5] = (S[2] + S[2]) / N; o[6] = S[5] / N;
-        o[7] = it.h * S[6] / N; o[8] = 4.0 * S[6]; o[9] = Bv; o[10] = N; o[11] = S[8]; o[12] = S[9];
+        o[7] = it.h * S[6] / N; o[8] = 4.0 * S[6]; o[9] = Bv; o[10] = S[kStatPaths]; o[11] = S[8]; o[12] = S[9];
         o[13] = (S[2] - S[10]) / N; o[14] = S[10] / N; o[15] = S[6] / N;
       }
     }

@@ -118,7 +118,7 @@ extern "C" int fk_solve_points_noalloc(const fk_bvp_desc* d, unsigned long long 
   ChunkDev* d_chunks = reinterpret_cast<ChunkDev*>(base + kChunksOff);
   double* d_stats = reinterpret_cast<double*>(base + kStatsOff);
   // the work counter and the FP64 sums start at zero on every call
-  if (cudaMemsetAsync(d_queue, 0, sizeof(int), s) != cudaSuccess) return FK_ERR_CUDA;
+  if (cudaMemsetAsync(d_queue, 0, 2 * sizeof(int), s) != cudaSuccess) return FK_ERR_CUDA;
   if (cudaMemsetAsync(d_stats, 0, sizeof(double) * kNumStats * n, s) != cudaSuccess) return FK_ERR_CUDA;
   noalloc_prepare<<<(n + 127) / 128, 128, 0, s>>>(b, n, d_xy, d_paths, d_h, d_bvp, d_items, d_chunks);
   if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;

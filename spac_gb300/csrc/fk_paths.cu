@@ -1,21 +1,30 @@
 // GB300 (sm_103a) path kernel of the Feynman-Kac hot path.
 //
-// Persistent grid.  Each CTA takes chunks of one item's paths from a global
-// queue; every thread runs one path at a time and pulls the next path index
-// of the chunk as soon as its path exits (per-lane regeneration: a lane never
-// waits for the longest path of its warp).  An exiting lane only pushes its
-// exit (X_tau, Y, Z, xi, steps, flags) onto its warp's shared-memory queue and
-// starts the next path; once 32 exits are queued the whole warp processes
-// them, one exit per lane, so the exit work runs at full SIMD width:
+// Persistent grid.  Each CTA keeps a ring of chunk slots in shared memory (a
+// chunk is a range of one item's paths; its slot holds the chunk's stencil
+// accumulators and stencil nodes).  The warps of a CTA walk the CTA's
+// sequence of chunks in order.  Inside a chunk every lane runs one path at a
+// time and takes the next path index of the chunk as soon as its path exits
+// (per-lane regeneration).  Once a chunk's paths are all taken its warps go
+// on to the next slot while the chunk's last paths finish: there is no
+// CTA-wide barrier between chunks, so the tail of one chunk overlaps the
+// next.  The last warp to leave a chunk flushes the chunk's stencil moments
+// into the item's FP64 accumulators and refills the slot from the global
+// chunk queue.
+//
+// An exiting lane only pushes its exit (X_tau, Y, Z, xi, steps, flags) onto
+// its warp's shared-memory queue and starts the next path; once 32 exits are
+// queued the whole warp processes them, one exit per lane, so the exit work
+// runs at full SIMD width:
 //  - exit value u(X_tau), B and the statistics into per-thread registers
 //    (compensated FP32 sums for FP32 stepping, FP64 for FP64 stepping);
 //  - the stencil moments Y phi of subdomain exits into the chunk's
 //    shared-memory accumulators (FP64 for the arc stencil, whose inverse has
 //    condition ~1e10, with lanes over the arc nodes; FP32 chunk partials for
 //    the Gaussian k-nearest stencil, one exit and its window per lane).
-// At the end of a chunk the thread sums are block-reduced and the moments
-// flushed into FP64 per-item accumulators.  On the FP32 path no FP64
-// instruction runs inside the step loop.
+// A warp leaving a chunk reduces its thread sums (compensated FP32 shuffles
+// on the FP32 path) and adds them to the item's FP64 sums.  On the FP32 path
+// no FP64 arithmetic runs inside the step loop.
 // Replaces Simulacion_OMP + Reduce_Analytic + Interfaz::Update_G
 // (Solvers/FeynmanKacSolver.cpp:137-292, Mesh/Interfaz.cpp:219-264).
 #include <cfloat>
@@ -29,15 +38,14 @@ namespace fk {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kMaxWarps = 32;
 constexpr int kNumAcc = 8;   // floating-point sums per thread
 
 struct AccD {
   double s = 0.0;
   __device__ __forceinline__ void add(double v) { s += v; }
-  __device__ __forceinline__ double get() const { return s; }
 };
 // Compensated (Kahan) FP32 sum: FP64-grade thread sums without FP64 work.
+// The sum is s - c.
 struct AccK {
   float s = 0.f, c = 0.f;
   __device__ __forceinline__ void add(float v) {
@@ -46,8 +54,31 @@ struct AccK {
     c = (t - s) - y;
     s = t;
   }
-  __device__ __forceinline__ double get() const { return static_cast<double>(s) - static_cast<double>(c); }
 };
+
+// Warp total of a thread sum; lane 0 holds the result.
+__device__ __forceinline__ double warp_reduce(const AccD& a, int) {
+  double t = a.s;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+  return t;
+}
+// Compensated FP32 butterfly: the (sum, correction) pairs are combined with
+// Knuth's TwoSum, so the warp total keeps the accuracy of the compensated
+// thread sums; only lane 0 converts the pair to FP64.
+__device__ __forceinline__ double warp_reduce(const AccK& a, int lane) {
+  float s = a.s, c = -a.c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(kFull, s, o), c2 = __shfl_xor_sync(kFull, c, o);
+    const float t = s + s2;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (s2 - bp);
+    s = t;
+    c = c + c2 + e;
+  }
+  return lane == 0 ? static_cast<double>(s) + static_cast<double>(c) : 0.0;
+}
 
 template <typename R, int ST>
 struct SAccType {
@@ -71,6 +102,105 @@ struct PatchSh {
   R side_fixed[4], side_start[4], side_inv_step[4];
   R e2;
 };
+
+// A chunk slot.  `ready` is written last, after the slot's contents.
+template <typename R>
+struct SlotSh {
+  int ready;        // position in the CTA's chunk sequence that the slot holds
+  int chunk;        // chunk index; -1: the chunk queue was exhausted
+  int warps_left;   // warps that have not yet left the chunk
+  unsigned next;    // next chunk-local path index
+  PatchSh<R> sp;
+  ArcDev sarc;
+};
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+__device__ __forceinline__ void st_volatile(int* p, int v) { *reinterpret_cast<volatile int*>(p) = v; }
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits until a slot holds sequence position `seq` (lane 0 polls, with
+// back-off).  The wait is for another warp of this CTA to finish the paths it
+// is running, which the step cap bounds; `limit_ns` bounds it again.  Returns
+// false if the wait gave up.
+__device__ bool wait_slot(const int* ready, int seq, unsigned long long limit_ns, int lane) {
+  int ok = 1;
+  if (lane == 0 && ld_volatile(ready) != seq) {
+    const unsigned long long t0 = global_ns();
+    while (ld_volatile(ready) != seq) {
+      if (global_ns() - t0 > limit_ns) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  ok = __shfl_sync(kFull, ok, 0);
+  __threadfence_block();
+  return ok != 0;
+}
+
+// One warp claims the next chunk of the global queue for a slot, clears the
+// slot's accumulators, stages the chunk's stencil and publishes the slot as
+// sequence position `seq`.
+template <typename R, int ST>
+__device__ void fill_slot(const LaunchArgs& a, SlotSh<R>& sl, unsigned char* mem, size_t acc_bytes, int seq,
+                          int nwarps, int lane) {
+  int c = 0;
+  if (lane == 0) c = atomicAdd(a.queue, 1);
+  c = __shfl_sync(kFull, c, 0);
+  if (c < a.n_chunks) {
+    const ChunkDev ch = a.chunks[c];
+    const ItemDev& itg = a.items[ch.item];
+    uint4* z = reinterpret_cast<uint4*>(mem);
+    for (int i = lane; i < static_cast<int>(acc_bytes / 16); i += 32) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (ST == 2) {
+      R* snx = reinterpret_cast<R*>(mem + acc_bytes);
+      R* sny = snx + a.smem_nodes;
+      const PatchDev& P = a.patches[itg.stencil];
+      const double* nd = a.patch_nodes + P.node_off;
+      for (int i = lane; i < P.m; i += 32) {
+        snx[i] = R(nd[2 * i]);
+        sny[i] = R(nd[2 * i + 1]);
+      }
+      if (lane < 4) {
+        const int s = lane;
+        sl.sp.side_first[s] = P.side_first[s];
+        sl.sp.side_count[s] = P.side_count[s];
+        sl.sp.side_axis[s] = P.side_axis[s];
+        sl.sp.side_fixed[s] = R(P.side_fixed[s]);
+        sl.sp.side_start[s] = R(P.side_start[s]);
+        sl.sp.side_inv_step[s] = R(1.0 / P.side_step[s]);
+      }
+      if (lane == 0) {
+        sl.sp.m = P.m;
+        sl.sp.k = P.k;
+        sl.sp.closed = P.closed;
+        sl.sp.e2 = R(P.eps2);
+      }
+    }
+    if (ST == 1) {
+      double* sth = reinterpret_cast<double*>(mem + acc_bytes);
+      const ArcDev& A = a.arcs[itg.stencil];
+      for (int i = lane; i < A.n; i += 32) sth[i] = a.arc_theta[A.theta_off + i];
+      if (lane == 0) sl.sarc = A;
+    }
+    if (lane == 0) {
+      sl.chunk = c;
+      sl.next = 0u;
+      sl.warps_left = nwarps;
+    }
+  } else if (lane == 0) {
+    sl.chunk = -1;
+  }
+  __syncwarp();
+  __threadfence_block();
+  if (lane == 0) st_volatile(&sl.ready, seq);
+  __syncwarp();
+}
 
 // Window (first chain index) of the k nearest patch-boundary nodes to an exit
 // point on the patch boundary.  The k nearest nodes of a point of a convex
@@ -116,56 +246,57 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
   return L;
 }
 
+// FP64 stepping is bound by the FP64 pipe, not by latency: it trades
+// occupancy for registers (2 CTAs of 256 per SM instead of 3).
 template <typename R, int PROB, int ST>
-__global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
+__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) paths_kernel(const LaunchArgs a) {
   using SAcc = typename SAccType<R, ST>::type;
   using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
+  constexpr int kPrec = std::is_same<R, double>::value ? 0 : 1;
+  constexpr int S = kPrec == 0 ? 2 : 3;  // paths_slots(kPrec)
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SAcc* sacc = reinterpret_cast<SAcc*>(smem_raw);
-  // after the accumulators: patch nodes (x[], y[]) or arc angles
-  R* snx = reinterpret_cast<R*>(smem_raw + static_cast<size_t>(a.acc_words) * sizeof(SAcc));
-  R* sny = snx + a.smem_nodes;
-  double* sth = reinterpret_cast<double*>(smem_raw + static_cast<size_t>(a.acc_words) * sizeof(SAcc));
-  __shared__ int s_chunk;
-  __shared__ unsigned s_next;
-  __shared__ double s_red[kNumAcc + 3][kMaxWarps];
-  __shared__ PatchSh<R> sp;
-  __shared__ ArcDev sarc;
+  __shared__ SlotSh<R> slots[S];
   __shared__ ExitQueue<R> sq[kMaxBlockWarps];
+  const size_t acc_bytes = paths_slot_acc_bytes(kPrec, ST, a.acc_words);
+  const size_t slot_bytes = paths_slot_bytes(kPrec, ST, a.acc_words, a.smem_nodes);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const bool cv = a.cv != 0;         // any control term
   const bool cv_exact = a.cv == 1;   // F from the problem functor
   const bool cv_table = a.cv == 2;   // F from the learned gradient table
+  const unsigned long long limit_ns = 60000000000ull + 1000ull * static_cast<unsigned long long>(a.max_steps);
 
-  for (;;) {
-    if (threadIdx.x == 0) s_chunk = atomicAdd(a.queue, 1);
-    __syncthreads();
-    const int c = s_chunk;
-    if (c >= a.n_chunks) break;
+  if (threadIdx.x < S) slots[threadIdx.x].ready = -1;
+  __syncthreads();
+  for (int s = warp; s < S; s += nwarps) fill_slot<R, ST>(a, slots[s], smem_raw + s * slot_bytes, acc_bytes, s, nwarps, lane);
+
+  ExitQueue<R>& q = sq[warp];
+  // Slots known to hold no further chunk: a slot whose chunk queue came up
+  // empty is never refilled, so the walk ends once every slot is dead.
+  unsigned dead = 0u;
+  for (int g = 0; dead != (1u << S) - 1u; ++g) {
+    const int si = g % S;
+    if (dead & (1u << si)) continue;
+    SlotSh<R>& sl = slots[si];
+    if (!wait_slot(&sl.ready, g, limit_ns, lane)) {
+      if (lane == 0) atomicExch(a.queue + 1, 1);
+      break;
+    }
+    const int c = ld_volatile(&sl.chunk);
+    if (c < 0) {
+      dead |= 1u << si;
+      continue;
+    }
+    unsigned char* mem = smem_raw + si * slot_bytes;
+    SAcc* sacc = reinterpret_cast<SAcc*>(mem);
+    const R* snx = reinterpret_cast<const R*>(mem + acc_bytes);
+    const R* sny = snx + a.smem_nodes;
+    const double* sth = reinterpret_cast<const double*>(mem + acc_bytes);
+    const PatchSh<R>& sp = sl.sp;
+    const ArcDev& sarc = sl.sarc;
     const ChunkDev ch = a.chunks[c];
     const ItemDev& itg = a.items[ch.item];
-    for (int i = threadIdx.x; i < a.acc_words; i += blockDim.x) sacc[i] = SAcc(0);
-    if (ST == 2) {
-      const PatchDev& P = a.patches[itg.stencil];
-      const double* nd = a.patch_nodes + P.node_off;
-      for (int i = threadIdx.x; i < P.m; i += blockDim.x) { snx[i] = R(nd[2 * i]); sny[i] = R(nd[2 * i + 1]); }
-      if (threadIdx.x == 0) {
-        sp.m = P.m; sp.k = P.k; sp.closed = P.closed; sp.e2 = R(P.eps2);
-        for (int s = 0; s < 4; ++s) {
-          sp.side_first[s] = P.side_first[s]; sp.side_count[s] = P.side_count[s]; sp.side_axis[s] = P.side_axis[s];
-          sp.side_fixed[s] = R(P.side_fixed[s]); sp.side_start[s] = R(P.side_start[s]);
-          sp.side_inv_step[s] = R(1.0 / P.side_step[s]);
-        }
-      }
-    }
-    if (ST == 1) {
-      const ArcDev& A = a.arcs[itg.stencil];
-      for (int i = threadIdx.x; i < A.n; i += blockDim.x) sth[i] = a.arc_theta[A.theta_off + i];
-      if (threadIdx.x == 0) sarc = A;
-    }
-    if (threadIdx.x == 0) s_next = ch.p0 + blockDim.x;
-    __syncthreads();
+    const unsigned n_ch = ch.p1 - ch.p0;
 
     // the item's BVP (independent problems of one functor share a launch)
     const BvpDev& bvp = a.bvp[itg.bvp];
@@ -191,25 +322,28 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
     }
 
     Acc acc[kNumAcc];
-    unsigned n_steps = 0, n_dom = 0, n_cap = 0;
+    unsigned long long n_steps = 0;
+    unsigned n_dom = 0, n_cap = 0, n_done = 0;
     R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0;
     int k = 0;
     uint32_t w2 = 0, w3 = 0;
-    unsigned p = ch.p0 + threadIdx.x;
-    bool active = p < ch.p1;
-    ExitQueue<R>& q = sq[warp];
+    // every lane's first path of the chunk (chunk-local index)
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&sl.next, 32u);
+    unsigned pl = __shfl_sync(kFull, base, 0) + lane;
+    bool active = pl < n_ch;
     int qn = 0;  // queued exits of this warp (warp-uniform)
 
     // Processes the top `cnt` (<= 32) queued exits, one per lane: exit value
     // and statistics (Reduce_Analytic, FeynmanKacSolver.cpp:198-292) and the
     // stencil moments of subdomain exits.
     auto process = [&](int cnt) {
-      const int base = qn - cnt;
+      const int qb = qn - cnt;
       const bool mine = lane < cnt;
       R ex = R(0), ey = R(0), Yv = R(0);
       bool sub_exit = false;
       if (mine) {
-        const int e = base + lane;
+        const int e = qb + lane;
         ex = q.x[e]; ey = q.y[e]; Yv = q.Y[e];
         const R Zv = q.Z[e], xv = q.xi[e];
         const unsigned kf = q.kf[e];
@@ -229,18 +363,23 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
         n_steps += kf & 0x3fffffffu;
         n_dom += dw ? 1u : 0u;
         n_cap += cp ? 1u : 0u;
+        ++n_done;
       }
       if (ST == 2) {
         if (sub_exit) {
-          // Gaussian k-nearest moments t_W[j] += Y phi_j, one exit per lane
+          // Gaussian k-nearest moments t_W[j] += Y phi_j, one exit per lane;
+          // each lane starts at its own j so that lanes sharing a window add
+          // to different words
           const int L = knn_window<R>(sp, snx, sny, ex, ey);
           const int kk = sp.k, m = sp.m;
           const R e2 = sp.e2;
-          for (int j = 0; j < kk; ++j) {
+          int j = lane % kk;
+          for (int jj = 0; jj < kk; ++jj) {
             int idx = L + j;
             if (idx >= m) idx -= m;
             const R dx = ex - snx[idx], dy = ey - sny[idx];
             atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(Yv * fexp(-e2 * (dx * dx + dy * dy))));
+            if (++j == kk) j = 0;
           }
         }
       } else if (ST == 1) {
@@ -262,7 +401,7 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
           }
         }
       }
-      qn = base;
+      qn = qb;
     };
 
     while (__any_sync(kFull, active)) {
@@ -288,7 +427,8 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
         }
         uint32_t wa, wb;
         if ((k & 1) == 0) {
-          const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k >> 1), p, item, a.stream), a.key0, a.key1);
+          const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k >> 1), ch.p0 + pl, item, a.stream), a.key0,
+                                   a.key1);
           wa = r.x; wb = r.y; w2 = r.z; w3 = r.w;
         } else {
           wa = w2; wb = w3;
@@ -325,54 +465,70 @@ __global__ void __launch_bounds__(256, 3) paths_kernel(const LaunchArgs a) {
       }
       // ---- queue the exits; the exiting lanes start their next path at once
       const unsigned em = __ballot_sync(kFull, exits);
-      if (exits) {
-        const int e = qn + __popc(em & ((1u << lane) - 1u));
-        q.x[e] = ex; q.y[e] = ey; q.Y[e] = Y; q.Z[e] = Z; q.xi[e] = xi;
-        q.kf[e] = static_cast<unsigned>(k) | (dom_wins ? 1u << 30 : 0u) | (capped ? 1u << 31 : 0u);
-        p = atomicAdd(&s_next, 1u);
-        active = p < ch.p1;
-        x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0; st = st0;
-      }
-      qn += __popc(em);
-      __syncwarp();
-      if (qn >= 32) {
-        process(32);
+      if (em) {
+        const int rank = __popc(em & ((1u << lane) - 1u));
+        const int leader = __ffs(em) - 1;
+        unsigned nb = 0;
+        if (lane == leader) nb = atomicAdd(&sl.next, static_cast<unsigned>(__popc(em)));
+        nb = __shfl_sync(kFull, nb, leader);
+        if (exits) {
+          const int e = qn + rank;
+          q.x[e] = ex; q.y[e] = ey; q.Y[e] = Y; q.Z[e] = Z; q.xi[e] = xi;
+          q.kf[e] = static_cast<unsigned>(k) | (dom_wins ? 1u << 30 : 0u) | (capped ? 1u << 31 : 0u);
+          pl = nb + rank;
+          active = pl < n_ch;
+          x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0; st = st0;
+        }
+        qn += __popc(em);
         __syncwarp();
+        if (qn >= 32) {
+          process(32);
+          __syncwarp();
+        }
       }
     }
     if (qn > 0) process(qn);
-    __syncthreads();
-    // ---- chunk flush: block reduction of the thread sums, FP64 atomics per item
-    double v[kNumAcc + 3];
+
+    // ---- the warp leaves the chunk: its sums into the item's FP64 sums
+    double* sums = a.stats + static_cast<long long>(ch.item) * kNumStats;
+    const int slot_of[kNumAcc] = {kStatScore, kStatScore2, kStatXiAlias, kStatVR,
+                                  kStatVR2, kStatXiScore, kStatB, kStatXi2};
 #pragma unroll
-    for (int j = 0; j < kNumAcc; ++j) v[j] = acc[j].get();
-    v[kNumAcc] = static_cast<double>(n_steps);
-    v[kNumAcc + 1] = static_cast<double>(n_dom);
-    v[kNumAcc + 2] = static_cast<double>(n_cap);
-#pragma unroll
-    for (int j = 0; j < kNumAcc + 3; ++j) {
-      double t = v[j];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
-      if (lane == 0) s_red[j][warp] = t;
+    for (int j = 0; j < kNumAcc; ++j) {
+      const double t = warp_reduce(acc[j], lane);
+      if (lane == 0 && t != 0.0) atomicAdd(&sums[slot_of[j]], t);
     }
-    __syncthreads();
-    if (threadIdx.x < kNumAcc + 3) {
-      double t = 0.0;
-      for (int w = 0; w < nwarps; ++w) t += s_red[threadIdx.x][w];
-      // slot layout of kStat*: score, score^2, xi+xi^2, vr, vr^2, xi score, steps, B, dom, cap, xi^2
-      const int slot_of[kNumAcc + 3] = {kStatScore, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScore,
-                                        kStatB, kStatXi2, kStatSteps, kStatDom, kStatCap};
-      if (t != 0.0) atomicAdd(&a.stats[static_cast<long long>(ch.item) * kNumStats + slot_of[threadIdx.x]], t);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      n_steps += __shfl_xor_sync(kFull, n_steps, o);
+      n_dom += __shfl_xor_sync(kFull, n_dom, o);
+      n_cap += __shfl_xor_sync(kFull, n_cap, o);
+      n_done += __shfl_xor_sync(kFull, n_done, o);
     }
-    if (ST != 0) {
-      double* gacc = a.acc + itg.acc_off;
-      for (int i = threadIdx.x; i < a.acc_words; i += blockDim.x) {
-        const double t = static_cast<double>(sacc[i]);
-        if (t != 0.0) atomicAdd(&gacc[i], t);
+    if (lane == 0) {
+      if (n_steps) atomicAdd(&sums[kStatSteps], static_cast<double>(n_steps));
+      if (n_dom) atomicAdd(&sums[kStatDom], static_cast<double>(n_dom));
+      if (n_cap) atomicAdd(&sums[kStatCap], static_cast<double>(n_cap));
+      if (n_done) atomicAdd(&sums[kStatPaths], static_cast<double>(n_done));
+    }
+    __syncwarp();
+    __threadfence_block();
+    int left = 0;
+    if (lane == 0) left = atomicSub(&sl.warps_left, 1);
+    left = __shfl_sync(kFull, left, 0);
+    if (left == 1) {
+      // last warp out: flush the chunk's stencil moments, refill the slot
+      __threadfence_block();
+      if (ST != 0) {
+        double* gacc = a.acc + itg.acc_off;
+        for (int i = lane; i < a.acc_words; i += 32) {
+          const double t = static_cast<double>(sacc[i]);
+          if (t != 0.0) atomicAdd(&gacc[i], t);
+        }
       }
+      __syncwarp();
+      fill_slot<R, ST>(a, sl, mem, acc_bytes, g + S, nwarps, lane);
     }
-    __syncthreads();
   }
 }
 
@@ -400,14 +556,12 @@ const void* select_paths(int problem, int precision, int st) {
 }  // namespace
 
 size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes) {
-  const size_t acc = static_cast<size_t>(acc_words) * ((precision == 0 || stencil_kind == 1) ? 8 : 4);
-  if (stencil_kind == 2) return acc + 2ull * smem_nodes * (precision == 0 ? 8 : 4);
-  if (stencil_kind == 1) return acc + static_cast<size_t>(smem_nodes) * 8;
-  return acc;
+  return static_cast<size_t>(paths_slots(precision)) * paths_slot_bytes(precision, stencil_kind, acc_words, smem_nodes);
 }
 
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block, size_t smem,
                          cudaStream_t s) {
+  if (block < 32 || block > 256 || block % 32 != 0) return cudaErrorInvalidValue;
   const void* fn = select_paths(problem, precision, a.stencil_kind);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
