@@ -184,6 +184,25 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------- replicas ------
+# The assembly shards by item with no exchange on the data path: under
+# torchrun every rank assembles its own replica of the workload (weak
+# scaling), the ranks meet only at barriers, and the job's time is the
+# slowest rank's.
+def max_over_ranks(x, dist):
+    """Max of a float over the ranks (a CUDA tensor under NCCL, CPU under gloo)."""
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, paths_per_rank, ms_per_step):
+    """Whole-job paths/s: the paths all ranks processed over the slowest rank's time."""
+    return world * paths_per_rank / (ms_per_step / 1000.0)
+
+
 # --------------------------------------------------------------- GPU side ----
 def main():
     ap = argparse.ArgumentParser()
@@ -259,15 +278,14 @@ def main():
     clocks = sampler.stop()
     t_step = float(np.sum(times)) / args.steps  # ms
     if dist:
-        t = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
+        t_step = max_over_ranks(t_step, dist)
         dist.barrier()
-    value = world * total_paths / (t_step / 1000.0)
+    value = job_value(world, total_paths, t_step)
 
-    # end to end: host output buffers (D2H of val and B inside the timed region)
-    val_h = np.empty(info["nnz"])
-    B_h = np.empty(info["n_rows"])
+    # end to end: pinned host output buffers (the item table goes host->device
+    # and val, B and the kernels' check flags device->host inside the timed region)
+    val_h = _pinned(info["nnz"])
+    B_h = _pinned(info["n_rows"])
     e2e_t = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
@@ -277,11 +295,11 @@ def main():
         e2e_t.append(time.perf_counter() - t0)
     e2e_step = float(np.mean(e2e_t))
     if dist:
-        t = torch.tensor([e2e_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    item_bytes = info["n_items"] * 80 + (info["n_items"] * 12)
-    d2h = 8 * (info["nnz"] + info["n_rows"])
+        e2e_step = max_over_ranks(e2e_step, dist)
+    # per call: one 96-byte item record and one 12-byte chunk record per item
+    # (an item of <= 32768 paths is one chunk); back: CSR values, B, 4 check words
+    item_bytes = info["n_items"] * (96 + 12)
+    d2h = 8 * (info["nnz"] + info["n_rows"]) + 16
 
     # roofline of the dominant kernel (the path kernel): algorithmic flops / its event time
     k_ms = float(np.mean([k[0] for k in kern]))
@@ -333,17 +351,34 @@ def _u_aniso(xy):
     return _franke_np(xy[:, 0], xy[:, 1]) * (1 + xy[:, 0] * xy[:, 1])
 
 
-def _assemble_stats(ctx, mesh, bvp, paths, prec, h):
-    """One fk_assemble call into host buffers; returns (seconds, per-item stats)."""
+_PINNED = {}
+
+
+def _pinned(n):
+    """Page-locked host array of n doubles (kept for reuse), as a user keeps its
+    output buffers."""
+    if n not in _PINNED:
+        import torch
+        _PINNED[n] = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    return _PINNED[n]
+
+
+def _assemble_stats(ctx, mesh, bvp, paths, prec, h, kernels=None):
+    """One fk_assemble call into pinned host buffers (CSR values and B);
+    returns (seconds, per-item stats).  `kernels`, if a list, receives the
+    path and finalize kernel times (ms)."""
     from spac_gb300 import fk
     info = ctx.mesh_info(mesh)
     st = (fk.Stats * info["n_items"])()
-    val = np.empty(info["nnz"])
-    B = np.empty(info["n_rows"])
+    val = _pinned(info["nnz"])
+    B = _pinned(info["n_rows"])
     t0 = time.perf_counter()
     ctx.check(ctx.L.fk_assemble(ctx.h, mesh, bvp, int(paths), None, h, prec, val.ctypes.data_as(fk._dp),
                                 B.ctypes.data_as(fk._dp), None, None, st))
-    return time.perf_counter() - t0, fk.stats_array(st)
+    dt = time.perf_counter() - t0
+    if kernels is not None:
+        kernels.extend(ctx.last_timing()[:2])
+    return dt, fk.stats_array(st)
 
 
 def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
@@ -356,7 +391,7 @@ def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
 
 
 def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=1000, pilot_h=5e-4, train_steps=2000,
-                   table=512):
+                   table=512, lr=3e-2, batch=4096):
     """Time to `target` RMS node error on the assembly, plain FK vs the learned
     control variate (both FP32 stepping, same h).
 
@@ -388,8 +423,9 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=10
         return out
     budget = target ** 2 - bias2
     n_plain = int(np.ceil(1.05 * var_p.mean() / budget))
-    t_plain, st = _assemble_stats(ctx, mesh, b_plain, n_plain, prec, h)
-    out["plain"] = {"paths_per_item": n_plain, "seconds": t_plain, "rms": rms_of(st)}
+    kp = []
+    t_plain, st = _assemble_stats(ctx, mesh, b_plain, n_plain, prec, h, kp)
+    out["plain"] = {"paths_per_item": n_plain, "seconds": t_plain, "rms": rms_of(st), "kernels_ms": kp}
 
     # learned control variate: pilot from boundary data only
     t0 = time.perf_counter()
@@ -408,7 +444,7 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=10
     hist = np.zeros(train_steps, dtype=np.float32)
     t1 = time.perf_counter()
     ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp), None,
-                                 train_steps, 4096, 1e-2, 777, hist.ctypes.data_as(fk._fp)))
+                                 train_steps, batch, lr, 777, hist.ctypes.data_as(fk._fp)))
     t_train = time.perf_counter() - t1
     t2 = time.perf_counter()
     ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
@@ -418,10 +454,11 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=10
     _, stc = _assemble_stats(ctx, mesh, b_cv, n_cal, prec, h)
     var_c = np.maximum(stc["phiphi_VR"] - stc["phi_VR"] ** 2, 0)
     n_cv = max(32, int(np.ceil(1.05 * var_c.mean() / budget)))
-    t_run, stc = _assemble_stats(ctx, mesh, b_cv, n_cv, prec, h)
+    kc = []
+    t_run, stc = _assemble_stats(ctx, mesh, b_cv, n_cv, prec, h, kc)
     t_cv = t_pilot + t_train + t_table + t_run
     out["learned_cv"] = {"paths_per_item": n_cv, "seconds": t_cv, "rms": rms_of(stc), "pilot_s": t_pilot,
-                         "train_s": t_train, "table_s": t_table, "run_s": t_run,
+                         "train_s": t_train, "table_s": t_table, "run_s": t_run, "run_kernels_ms": kc,
                          "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
                          "train_loss_first_last": [float(hist[0]), float(hist[-1])]}
     out["variance_reduction"] = float(var_p.mean() / max(var_c.mean(), 1e-300))

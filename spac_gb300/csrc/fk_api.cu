@@ -1,6 +1,7 @@
 // C ABI of libspac_fk (include/spac_fk.h): context, registries, meshes and the
 // launch sequence path kernel -> finalize/scatter on the context stream.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -316,7 +317,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
   if (acc_total > 0) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
   FK_CUDA(ctx->w_queue.ensure(16));
-  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 2 * sizeof(int), s));
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));  // queue, error word, result flags
 
   fk::LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -372,6 +373,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   f.csr_val = d_csr_val;
   f.row = d_row;
   f.B = d_B;
+  f.flags = ctx->w_queue.as<int>() + 2;
   FK_CUDA(fk::launch_finalize(f, bvp.problem, s));
   FK_CUDA(cudaEventRecord(ctx->ev[2], s));
   FK_CUDA(cudaStreamSynchronize(s));
@@ -385,17 +387,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   out.item_G = f.item_G;
   out.item_B = f.item_B;
   out.item_stats = f.item_stats;
-  // every requested path completed?  capped paths?
-  int qerr[2] = {0, 0};
-  FK_CUDA(cudaMemcpy(qerr, ctx->w_queue.p, sizeof(qerr), cudaMemcpyDeviceToHost));
-  if (qerr[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
-  std::vector<double> st(static_cast<size_t>(n) * 16);
-  FK_CUDA(cudaMemcpy(st.data(), f.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < n; ++i) {
-    if (st[static_cast<size_t>(i) * 16 + 12] > 0) out.capped = true;
-    if (!it[i].frontera && it[i].paths > 0 && st[static_cast<size_t>(i) * 16 + 10] != static_cast<double>(it[i].paths))
-      return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
-  }
+  // the kernels' own checks: slot waits, completed paths, capped paths
+  int q[4] = {0, 0, 0, 0};
+  FK_CUDA(cudaMemcpy(q, ctx->w_queue.p, sizeof(q), cudaMemcpyDeviceToHost));
+  if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
+  if (q[3] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
+  out.capped = q[2] != 0;
   return FK_OK;
 }
 
@@ -712,31 +709,35 @@ static int finish_mesh(fk_ctx* ctx, std::unique_ptr<fk::Mesh>& M, int* id) {
     if (h.kind == 1) add_arc(S, st, nullptr); else add_patch(S, st, h.knn, h.eps);
   }
   if (h.kind == 1 && S.nmax > 64) return fail(ctx, FK_ERR_CAPACITY, "arcs with more than 64 nodes");
-  // item -> G offsets and CSR positions
-  M->g_off.resize(h.items.size());
+  // item -> G offsets and CSR positions (binary search in the sorted row;
+  // items in parallel on the host cores)
+  const int n_items = static_cast<int>(h.items.size());
+  M->g_off.resize(n_items);
+  M->rows.resize(n_items);
   M->g_total = 0;
-  std::vector<int> rows;
-  for (size_t i = 0; i < h.items.size(); ++i) {
-    const fk::MeshItem& q = h.items[i];
+  for (int i = 0; i < n_items; ++i) {
     M->g_off[i] = M->g_total;
-    const int sz = S.size_of(q.stencil);
-    const int* gids = (h.kind == 1) ? &S.arc_gids[S.arc_gid_off[q.stencil]] : nullptr;
-    std::vector<int> pg;
-    if (h.kind == 2) {
-      for (const fk::MeshNode& nd : h.stencils[q.stencil].nodes) pg.push_back(nd.gid);
-      gids = pg.data();
-    }
-    for (int j = 0; j < sz; ++j) {
-      int pos = -1;
-      for (int c = h.rowptr[q.row]; c < h.rowptr[q.row + 1]; ++c)
-        if (h.col[c] == gids[j]) { pos = c; break; }
-      if (pos < 0) return fail(ctx, FK_ERR_NOT_FOUND, "stencil node missing from the CSR row");
-      M->csr_idx.push_back(pos);
-    }
-    M->g_total += sz;
-    rows.push_back(q.row);
+    M->g_total += S.size_of(h.items[i].stencil);
+    M->rows[i] = h.items[i].row;
   }
-  M->rows = rows;
+  M->csr_idx.assign(static_cast<size_t>(M->g_total), -1);
+  std::atomic<int> missing{0};
+  fk::host_parallel_for(n_items, [&](int i) {
+    const fk::MeshItem& q = h.items[i];
+    const int sz = S.size_of(q.stencil);
+    const int* row_begin = h.col.data() + h.rowptr[q.row];
+    const int* row_end = h.col.data() + h.rowptr[q.row + 1];
+    for (int j = 0; j < sz; ++j) {
+      const int gid = (h.kind == 1) ? S.arc_gids[S.arc_gid_off[q.stencil] + j] : h.stencils[q.stencil].nodes[j].gid;
+      const int* p = std::lower_bound(row_begin, row_end, gid);
+      if (p == row_end || *p != gid) {
+        missing.store(1);
+        return;
+      }
+      M->csr_idx[M->g_off[i] + j] = static_cast<int>(p - h.col.data());
+    }
+  });
+  if (missing.load()) return fail(ctx, FK_ERR_NOT_FOUND, "stencil node missing from the CSR row");
   ctx->meshes.push_back(std::move(M));
   *id = static_cast<int>(ctx->meshes.size()) - 1;
   return FK_OK;

@@ -115,6 +115,7 @@ struct FinalizeArgs {
   double* csr_val;          // may be null
   const int* row;           // item -> row (for B scatter)
   double* B;                // may be null
+  int* flags;               // may be null: [0] |= an item had capped paths, [1] |= an item lost paths
 };
 
 // host launchers (fk_paths.cu)

@@ -14,6 +14,8 @@
 namespace fk {
 
 // ------------------------------------------------------------- finalize -----
+constexpr int kMaxFinalizeWindows = 1024;  // windows flagged in shared memory (more: no skipping)
+
 // fk_stats layout (16 doubles): phi, phiphi, phi_VR, phiphi_VR, xi, xixi,
 // xiphi, APL, RNGC, B, n_paths, n_domain_exits, n_capped, xi_mean,
 // xi_sq_mean, mean_steps.
@@ -49,6 +51,10 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
     }
     if (a.item_B) a.item_B[item] = Bv;
     if (a.B) atomicAdd(&a.B[a.row[item]], Bv);
+    if (a.flags && live) {
+      if (S[kStatCap] > 0.0) atomicOr(&a.flags[0], 1);
+      if (S[kStatPaths] != N) atomicOr(&a.flags[1], 1);  // every requested path must have completed
+    }
   }
   if (a.stencil_kind == 0 || it.stencil < 0) return;
   const double* acc = a.acc + it.acc_off;
@@ -69,6 +75,20 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
     const PatchDev P = a.patches[it.stencil];
     const double* Ainv = a.patch_ainv + P.ainv_off;
     const int m = P.m, k = P.k;
+    // windows that no exit of this item chose have zero moments: flag the
+    // visited ones so that the FP64 products below skip the others
+    __shared__ unsigned char visited[kMaxFinalizeWindows];
+    const bool flags = m <= kMaxFinalizeWindows;
+    if (flags && live) {
+      for (int W = threadIdx.x; W < P.nwin; W += blockDim.x) {
+        const double* tw = acc + static_cast<long long>(W) * k;
+        bool any = false;
+        for (int b = 0; b < k; ++b) any |= tw[b] != 0.0;
+        visited[W] = any ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    auto window = [&](int W) { return !flags || visited[W] != 0; };
     for (int gi = threadIdx.x; gi < m; gi += blockDim.x) {
       double g = 0.0;
       if (live) {
@@ -76,6 +96,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
           for (int t = 0; t < k; ++t) {
             int W = gi - t;
             if (W < 0) W += m;
+            if (!window(W)) continue;
             const double* Ai = Ainv + static_cast<long long>(W) * k * k;
             const double* tw = acc + static_cast<long long>(W) * k;
             for (int b = 0; b < k; ++b) g += Ai[t + b * k] * tw[b];
@@ -83,6 +104,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
         } else {
           const int wlo = max(0, gi - k + 1), whi = min(gi, m - k);
           for (int W = wlo; W <= whi; ++W) {
+            if (!window(W)) continue;
             const int t = gi - W;
             const double* Ai = Ainv + static_cast<long long>(W) * k * k;
             const double* tw = acc + static_cast<long long>(W) * k;

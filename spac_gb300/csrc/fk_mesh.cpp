@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <set>
+#include <vector>
 
 namespace fk {
 namespace {
@@ -265,24 +266,67 @@ bool build_square_patch_mesh(const double dom[4], int n_sub, int nodes_per_side,
   m.nodes.resize(n_nodes);
   for (const MeshStencil& S : m.stencils)
     for (const MeshNode& nd : S.nodes) m.nodes[nd.gid] = nd;
-  // nodes strictly inside each patch (other than its own boundary nodes)
-  std::vector<std::vector<int>> adj(n_nodes);
-  std::vector<double> diag(n_nodes, 0.0);
-  for (int s = 0; s < static_cast<int>(m.stencils.size()); ++s) {
+  // nodes strictly inside each patch (other than its own boundary nodes), in
+  // node order: the nodes are bucketed by subdomain cell, and a patch (its
+  // cell enlarged by less than half a cell) only overlaps the 3 x 3 cells
+  // around its own
+  const int n_st = static_cast<int>(m.stencils.size());
+  auto cell_of = [&](double v, double lo, double H) {
+    return std::max(0, std::min(n_sub - 1, static_cast<int>(std::floor((v - lo) / H))));
+  };
+  std::vector<std::vector<int>> bucket(static_cast<size_t>(n_sub) * n_sub);
+  for (const MeshNode& nd : m.nodes)
+    bucket[static_cast<size_t>(cell_of(nd.x, dom[0], Hx)) * n_sub + cell_of(nd.y, dom[1], Hy)].push_back(nd.gid);
+  host_parallel_for(n_st, [&](int s) {
     MeshStencil& S = m.stencils[s];
-    const double tx = tol, ty = tol;
-    for (const MeshNode& nd : m.nodes) {
-      if (nd.ifx * n_sub + nd.ify == s) continue;
-      if (nd.x > S.rect[0] + tx && nd.x < S.rect[2] - tx && nd.y > S.rect[1] + ty && nd.y < S.rect[3] - ty)
-        S.inner.push_back(nd);
-    }
-    add_adjacency(S, adj, diag);
-  }
-  build_csr(m, adj, diag);
-  // items grouped by row (node), patches in index order
+    const int a = s / n_sub, b = s % n_sub;
+    std::vector<int> in;
+    for (int ca = std::max(0, a - 1); ca <= std::min(n_sub - 1, a + 1); ++ca)
+      for (int cb = std::max(0, b - 1); cb <= std::min(n_sub - 1, b + 1); ++cb)
+        for (int g : bucket[static_cast<size_t>(ca) * n_sub + cb]) {
+          const MeshNode& nd = m.nodes[g];
+          if (nd.ifx * n_sub + nd.ify == s) continue;
+          if (nd.x > S.rect[0] + tol && nd.x < S.rect[2] - tol && nd.y > S.rect[1] + tol && nd.y < S.rect[3] - tol)
+            in.push_back(g);
+        }
+    std::sort(in.begin(), in.end());
+    for (int g : in) S.inner.push_back(m.nodes[g]);
+  });
+  // patches holding each node inside (patch order); the node's own ring is its
+  // patch (ifx, ify)
   std::vector<std::vector<int>> by_node(n_nodes);
-  for (int s = 0; s < static_cast<int>(m.stencils.size()); ++s)
+  for (int s = 0; s < n_st; ++s)
     for (const MeshNode& nd : m.stencils[s].inner) by_node[nd.gid].push_back(s);
+  // CSR pattern, as SistemaLineal::Anadir_Lista_Adyacencia + Inicializa_CSR
+  // (Mesh/SistemaLineal.cpp:8-66) build it: row r couples to itself, to the
+  // ring nodes of every patch holding r inside, and to the inner nodes of the
+  // patch whose ring holds r; the diagonal counts the patches holding r inside
+  std::vector<std::vector<int>> rows(n_nodes);
+  host_parallel_for(n_nodes, [&](int r) {
+    std::vector<int>& c = rows[r];
+    c.push_back(r);
+    for (int s : by_node[r])
+      for (const MeshNode& nd : m.stencils[s].nodes) c.push_back(nd.gid);
+    const MeshNode& me = m.nodes[r];
+    for (const MeshNode& nd : m.stencils[me.ifx * n_sub + me.ify].inner) c.push_back(nd.gid);
+    std::sort(c.begin(), c.end());
+    c.erase(std::unique(c.begin(), c.end()), c.end());
+  });
+  m.n_rows = n_nodes;
+  m.rowptr.assign(n_nodes + 1, 0);
+  for (int r = 0; r < n_nodes; ++r) m.rowptr[r + 1] = m.rowptr[r] + static_cast<int>(rows[r].size());
+  m.nnz = m.rowptr[n_nodes];
+  m.col.resize(m.nnz);
+  m.val0.resize(m.nnz);
+  host_parallel_for(n_nodes, [&](int r) {
+    int k = m.rowptr[r];
+    for (int c : rows[r]) {
+      m.col[k] = c;
+      m.val0[k] = c == r ? static_cast<double>(by_node[r].size()) : 1.0E-23;
+      ++k;
+    }
+    std::vector<int>().swap(rows[r]);
+  });
   for (int g = 0; g < n_nodes; ++g)
     for (int s : by_node[g]) m.items.push_back(MeshItem{m.nodes[g].x, m.nodes[g].y, g, s, false});
   return true;

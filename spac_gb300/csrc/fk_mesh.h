@@ -1,9 +1,34 @@
 // Host-side mesh construction for the G/B assembly (setup code, C++).
 #pragma once
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace fk {
+
+// f(0..n-1) on the host cores in contiguous blocks (setup of large meshes;
+// f must only write state owned by its index).
+template <class F>
+void host_parallel_for(int n, F f) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min(nt, 64u));
+  if (n < 2048) nt = 1;
+  if (nt == 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const int per = (n + static_cast<int>(nt) - 1) / static_cast<int>(nt);
+  for (unsigned t = 0; t < nt; ++t) {
+    const int lo = static_cast<int>(t) * per, hi = std::min(n, lo + per);
+    if (lo >= hi) break;
+    pool.emplace_back([lo, hi, &f] {
+      for (int i = lo; i < hi; ++i) f(i);
+    });
+  }
+  for (std::thread& th : pool) th.join();
+}
 
 struct MeshNode {
   double x, y, theta;

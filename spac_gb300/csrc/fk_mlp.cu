@@ -1,7 +1,7 @@
 // Learned control variate: MLP 2 -> 64 -> 64 -> 64 -> 1 (SiLU), one network
 // per region (a patch or the whole domain), trained by the library's own
 // kernels:
-//  mlp_pass_kernel  128 rows per CTA (4 warps): forward and backward through
+//  mlp_pass_kernel  32 rows per CTA (8 warps): forward and backward through
 //                   the two 64x64 layers on the tensor cores (mma.sync
 //                   m16n8k16 BF16, FP32 accumulate), activations staged in
 //                   shared memory.  Modes: training-gradient partials on a
@@ -10,6 +10,8 @@
 //  mlp_adam_kernel  sums the per-CTA gradient partials in a fixed order,
 //                   Adam update of the FP32 master weights, refresh of the
 //                   BF16 copies (row-major and transposed) used by the GEMMs.
+//  mlp_train_kernel all training steps in one cooperative launch (pass,
+//                   grid barrier, Adam on each CTA's slice, grid barrier).
 //  mlp_table        grad u_hat on a grid per region (the inference pass),
 //                   read by the path kernel with bilinear interpolation to
 //                   form the control term F = -sigma^T grad u_hat of every step.
@@ -31,20 +33,31 @@ Mlp::~Mlp() {
   for (void* p : {static_cast<void*>(d_master), d_bf16, static_cast<void*>(d_m), static_cast<void*>(d_v),
                   static_cast<void*>(d_norm), static_cast<void*>(d_partial), static_cast<void*>(d_loss),
                   static_cast<void*>(d_rect), static_cast<void*>(d_table), static_cast<void*>(d_samples),
-                  static_cast<void*>(d_hist)})
+                  static_cast<void*>(d_hist), static_cast<void*>(d_sync)})
     if (p) cudaFree(p);
 }
 
 namespace {
 
 constexpr int W = 64;
-constexpr int kRows = 64;       // rows per CTA pass (the step is latency-bound: short chains)
-constexpr int kThreads = 128;   // 4 warps
-constexpr int kWarpRows = kRows / 4;
+// The training step is latency-bound (a chain of small dependent GEMMs), so
+// the batch is spread thin: 32 rows per CTA (128 CTAs at batch 4096) and 8
+// warps per CTA, warp w owning the 16 rows 16 (w % 2).. and the 16 columns
+// 16 (w / 2).. of every 64-wide product; two warps share each SM
+// sub-partition to hide latencies.
+constexpr int kRows = 32;
+constexpr int kThreads = 256;
+constexpr int kRowGroups = kRows / 16;
+constexpr int kWarpRows = kRows / kRowGroups;
 constexpr int kMT = kWarpRows / 16;  // m16 tiles per warp
+constexpr int kNT = 2;               // n8 tiles per warp (16 columns)
+constexpr int kColsPerWarp = 8 * kNT;
+constexpr int kColGroups = W / kColsPerWarp;
+constexpr int kQuarters = kThreads / W;  // row groups of the per-column sums
 constexpr int LD = 72;          // bf16 leading dimension of [rows][64] tiles (144 B rows)
 constexpr int LDT = kRows + 8;  // bf16 leading dimension of [64][rows] transposed tiles (16 B multiple)
-static_assert(kMT >= 1 && kWarpRows % 16 == 0, "rows per warp");
+static_assert(kMT == 1 && kWarpRows % 16 == 0, "rows per warp");
+static_assert(kThreads / 32 == kRowGroups * (W / kColsPerWarp), "warp tiling");
 constexpr int OFF_W1 = 0, OFF_B1 = 128, OFF_W2 = 192, OFF_B2 = OFF_W2 + W * W, OFF_W3 = OFF_B2 + W,
               OFF_B3 = OFF_W3 + W * W, OFF_W4 = OFF_B3 + W, OFF_B4 = OFF_W4 + W, NPARAM = OFF_B4 + 1;
 constexpr int BF_PER_REGION = 4 * W * W;  // W2, W2^T, W3, W3^T
@@ -93,38 +106,49 @@ struct Smem {
   __nv_bfloat16 dp[kRows * LD], dpt[W * LDT];
   float w1[2 * W], b1[W], b2[W], b3[W], w4[W], b4;
   float z[kRows][2], tgt[kRows], dO[kRows], o[kRows];
+  float o_part[kColGroups][kRows];   // output-unit partial sums of the column groups
+  float csum[7][kQuarters][W];       // per-column gradient sums of the row quarters
   int valid[kRows];
 };
 
-__global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// One pass over a CTA's rows (see the modes above).  Shared by the one-step
+// kernel and the persistent training kernel; the weights are read through
+// L2 (ld.global.cg), since the persistent kernel rewrites them between passes.
+__device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x, unsigned char* smem_raw) {
   Smem& S = *reinterpret_cast<Smem*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, t4 = lane & 3;
-  const int region = blockIdx.y, cta = blockIdx.x;
   const float* P = a.params + static_cast<long long>(region) * NPARAM;
   const __nv_bfloat16* WB = a.wbf + static_cast<long long>(region) * BF_PER_REGION;
   // weights into shared memory, 8 bf16 (16 bytes) per load
   for (int e8 = tid; e8 < W * W / 8; e8 += kThreads) {
     const int r = (e8 * 8) / W, c = (e8 * 8) % W;
     const uint4* src = reinterpret_cast<const uint4*>(WB) + e8;
-    *reinterpret_cast<uint4*>(&S.w2[r * LD + c]) = __ldg(src);
-    *reinterpret_cast<uint4*>(&S.w2t[r * LD + c]) = __ldg(src + W * W / 8);
-    *reinterpret_cast<uint4*>(&S.w3[r * LD + c]) = __ldg(src + 2 * W * W / 8);
-    *reinterpret_cast<uint4*>(&S.w3t[r * LD + c]) = __ldg(src + 3 * W * W / 8);
+    *reinterpret_cast<uint4*>(&S.w2[r * LD + c]) = __ldcg(src);
+    *reinterpret_cast<uint4*>(&S.w2t[r * LD + c]) = __ldcg(src + W * W / 8);
+    *reinterpret_cast<uint4*>(&S.w3[r * LD + c]) = __ldcg(src + 2 * W * W / 8);
+    *reinterpret_cast<uint4*>(&S.w3t[r * LD + c]) = __ldcg(src + 3 * W * W / 8);
   }
-  for (int e = tid; e < 2 * W; e += kThreads) S.w1[e] = P[OFF_W1 + e];
+  for (int e = tid; e < 2 * W; e += kThreads) S.w1[e] = __ldcg(P + OFF_W1 + e);
   for (int e = tid; e < W; e += kThreads) {
-    S.b1[e] = P[OFF_B1 + e]; S.b2[e] = P[OFF_B2 + e]; S.b3[e] = P[OFF_B3 + e]; S.w4[e] = P[OFF_W4 + e];
+    S.b1[e] = __ldcg(P + OFF_B1 + e);
+    S.b2[e] = __ldcg(P + OFF_B2 + e);
+    S.b3[e] = __ldcg(P + OFF_B3 + e);
+    S.w4[e] = __ldcg(P + OFF_W4 + e);
   }
-  if (tid == 0) S.b4 = P[OFF_B4];
+  if (tid == 0) S.b4 = __ldcg(P + OFF_B4);
   const float4 nm = a.norm[region];
   const bool train = a.mode != MODE_GRADX;
 
-  // persistent gradient accumulators: this warp owns rows 16*warp.. of dW2 / dW3
-  float cW2[1][8][4], cW3[1][8][4];
+  // warp tile: rows m0.., columns n0.. of every 64x64 product
+  const int m0 = (warp % kRowGroups) * kWarpRows, n0 = (warp / kRowGroups) * kColsPerWarp;
+  // per-column sums: thread <-> (column cj, row quarter cq)
+  const int cj = tid % W, cq = tid / W;
+  constexpr int kQRows = kRows / kQuarters;
+  // persistent gradient accumulators: this warp's tile of dW2 / dW3
+  float cW2[1][kNT][4], cW3[1][kNT][4];
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
+  for (int j = 0; j < kNT; ++j)
 #pragma unroll
     for (int q = 0; q < 4; ++q) cW2[0][j][q] = cW3[0][j][q] = 0.f;
   float gW4 = 0.f, gB3 = 0.f, gB2 = 0.f, gB1 = 0.f, gW10 = 0.f, gW11 = 0.f, gB4 = 0.f, lsum = 0.f;
@@ -132,7 +156,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
   int n_tiles, row0;
   if (a.mode == MODE_GRADX) {
     n_tiles = 1;
-    row0 = (blockIdx.x + blockIdx.y * gridDim.x) * kRows;
+    row0 = (cta + region * grid_x) * kRows;
   } else {
     n_tiles = a.rows_per_cta / kRows;
     row0 = cta * a.rows_per_cta;
@@ -185,30 +209,30 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
       if (train) S.h1t[j * LDT + r] = __float2bfloat16_rn(hv);
     }
     __syncthreads();
-    // ---- layers 2 and 3 on the tensor cores, warp w owns rows 32w..32w+31
+    // ---- layers 2 and 3 on the tensor cores, one (16-row, 32-column) tile per warp
     for (int layer = 0; layer < 2; ++layer) {
       const __nv_bfloat16* Ain = layer == 0 ? S.h1 : S.h2;
       const __nv_bfloat16* Bw = layer == 0 ? S.w2 : S.w3;
       const float* bias = layer == 0 ? S.b2 : S.b3;
       __nv_bfloat16* Hout = layer == 0 ? S.h2 : S.h3;
       __nv_bfloat16* Sout = layer == 0 ? S.s2 : S.s3;
-      float c[kMT][8][4];
+      float c[kMT][kNT][4];
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<kMT, 8, W>(c,Ain, LD, warp * kWarpRows,Bw, LD, 0, lane);
+      warp_gemm_tn<kMT, kNT, W>(c, Ain, LD, m0, Bw, LD, n0, lane);
       float orow[kMT][2] = {};
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int r = warp * kWarpRows + mt * 16 + g + ((q >> 1) << 3);
-            const int col = nt * 8 + 2 * t4 + (q & 1);
+            const int r = m0 + mt * 16 + g + ((q >> 1) << 3);
+            const int col = n0 + nt * 8 + 2 * t4 + (q & 1);
             float ds;
             const float hv = silu_f(c[mt][nt][q] + bias[col], ds);
             Hout[r * LD + col] = __float2bfloat16_rn(hv);
@@ -217,7 +241,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
             if (layer == 1) orow[mt][q >> 1] += S.w4[col] * hv;
           }
       if (layer == 1) {
-        // output unit: reduce the row partial sums over the quad
+        // output unit: this warp's column half of each row, reduced over the quad
 #pragma unroll
         for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
@@ -225,7 +249,7 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
             float v = orow[mt][hh];
             v += __shfl_xor_sync(0xffffffffu, v, 1);
             v += __shfl_xor_sync(0xffffffffu, v, 2);
-            if (t4 == 0) S.o[warp * kWarpRows + mt * 16 + g + hh * 8] = v + S.b4;
+            if (t4 == 0) S.o_part[n0 / kColsPerWarp][m0 + mt * 16 + g + hh * 8] = v;
           }
       }
       __syncthreads();
@@ -233,7 +257,10 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
     // ---- output gradient and dp3 = dO * w4 * silu'(p3)
     if (tid < kRows) {
       const int r = tid;
-      const float o = S.o[r];
+      float o = S.b4;
+#pragma unroll
+      for (int cg = 0; cg < kColGroups; ++cg) o += S.o_part[cg][r];
+      S.o[r] = o;
       float d;
       if (a.mode == MODE_GRADX) {
         d = 1.f;
@@ -254,35 +281,31 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
     __syncthreads();
     // layer-3 backward: dW3 += dp3^T h2, db3, dW4, db4; dh2 = dp3 W3
     if (train) {
-      warp_gemm_tn<1, 8, kRows>(cW3, S.dpt, LDT, warp * 16, S.h2t, LDT, 0, lane);
-      if (tid < W) {
-        const int j = tid;
-        for (int r = 0; r < kRows; ++r) {
-          gW4 += S.dO[r] * __bfloat162float(S.h3[r * LD + j]);
-          gB3 += __bfloat162float(S.dp[r * LD + j]);
-        }
-        if (j == 0)
-          for (int r = 0; r < kRows; ++r) gB4 += S.dO[r];
+      warp_gemm_tn<1, kNT, kRows>(cW3, S.dpt, LDT, m0, S.h2t, LDT, n0, lane);
+      for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) {
+        gW4 += S.dO[r] * __bfloat162float(S.h3[r * LD + cj]);
+        gB3 += __bfloat162float(S.dp[r * LD + cj]);
+        if (cj == 0) gB4 += S.dO[r];
       }
     }
     {
-      float c[kMT][8][4];
+      float c[kMT][kNT][4];
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<kMT, 8, W>(c,S.dp, LD, warp * kWarpRows,S.w3t, LD, 0, lane);
+      warp_gemm_tn<kMT, kNT, W>(c, S.dp, LD, m0, S.w3t, LD, n0, lane);
       __syncthreads();  // everyone is done reading dp / dpt of layer 3
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int r = warp * kWarpRows + mt * 16 + g + ((q >> 1) << 3);
-            const int col = nt * 8 + 2 * t4 + (q & 1);
+            const int r = m0 + mt * 16 + g + ((q >> 1) << 3);
+            const int col = n0 + nt * 8 + 2 * t4 + (q & 1);
             const __nv_bfloat16 vb = __float2bfloat16_rn(c[mt][nt][q] * __bfloat162float(S.s2[r * LD + col]));
             S.dp[r * LD + col] = vb;
             if (train) S.dpt[col * LDT + r] = vb;
@@ -291,19 +314,18 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
     __syncthreads();
     // layer-2 backward: dW2 += dp2^T h1, db2; dh1 = dp2 W2
     if (train) {
-      warp_gemm_tn<1, 8, kRows>(cW2, S.dpt, LDT, warp * 16, S.h1t, LDT, 0, lane);
-      if (tid < W)
-        for (int r = 0; r < kRows; ++r) gB2 += __bfloat162float(S.dp[r * LD + tid]);
+      warp_gemm_tn<1, kNT, kRows>(cW2, S.dpt, LDT, m0, S.h1t, LDT, n0, lane);
+      for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) gB2 += __bfloat162float(S.dp[r * LD + cj]);
     }
     {
-      float c[kMT][8][4];
+      float c[kMT][kNT][4];
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<kMT, 8, W>(c,S.dp, LD, warp * kWarpRows,S.w2t, LD, 0, lane);
+      warp_gemm_tn<kMT, kNT, W>(c, S.dp, LD, m0, S.w2t, LD, n0, lane);
       __syncthreads();
       // dp1 = dh1 * silu'(p1), kept in FP32 in the (now free) h3 / s3 area as pairs
       static_assert(sizeof(float) * kRows * W <= 2 * sizeof(__nv_bfloat16) * kRows * LD, "dp1 overlay");
@@ -311,11 +333,11 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int r = warp * kWarpRows + mt * 16 + g + ((q >> 1) << 3);
-            const int col = nt * 8 + 2 * t4 + (q & 1);
+            const int r = m0 + mt * 16 + g + ((q >> 1) << 3);
+            const int col = n0 + nt * 8 + 2 * t4 + (q & 1);
             dp1[r * W + col] = c[mt][nt][q] * __bfloat162float(S.s1[r * LD + col]);
           }
     }
@@ -334,10 +356,9 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
           a.out[3 * pi + 1] = gx * nm.z;
           a.out[3 * pi + 2] = gy * nm.w;
         }
-      } else if (a.mode != MODE_GRADX && tid < W) {
-        const int j = tid;
-        for (int r = 0; r < kRows; ++r) {
-          const float d = dp1[r * W + j];
+      } else if (a.mode != MODE_GRADX) {
+        for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) {
+          const float d = dp1[r * W + cj];
           gB1 += d;
           gW10 += d * S.z[r][0];
           gW11 += d * S.z[r][1];
@@ -350,23 +371,43 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
   // ---- write this CTA's gradient partial
   float* out = a.partial + (static_cast<long long>(region) * a.ctas_per_region + cta) * NPARAM;
 #pragma unroll
-  for (int nt = 0; nt < 8; ++nt)
+  for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int r = warp * 16 + g + ((q >> 1) << 3);
-      const int col = nt * 8 + 2 * t4 + (q & 1);
+      const int r = m0 + g + ((q >> 1) << 3);
+      const int col = n0 + nt * 8 + 2 * t4 + (q & 1);
       out[OFF_W2 + r * W + col] = cW2[0][nt][q];
       out[OFF_W3 + r * W + col] = cW3[0][nt][q];
     }
+  // per-column sums: the row quarters combined in a fixed order
+  S.csum[0][cq][cj] = gW4;
+  S.csum[1][cq][cj] = gB3;
+  S.csum[2][cq][cj] = gB2;
+  S.csum[3][cq][cj] = gB1;
+  S.csum[4][cq][cj] = gW10;
+  S.csum[5][cq][cj] = gW11;
+  S.csum[6][cq][cj] = gB4;
+  __syncthreads();
   if (tid < W) {
     const int j = tid;
-    out[OFF_W4 + j] = gW4;
-    out[OFF_B3 + j] = gB3;
-    out[OFF_B2 + j] = gB2;
-    out[OFF_B1 + j] = gB1;
-    out[OFF_W1 + 2 * j] = gW10;
-    out[OFF_W1 + 2 * j + 1] = gW11;
-    if (j == 0) out[OFF_B4] = gB4;
+    float v[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      v[k] = S.csum[k][0][j];
+#pragma unroll
+      for (int qd = 1; qd < kQuarters; ++qd) v[k] += S.csum[k][qd][j];
+    }
+    out[OFF_W4 + j] = v[0];
+    out[OFF_B3 + j] = v[1];
+    out[OFF_B2 + j] = v[2];
+    out[OFF_B1 + j] = v[3];
+    out[OFF_W1 + 2 * j] = v[4];
+    out[OFF_W1 + 2 * j + 1] = v[5];
+    if (j == 0) {
+      float b4 = S.csum[6][0][0];
+      for (int qd = 1; qd < kQuarters; ++qd) b4 += S.csum[6][qd][0];
+      out[OFF_B4] = b4;
+    }
   }
   // loss partial (sum of squared errors of this CTA)
   __shared__ float red[kThreads];
@@ -377,6 +418,35 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
     __syncthreads();
   }
   if (tid == 0) a.loss[region * a.ctas_per_region + cta] = red[0];
+}
+
+__global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  mlp_pass_body(a, blockIdx.y, blockIdx.x, gridDim.x, smem_raw);
+}
+
+// Adam update of parameter e (= region r, index p) with gradient gsum; keeps
+// the BF16 copies (W and W^T of the two 64x64 layers) in step.
+__device__ __forceinline__ void adam_apply(long long e, int r, int p, float gsum, float* params, __nv_bfloat16* wbf,
+                                           float* m, float* v, float lr, float b1, float b2, float eps, float bc1,
+                                           float bc2) {
+  const float mm = b1 * m[e] + (1.f - b1) * gsum;
+  const float vv = b2 * v[e] + (1.f - b2) * gsum * gsum;
+  m[e] = mm;
+  v[e] = vv;
+  const float th = params[e] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+  params[e] = th;
+  __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
+  const __nv_bfloat16 tb = __float2bfloat16_rn(th);
+  if (p >= OFF_W2 && p < OFF_W2 + W * W) {
+    const int q = p - OFF_W2, o = q / W, i = q % W;
+    B[q] = tb;
+    B[W * W + i * W + o] = tb;
+  } else if (p >= OFF_W3 && p < OFF_W3 + W * W) {
+    const int q = p - OFF_W3, o = q / W, i = q % W;
+    B[2 * W * W + q] = tb;
+    B[3 * W * W + i * W + o] = tb;
+  }
 }
 
 // Sum of partials (fixed order) and Adam update; refreshes the BF16 copies.
@@ -414,28 +484,126 @@ __global__ void mlp_adam_kernel(float* params, __nv_bfloat16* wbf, float* m, flo
     const float gsum = part;
     if (grad_out) grad_out[e] = gsum;
     if (!apply) continue;
-    const float mm = b1 * m[e] + (1.f - b1) * gsum;
-    const float vv = b2 * v[e] + (1.f - b2) * gsum * gsum;
-    m[e] = mm;
-    v[e] = vv;
-    const float th = params[e] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
-    params[e] = th;
-    __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
-    const __nv_bfloat16 tb = __float2bfloat16_rn(th);
-    if (p >= OFF_W2 && p < OFF_W2 + W * W) {
-      const int q = p - OFF_W2, o = q / W, i = q % W;
-      B[q] = tb;
-      B[W * W + i * W + o] = tb;
-    } else if (p >= OFF_W3 && p < OFF_W3 + W * W) {
-      const int q = p - OFF_W3, o = q / W, i = q % W;
-      B[2 * W * W + q] = tb;
-      B[3 * W * W + i * W + o] = tb;
-    }
+    adam_apply(e, r, p, gsum, params, wbf, m, v, lr, b1, b2, eps, bc1, bc2);
   }
   if (hist && blockIdx.x == 0 && threadIdx.x == 0) {
     float s = 0.f;
     for (int i = 0; i < n_regions * ctas; ++i) s += loss[i];
     *hist = s * loss_scale;
+  }
+}
+
+// ---------------------------------------------------- persistent training --
+// All training steps in one cooperative launch: every CTA runs its pass,
+// the grid meets at a barrier, each CTA applies Adam to its slice of the
+// parameters (the partials summed in a fixed CTA order, as in
+// mlp_adam_kernel), and the grid meets again before the next pass reads the
+// new weights.  The barrier is a monotonic arrival counter; its waits give
+// up after kBarrierNs, set the error word and end the kernel.
+struct TrainArgs {
+  PassArgs a;
+  float* params;
+  __nv_bfloat16* wbf;
+  float* m;
+  float* v;
+  unsigned* bar;     // arrival counter, zeroed before the launch
+  int* err;          // error word, zeroed before the launch
+  float* hist;       // loss per step
+  float loss_scale;
+  int steps;
+  long long t0;      // Adam steps taken before this launch
+  double lr;
+};
+constexpr unsigned long long kBarrierNs = 5000000000ull;
+
+__device__ __forceinline__ unsigned long long mlp_global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ bool grid_barrier(unsigned* bar, unsigned target, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    atomicAdd(bar, 1u);
+    const unsigned long long t0 = mlp_global_ns();
+    while (*reinterpret_cast<volatile unsigned*>(bar) < target) {
+      if (*reinterpret_cast<volatile int*>(err) != 0) { ok = 0; break; }
+      if (mlp_global_ns() - t0 > kBarrierNs) {
+        atomicExch(err, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs t) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float s_coef[3];  // lr_t, bc1, bc2 of the step
+  const int nb = gridDim.x * gridDim.y;
+  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+  const int ctas = t.a.ctas_per_region;
+  const long long total = static_cast<long long>(t.a.n_regions) * NPARAM;
+  const long long per = (total + nb - 1) / nb;
+  const long long e0 = bid * per, e1 = min(total, e0 + per);
+  PassArgs a = t.a;
+  unsigned target = 0;
+  for (int s = 0; s < t.steps; ++s) {
+    a.step = static_cast<uint32_t>(t.t0 + s);
+    mlp_pass_body(a, blockIdx.y, blockIdx.x, gridDim.x, smem_raw);
+    target += nb;
+    if (!grid_barrier(t.bar, target, t.err)) return;
+    if (threadIdx.x == 0) {
+      const double tt = static_cast<double>(t.t0 + s + 1);
+      // cosine decay from lr to lr/100 over the launch
+      s_coef[0] = static_cast<float>(t.lr * (0.01 + 0.99 * 0.5 * (1.0 + cos(3.141592653589793 * s / t.steps))));
+      s_coef[1] = static_cast<float>(1.0 - pow(0.9, tt));
+      s_coef[2] = static_cast<float>(1.0 - pow(0.999, tt));
+    }
+    __syncthreads();
+    const float lr_t = s_coef[0], bc1 = s_coef[1], bc2 = s_coef[2];
+    // 8 lanes per parameter, each summing every 8th CTA partial (all loads
+    // independent), then a fixed shuffle tree: the same order as mlp_adam_kernel
+    const int sub = threadIdx.x & 7;
+    for (long long base = e0; base < e1; base += kThreads / 8) {
+      const long long e = base + (threadIdx.x >> 3);
+      const bool live = e < e1;
+      float part = 0.f;
+      int r = 0, p = 0;
+      if (live) {
+        r = static_cast<int>(e / NPARAM);
+        p = static_cast<int>(e % NPARAM);
+        const float* src = a.partial + static_cast<long long>(r) * ctas * NPARAM + p;
+        float a0 = 0.f, a1 = 0.f;
+        int c = sub;
+        for (; c + 8 < ctas; c += 16) {
+          a0 += __ldcg(src + static_cast<long long>(c) * NPARAM);
+          a1 += __ldcg(src + static_cast<long long>(c + 8) * NPARAM);
+        }
+        if (c < ctas) a0 += __ldcg(src + static_cast<long long>(c) * NPARAM);
+        part = a0 + a1;
+      }
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      part += __shfl_xor_sync(0xffffffffu, part, 4);
+      if (live && sub == 0) adam_apply(e, r, p, part, t.params, t.wbf, t.m, t.v, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
+    }
+    if (bid == 0 && threadIdx.x == 0) {
+      float sl = 0.f;
+      for (int i = 0; i < t.a.n_regions * ctas; ++i) sl += __ldcg(a.loss + i);
+      t.hist[s] = sl * t.loss_scale;
+    }
+    target += nb;
+    if (!grid_barrier(t.bar, target, t.err)) return;
   }
 }
 
@@ -589,16 +757,38 @@ static int upload_samples(Mlp& M, int n, const double* xy, const double* target,
 
 int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* region, int steps, int batch,
               double lr, unsigned long long seed, float* loss_hist, cudaStream_t s, std::string& err) {
-  if (steps < 0 || batch < kRows || batch % kRows) { err = "batch must be a positive multiple of 64"; return FK_ERR_ARG; }
+  if (steps < 0 || batch < kRows || batch % kRows) { err = "batch must be a positive multiple of " + std::to_string(kRows); return FK_ERR_ARG; }
   std::vector<int> off;
   int rc = upload_samples(M, n, xy, target, region, off, err);
   if (rc) return rc;
-  // one 128-row tile per CTA (the step is latency-bound: more CTAs, shorter
-  // step); larger tiles per CTA only when the grid would exceed ~4 waves
+  // Persistent training (all steps in one cooperative launch) when the grid
+  // fits on the device at once, with as many CTAs (one 64-row tile each) as
+  // fit; otherwise one graph-captured pass + Adam launch pair per step.
+  int dev = 0, coop = 0, sms = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(sizeof(Smem))) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mlp_train_kernel, kThreads, sizeof(Smem)) != cudaSuccess)
+    occ = 0;
+  const long long capacity = static_cast<long long>(occ) * sms;
   int rows_per_cta = kRows;
-  while (rows_per_cta < 1024 && batch % (2 * rows_per_cta) == 0 &&
-         static_cast<long long>(batch / rows_per_cta) * M.n_regions > 4 * 152)
-    rows_per_cta *= 2;
+  bool persistent = false;
+  if (coop && steps > 0 && capacity > 0) {
+    while (rows_per_cta < batch && batch % (2 * rows_per_cta) == 0 &&
+           static_cast<long long>(batch / rows_per_cta) * M.n_regions > capacity)
+      rows_per_cta *= 2;
+    persistent = static_cast<long long>(batch / rows_per_cta) * M.n_regions <= capacity;
+  }
+  if (!persistent) {
+    // one 64-row tile per CTA (the step is latency-bound: more CTAs, shorter
+    // step); larger tiles per CTA only when the grid would exceed ~4 waves
+    rows_per_cta = kRows;
+    while (rows_per_cta < 1024 && batch % (2 * rows_per_cta) == 0 &&
+           static_cast<long long>(batch / rows_per_cta) * M.n_regions > 4 * 152)
+      rows_per_cta *= 2;
+  }
   const int ctas = batch / rows_per_cta;
   const size_t np = static_cast<size_t>(M.n_regions) * NPARAM;
   if (M.d_partial) cudaFree(M.d_partial);
@@ -629,6 +819,41 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
   a.inv_batch = 1.f / batch;
   a.partial = M.d_partial;
   a.loss = M.d_loss;
+  if (persistent) {
+    if (!M.d_sync && cudaMalloc(&M.d_sync, 2 * sizeof(unsigned)) != cudaSuccess) {
+      err = "mlp: training buffers";
+      return FK_ERR_CUDA;
+    }
+    TrainArgs t;
+    std::memset(&t, 0, sizeof(t));
+    t.a = a;
+    t.params = M.d_master;
+    t.wbf = static_cast<__nv_bfloat16*>(M.d_bf16);
+    t.m = M.d_m;
+    t.v = M.d_v;
+    t.bar = M.d_sync;
+    t.err = reinterpret_cast<int*>(M.d_sync + 1);
+    t.hist = M.d_hist;
+    t.loss_scale = 1.f / (static_cast<float>(batch) * M.n_regions);
+    t.steps = steps;
+    t.t0 = M.adam_t;
+    t.lr = lr;
+    e = cudaMemsetAsync(M.d_sync, 0, 2 * sizeof(unsigned), s);
+    void* args[] = {&t};
+    if (e == cudaSuccess)
+      e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel), dim3(ctas, M.n_regions),
+                                      dim3(kThreads), args, sizeof(Smem), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+    unsigned sync[2] = {0u, 0u};
+    if (cudaMemcpy(sync, M.d_sync, sizeof(sync), cudaMemcpyDeviceToHost) != cudaSuccess || sync[1] != 0u) {
+      err = "mlp: a training barrier timed out";
+      return FK_ERR_CUDA;
+    }
+    M.adam_t += steps;
+    if (loss_hist) cudaMemcpy(loss_hist, M.d_hist, steps * sizeof(float), cudaMemcpyDeviceToHost);
+    return FK_OK;
+  }
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   // capture the whole loop in one CUDA graph: 2 kernels per step
   cudaGraph_t graph;

@@ -39,6 +39,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kNumAcc = 8;   // floating-point sums per thread
+constexpr float kPhiCut = 69.0f;  // Gaussian stencil weights exp(-arg) with arg >= 69 (< 1e-30) are not added
 
 struct AccD {
   double s = 0.0;
@@ -373,12 +374,15 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
           const int L = knn_window<R>(sp, snx, sny, ex, ey);
           const int kk = sp.k, m = sp.m;
           const R e2 = sp.e2;
+          // weights below exp(-kPhiCut) ~ 1e-30 are skipped (they are 0 or
+          // denormal in FP32 and far below any tolerance in FP64)
           int j = lane % kk;
           for (int jj = 0; jj < kk; ++jj) {
             int idx = L + j;
             if (idx >= m) idx -= m;
             const R dx = ex - snx[idx], dy = ey - sny[idx];
-            atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(Yv * fexp(-e2 * (dx * dx + dy * dy))));
+            const R arg = e2 * (dx * dx + dy * dy);
+            if (arg < R(kPhiCut)) atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(Yv * fexp(-arg)));
             if (++j == kk) j = 0;
           }
         }
@@ -404,7 +408,12 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
       qn = qb;
     };
 
-    while (__any_sync(kFull, active)) {
+    // One loop, one call site of process(): while any lane has a path it
+    // steps; queued exits are processed 32 at a time and, once the chunk is
+    // exhausted for this warp, the remainder.
+    for (;;) {
+      const bool any = __any_sync(kFull, active);
+      if (!any && qn == 0) break;
       bool exits = false, dom_wins = true, capped = false;
       R ex = R(0), ey = R(0);
       if (active) {
@@ -448,14 +457,12 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
           const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
           if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
         }
-        // sigma at the new point (kept for the next step) or at the projection
-        R sg;
-        if (w.d < R(0)) {
-          st = Problem<PROB>::template state<R>(bvp, x, y);
-          sg = Problem<PROB>::template sigma_of<R>(st);
-        } else {
-          sg = Problem<PROB>::template sigma_of<R>(Problem<PROB>::template state<R>(bvp, w.ex, w.ey));
-        }
+        // sigma at the new point (kept for the next step) or at the
+        // projection: one evaluation at the selected point, no divergence
+        const bool inside = w.d < R(0);
+        const R stq = Problem<PROB>::template state<R>(bvp, inside ? x : w.ex, inside ? y : w.ey);
+        if (inside) st = stq;
+        const R sg = Problem<PROB>::template sigma_of<R>(stq);
         const R nsx = w.nx * sg, nsy = w.ny * sg;
         const R thr = R(kGobet) * sqrt(nsx * nsx + nsy * nsy) * sqrth;
         capped = k >= a.max_steps;
@@ -481,13 +488,12 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         }
         qn += __popc(em);
         __syncwarp();
-        if (qn >= 32) {
-          process(32);
-          __syncwarp();
-        }
+      }
+      if (qn >= 32 || !any) {
+        process(qn >= 32 ? 32 : qn);
+        __syncwarp();
       }
     }
-    if (qn > 0) process(qn);
 
     // ---- the warp leaves the chunk: its sums into the item's FP64 sums
     double* sums = a.stats + static_cast<long long>(ch.item) * kNumStats;
