@@ -53,6 +53,7 @@ struct StencilSet {
   long long ipsi_total = 0, ainv_total = 0;
   int nmax = 0;
   DBuf d_arcs, d_theta, d_ipsi, d_patches, d_nodes, d_ainv;
+  DBuf d_e32, d_emax;  // patches: A^-1 - I in FP32 and its max |.| per patch
   bool uploaded = false;
   int size_of(int s) const { return kind == 1 ? arcs[s].n : patches[s].m; }
   long long acc_of(int s) const {
@@ -193,6 +194,10 @@ int upload_stencils(fk_ctx* ctx, fk::StencilSet& S, const std::vector<char>* hav
       FK_CUDA(fk::upload(doff, offs, s));
       FK_CUDA(fk::launch_inverse(ctx->w_tmp.as<double>(), S.d_ainv.as<double>(), dn.as<int>(), doff.as<long long>(), k,
                                  static_cast<int>(total), s));
+      FK_CUDA(S.d_e32.ensure(std::max<long long>(S.ainv_total, 1) * sizeof(float)));
+      FK_CUDA(S.d_emax.ensure(std::max(n_p, 1) * sizeof(float)));
+      FK_CUDA(fk::launch_split_inverse(S.d_patches.as<fk::PatchDev>(), n_p, S.d_ainv.as<double>(), S.d_e32.as<float>(),
+                                       S.d_emax.as<float>(), s));
       FK_CUDA(cudaStreamSynchronize(s));
     }
   }
@@ -361,7 +366,13 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   f.items = a.items;
   f.n_items = n;
   if (kind == 1) { f.arcs = a.arcs; f.arc_ipsi = S->d_ipsi.as<double>(); }
-  if (kind == 2) { f.patches = a.patches; f.patch_ainv = S->d_ainv.as<double>(); }
+  if (kind == 2) {
+    f.patches = a.patches;
+    f.patch_ainv = S->d_ainv.as<double>();
+    f.patch_e32 = S->d_e32.as<float>();
+    f.patch_emax = S->d_emax.as<float>();
+    f.split_ok = precision == FK_FP32 ? 1 : 0;
+  }
   f.stats = a.stats;
   f.acc = a.acc;
   f.stencil_kind = kind;

@@ -104,6 +104,12 @@ struct FinalizeArgs {
   const double* arc_ipsi;
   const PatchDev* patches;
   const double* patch_ainv;
+  // FP32-stepping assemblies: A_W^-1 = I + E_W with E_W in FP32 (same layout
+  // as patch_ainv) and max |E| per patch; the identity part is applied in
+  // FP64, E_W t_W in FP32 when max |E| < kSplitMaxE (may be null: FP64 only)
+  const float* patch_e32;
+  const float* patch_emax;
+  int split_ok;
   const double* stats;
   const double* acc;
   int stencil_kind;
@@ -134,5 +140,9 @@ cudaError_t launch_build_psi(const ArcDev* arcs, const double* theta, int n_arcs
 cudaError_t launch_build_windows(const PatchDev* patches, const double* nodes, int n_patches,
                                  const long long* win_base, long long total_windows, int k, double* out,
                                  cudaStream_t s);
+// E = A^-1 - I of every window in FP32, and max |E| per patch
+cudaError_t launch_split_inverse(const PatchDev* patches, int n_patches, const double* ainv, float* e32, float* emax,
+                                 cudaStream_t s);
+constexpr float kSplitMaxE = 1e-2f;
 
 }  // namespace fk

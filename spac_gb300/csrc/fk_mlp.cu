@@ -33,7 +33,7 @@ Mlp::~Mlp() {
   for (void* p : {static_cast<void*>(d_master), d_bf16, static_cast<void*>(d_m), static_cast<void*>(d_v),
                   static_cast<void*>(d_norm), static_cast<void*>(d_partial), static_cast<void*>(d_loss),
                   static_cast<void*>(d_rect), static_cast<void*>(d_table), static_cast<void*>(d_samples),
-                  static_cast<void*>(d_hist), static_cast<void*>(d_sync)})
+                  static_cast<void*>(d_hist), static_cast<void*>(d_sync), static_cast<void*>(d_sched)})
     if (p) cudaFree(p);
 }
 
@@ -54,6 +54,11 @@ constexpr int kNT = 2;               // n8 tiles per warp (16 columns)
 constexpr int kColsPerWarp = 8 * kNT;
 constexpr int kColGroups = W / kColsPerWarp;
 constexpr int kQuarters = kThreads / W;  // row groups of the per-column sums
+// weight-gradient products dW = dp^T h are 64 x 64 whatever the rows per CTA:
+// warp w owns output units 16 (w % 4).. and input units 32 (w / 4)..
+constexpr int kDwNT = 4;
+constexpr int kDwCols = 8 * kDwNT;
+static_assert(kThreads / 32 == (W / 16) * (W / kDwCols), "weight-gradient tiling");
 constexpr int LD = 72;          // bf16 leading dimension of [rows][64] tiles (144 B rows)
 constexpr int LDT = kRows + 8;  // bf16 leading dimension of [64][rows] transposed tiles (16 B multiple)
 static_assert(kMT == 1 && kWarpRows % 16 == 0, "rows per warp");
@@ -145,10 +150,12 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
   // per-column sums: thread <-> (column cj, row quarter cq)
   const int cj = tid % W, cq = tid / W;
   constexpr int kQRows = kRows / kQuarters;
-  // persistent gradient accumulators: this warp's tile of dW2 / dW3
-  float cW2[1][kNT][4], cW3[1][kNT][4];
+  // persistent gradient accumulators: this warp's (16-row, 32-column) tile of
+  // the 64x64 dW2 / dW3 (output unit x input unit, summed over the rows)
+  const int mw = (warp % (W / 16)) * 16, nw = (warp / (W / 16)) * kDwCols;
+  float cW2[1][kDwNT][4], cW3[1][kDwNT][4];
 #pragma unroll
-  for (int j = 0; j < kNT; ++j)
+  for (int j = 0; j < kDwNT; ++j)
 #pragma unroll
     for (int q = 0; q < 4; ++q) cW2[0][j][q] = cW3[0][j][q] = 0.f;
   float gW4 = 0.f, gB3 = 0.f, gB2 = 0.f, gB1 = 0.f, gW10 = 0.f, gW11 = 0.f, gB4 = 0.f, lsum = 0.f;
@@ -281,7 +288,7 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
     __syncthreads();
     // layer-3 backward: dW3 += dp3^T h2, db3, dW4, db4; dh2 = dp3 W3
     if (train) {
-      warp_gemm_tn<1, kNT, kRows>(cW3, S.dpt, LDT, m0, S.h2t, LDT, n0, lane);
+      warp_gemm_tn<1, kDwNT, kRows>(cW3, S.dpt, LDT, mw, S.h2t, LDT, nw, lane);
       for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) {
         gW4 += S.dO[r] * __bfloat162float(S.h3[r * LD + cj]);
         gB3 += __bfloat162float(S.dp[r * LD + cj]);
@@ -314,7 +321,7 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
     __syncthreads();
     // layer-2 backward: dW2 += dp2^T h1, db2; dh1 = dp2 W2
     if (train) {
-      warp_gemm_tn<1, kNT, kRows>(cW2, S.dpt, LDT, m0, S.h1t, LDT, n0, lane);
+      warp_gemm_tn<1, kDwNT, kRows>(cW2, S.dpt, LDT, mw, S.h1t, LDT, nw, lane);
       for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) gB2 += __bfloat162float(S.dp[r * LD + cj]);
     }
     {
@@ -371,11 +378,11 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
   // ---- write this CTA's gradient partial
   float* out = a.partial + (static_cast<long long>(region) * a.ctas_per_region + cta) * NPARAM;
 #pragma unroll
-  for (int nt = 0; nt < kNT; ++nt)
+  for (int nt = 0; nt < kDwNT; ++nt)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int r = m0 + g + ((q >> 1) << 3);
-      const int col = n0 + nt * 8 + 2 * t4 + (q & 1);
+      const int r = mw + g + ((q >> 1) << 3);
+      const int col = nw + nt * 8 + 2 * t4 + (q & 1);
       out[OFF_W2 + r * W + col] = cW2[0][nt][q];
       out[OFF_W3 + r * W + col] = cW3[0][nt][q];
     }
@@ -512,9 +519,15 @@ struct TrainArgs {
   float loss_scale;
   int steps;
   long long t0;      // Adam steps taken before this launch
-  double lr;
+  const float* sched;  // per step: learning rate, 1 - beta1^t, 1 - beta2^t
 };
 constexpr unsigned long long kBarrierNs = 5000000000ull;
+// Adam on the CTA partials: kAdamGroups thread groups of 64, each loading
+// up to kMaxPartialLoads partials per parameter; the persistent grid has at
+// most 4 x 40 = 160 CTAs per region (one per SM of a 152-SM part)
+constexpr int kAdamGroups = kThreads / W;
+constexpr int kMaxPartialLoads = 40;
+constexpr int kMaxPersistentCtas = kAdamGroups * kMaxPartialLoads;
 
 __device__ __forceinline__ unsigned long long mlp_global_ns() {
   unsigned long long t;
@@ -548,7 +561,6 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* err) {
 
 __global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs t) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ float s_coef[3];  // lr_t, bc1, bc2 of the step
   const int nb = gridDim.x * gridDim.y;
   const int bid = blockIdx.y * gridDim.x + blockIdx.x;
   const int ctas = t.a.ctas_per_region;
@@ -562,45 +574,51 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs 
     mlp_pass_body(a, blockIdx.y, blockIdx.x, gridDim.x, smem_raw);
     target += nb;
     if (!grid_barrier(t.bar, target, t.err)) return;
-    if (threadIdx.x == 0) {
-      const double tt = static_cast<double>(t.t0 + s + 1);
-      // cosine decay from lr to lr/100 over the launch
-      s_coef[0] = static_cast<float>(t.lr * (0.01 + 0.99 * 0.5 * (1.0 + cos(3.141592653589793 * s / t.steps))));
-      s_coef[1] = static_cast<float>(1.0 - pow(0.9, tt));
-      s_coef[2] = static_cast<float>(1.0 - pow(0.999, tt));
-    }
-    __syncthreads();
-    const float lr_t = s_coef[0], bc1 = s_coef[1], bc2 = s_coef[2];
-    // 8 lanes per parameter, each summing every 8th CTA partial (all loads
-    // independent), then a fixed shuffle tree: the same order as mlp_adam_kernel
-    const int sub = threadIdx.x & 7;
-    for (long long base = e0; base < e1; base += kThreads / 8) {
-      const long long e = base + (threadIdx.x >> 3);
+    // the step's learning rate and bias corrections, computed on the host
+    const float lr_t = __ldg(t.sched + 3 * s), bc1 = __ldg(t.sched + 3 * s + 1), bc2 = __ldg(t.sched + 3 * s + 2);
+    // Thread (g, j): parameter e0 + j of a 64-parameter round and the CTA
+    // partials g, g + 4, ... in order; a warp's loads of one CTA's partial
+    // are 32 consecutive floats.  The step is bound by L2 latency, so every
+    // thread issues all its loads (predicated) before it adds any; the four
+    // group sums are combined in a fixed order.
+    __shared__ float s_part[kAdamGroups][W];
+    const int j = threadIdx.x % W, grp = threadIdx.x / W;
+    for (long long base = e0; base < e1; base += W) {
+      const long long e = base + j;
       const bool live = e < e1;
-      float part = 0.f;
       int r = 0, p = 0;
+      float part = 0.f;
       if (live) {
         r = static_cast<int>(e / NPARAM);
         p = static_cast<int>(e % NPARAM);
         const float* src = a.partial + static_cast<long long>(r) * ctas * NPARAM + p;
-        float a0 = 0.f, a1 = 0.f;
-        int c = sub;
-        for (; c + 8 < ctas; c += 16) {
-          a0 += __ldcg(src + static_cast<long long>(c) * NPARAM);
-          a1 += __ldcg(src + static_cast<long long>(c + 8) * NPARAM);
+        float vals[kMaxPartialLoads];
+#pragma unroll
+        for (int i = 0; i < kMaxPartialLoads; ++i) {
+          const int c = grp + kAdamGroups * i;
+          vals[i] = c < ctas ? __ldcg(src + static_cast<long long>(c) * NPARAM) : 0.f;
         }
-        if (c < ctas) a0 += __ldcg(src + static_cast<long long>(c) * NPARAM);
-        part = a0 + a1;
+#pragma unroll
+        for (int i = 0; i < kMaxPartialLoads; ++i) part += vals[i];
       }
-      part += __shfl_xor_sync(0xffffffffu, part, 1);
-      part += __shfl_xor_sync(0xffffffffu, part, 2);
-      part += __shfl_xor_sync(0xffffffffu, part, 4);
-      if (live && sub == 0) adam_apply(e, r, p, part, t.params, t.wbf, t.m, t.v, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
+      s_part[grp][j] = part;
+      __syncthreads();
+      if (grp == 0 && live) {
+        float gsum = s_part[0][j];
+#pragma unroll
+        for (int q = 1; q < kAdamGroups; ++q) gsum += s_part[q][j];
+        adam_apply(e, r, p, gsum, t.params, t.wbf, t.m, t.v, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
+      }
+      __syncthreads();
     }
-    if (bid == 0 && threadIdx.x == 0) {
+    if (bid == 0 && threadIdx.x < 32) {
+      // loss of the step: one warp, loads first, then a shuffle tree
+      const int nl = t.a.n_regions * ctas;
       float sl = 0.f;
-      for (int i = 0; i < t.a.n_regions * ctas; ++i) sl += __ldcg(a.loss + i);
-      t.hist[s] = sl * t.loss_scale;
+      for (int i = threadIdx.x; i < nl; i += 32) sl += __ldcg(a.loss + i);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o);
+      if (threadIdx.x == 0) t.hist[s] = sl * t.loss_scale;
     }
     target += nb;
     if (!grid_barrier(t.bar, target, t.err)) return;
@@ -779,7 +797,8 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
     while (rows_per_cta < batch && batch % (2 * rows_per_cta) == 0 &&
            static_cast<long long>(batch / rows_per_cta) * M.n_regions > capacity)
       rows_per_cta *= 2;
-    persistent = static_cast<long long>(batch / rows_per_cta) * M.n_regions <= capacity;
+    persistent = static_cast<long long>(batch / rows_per_cta) * M.n_regions <= capacity &&
+                 batch / rows_per_cta <= kMaxPersistentCtas;
   }
   if (!persistent) {
     // one 64-row tile per CTA (the step is latency-bound: more CTAs, shorter
@@ -837,8 +856,24 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
     t.loss_scale = 1.f / (static_cast<float>(batch) * M.n_regions);
     t.steps = steps;
     t.t0 = M.adam_t;
-    t.lr = lr;
-    e = cudaMemsetAsync(M.d_sync, 0, 2 * sizeof(unsigned), s);
+    // learning-rate schedule and Adam bias corrections of every step (the
+    // same values as the per-step launches below compute)
+    std::vector<float> sched(3 * static_cast<size_t>(steps));
+    for (int st = 0; st < steps; ++st) {
+      const double tt = static_cast<double>(M.adam_t + st + 1);
+      sched[3 * st] = static_cast<float>(lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(M_PI * st / std::max(1, steps)))));
+      sched[3 * st + 1] = static_cast<float>(1.0 - std::pow(0.9, tt));
+      sched[3 * st + 2] = static_cast<float>(1.0 - std::pow(0.999, tt));
+    }
+    if (M.d_sched) cudaFree(M.d_sched);
+    M.d_sched = nullptr;
+    if (cudaMalloc(&M.d_sched, sched.size() * sizeof(float)) != cudaSuccess) {
+      err = "mlp: training buffers";
+      return FK_ERR_CUDA;
+    }
+    t.sched = M.d_sched;
+    e = cudaMemcpyAsync(M.d_sched, sched.data(), sched.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(M.d_sync, 0, 2 * sizeof(unsigned), s);
     void* args[] = {&t};
     if (e == cudaSuccess)
       e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel), dim3(ctas, M.n_regions),

@@ -21,6 +21,7 @@ struct Mlp {
   float* d_loss = nullptr;
   float* d_hist = nullptr;
   unsigned* d_sync = nullptr;       // persistent training: barrier counter and error word
+  float* d_sched = nullptr;         // persistent training: per-step learning rate and bias corrections
   float4* d_samples = nullptr;      // training samples (x, y, target) grouped by region
   int* d_sample_off = nullptr;      // inside the d_samples allocation
   float2* d_table = nullptr;        // grad u_hat on a G x G grid per region
