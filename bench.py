@@ -435,6 +435,7 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=10
     # unbiased), so it runs at the coarse step pilot_h
     pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec)
     t_pilot = time.perf_counter() - t0
+    pilot_kernel_ms = ctx.last_timing()[0]
     rects = np.array([[0.0, 0.0, 1.0, 1.0]])
     mid = fk.C.c_int()
     ctx.check(ctx.L.fk_mlp_create(ctx.h, 1, rects.ctypes.data_as(fk._dp), 12345, fk.C.byref(mid)))
@@ -459,6 +460,7 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=10
     t_cv = t_pilot + t_train + t_table + t_run
     out["learned_cv"] = {"paths_per_item": n_cv, "seconds": t_cv, "rms": rms_of(stc), "pilot_s": t_pilot,
                          "train_s": t_train, "table_s": t_table, "run_s": t_run, "run_kernels_ms": kc,
+                         "pilot_kernel_ms": pilot_kernel_ms,
                          "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
                          "train_loss_first_last": [float(hist[0]), float(hist[-1])]}
     out["variance_reduction"] = float(var_p.mean() / max(var_c.mean(), 1e-300))

@@ -434,14 +434,14 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a)
 
 // Adam update of parameter e (= region r, index p) with gradient gsum; keeps
 // the BF16 copies (W and W^T of the two 64x64 layers) in step.
-__device__ __forceinline__ void adam_apply(long long e, int r, int p, float gsum, float* params, __nv_bfloat16* wbf,
-                                           float* m, float* v, float lr, float b1, float b2, float eps, float bc1,
-                                           float bc2) {
-  const float mm = b1 * m[e] + (1.f - b1) * gsum;
-  const float vv = b2 * v[e] + (1.f - b2) * gsum * gsum;
+__device__ __forceinline__ void adam_apply_vals(long long e, int r, int p, float gsum, float m_old, float v_old,
+                                                float th_old, float* params, __nv_bfloat16* wbf, float* m, float* v,
+                                                float lr, float b1, float b2, float eps, float bc1, float bc2) {
+  const float mm = b1 * m_old + (1.f - b1) * gsum;
+  const float vv = b2 * v_old + (1.f - b2) * gsum * gsum;
   m[e] = mm;
   v[e] = vv;
-  const float th = params[e] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+  const float th = th_old - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
   params[e] = th;
   __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
   const __nv_bfloat16 tb = __float2bfloat16_rn(th);
@@ -454,6 +454,11 @@ __device__ __forceinline__ void adam_apply(long long e, int r, int p, float gsum
     B[2 * W * W + q] = tb;
     B[3 * W * W + i * W + o] = tb;
   }
+}
+__device__ __forceinline__ void adam_apply(long long e, int r, int p, float gsum, float* params, __nv_bfloat16* wbf,
+                                           float* m, float* v, float lr, float b1, float b2, float eps, float bc1,
+                                           float bc2) {
+  adam_apply_vals(e, r, p, gsum, m[e], v[e], params[e], params, wbf, m, v, lr, b1, b2, eps, bc1, bc2);
 }
 
 // Sum of partials (fixed order) and Adam update; refreshes the BF16 copies.
@@ -522,11 +527,12 @@ struct TrainArgs {
   const float* sched;  // per step: learning rate, 1 - beta1^t, 1 - beta2^t
 };
 constexpr unsigned long long kBarrierNs = 5000000000ull;
-// Adam on the CTA partials: kAdamGroups thread groups of 64, each loading
-// up to kMaxPartialLoads partials per parameter; the persistent grid has at
-// most 4 x 40 = 160 CTAs per region (one per SM of a 152-SM part)
-constexpr int kAdamGroups = kThreads / W;
-constexpr int kMaxPartialLoads = 40;
+// Adam on the CTA partials: kAdamGroups thread groups of kAdamRound, each
+// loading up to kMaxPartialLoads partials per parameter; the persistent grid
+// has at most 2 x 80 = 160 CTAs per region (one per SM of a 152-SM part)
+constexpr int kAdamGroups = 2;
+constexpr int kAdamRound = kThreads / kAdamGroups;
+constexpr int kMaxPartialLoads = 80;
 constexpr int kMaxPersistentCtas = kAdamGroups * kMaxPartialLoads;
 
 __device__ __forceinline__ unsigned long long mlp_global_ns() {
@@ -576,21 +582,27 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs 
     if (!grid_barrier(t.bar, target, t.err)) return;
     // the step's learning rate and bias corrections, computed on the host
     const float lr_t = __ldg(t.sched + 3 * s), bc1 = __ldg(t.sched + 3 * s + 1), bc2 = __ldg(t.sched + 3 * s + 2);
-    // Thread (g, j): parameter e0 + j of a 64-parameter round and the CTA
-    // partials g, g + 4, ... in order; a warp's loads of one CTA's partial
-    // are 32 consecutive floats.  The step is bound by L2 latency, so every
-    // thread issues all its loads (predicated) before it adds any; the four
-    // group sums are combined in a fixed order.
-    __shared__ float s_part[kAdamGroups][W];
-    const int j = threadIdx.x % W, grp = threadIdx.x / W;
-    for (long long base = e0; base < e1; base += W) {
+    // Thread (g, j): parameter e0 + j of a kAdamRound-parameter round (one
+    // round covers a CTA's slice) and the CTA partials g, g + kAdamGroups, ...
+    // in order; a warp's loads of one CTA's partial are 32 consecutive
+    // floats.  The step is bound by L2 latency, so every thread issues all its
+    // loads (predicated), and the parameter's Adam state with them, before it
+    // adds any; the group sums are combined in a fixed order.
+    __shared__ float s_part[kAdamGroups][kAdamRound];
+    const int j = threadIdx.x % kAdamRound, grp = threadIdx.x / kAdamRound;
+    for (long long base = e0; base < e1; base += kAdamRound) {
       const long long e = base + j;
       const bool live = e < e1;
       int r = 0, p = 0;
-      float part = 0.f;
+      float part = 0.f, m_old = 0.f, v_old = 0.f, th_old = 0.f;
       if (live) {
         r = static_cast<int>(e / NPARAM);
         p = static_cast<int>(e % NPARAM);
+        if (grp == 0) {
+          m_old = t.m[e];
+          v_old = t.v[e];
+          th_old = t.params[e];
+        }
         const float* src = a.partial + static_cast<long long>(r) * ctas * NPARAM + p;
         float vals[kMaxPartialLoads];
 #pragma unroll
@@ -607,7 +619,8 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs 
         float gsum = s_part[0][j];
 #pragma unroll
         for (int q = 1; q < kAdamGroups; ++q) gsum += s_part[q][j];
-        adam_apply(e, r, p, gsum, t.params, t.wbf, t.m, t.v, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
+        adam_apply_vals(e, r, p, gsum, m_old, v_old, th_old, t.params, t.wbf, t.m, t.v, lr_t, 0.9f, 0.999f, 1e-8f,
+                        bc1, bc2);
       }
       __syncthreads();
     }
