@@ -96,6 +96,9 @@ struct fk_ctx {
 
 namespace {
 
+// items of at most this many paths on average run the path kernel in warp mode
+constexpr long long kWarpModeMaxPaths = 4096;
+
 int fail(fk_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
@@ -290,14 +293,27 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   if (kind != 0)
     for (auto& x : it)
       if (x.stencil >= 0) smem_nodes = std::max(smem_nodes, S->size_of(x.stencil));
-  const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes);
+  // Items of few paths (on average at most kWarpModeMaxPaths) run in warp
+  // mode: every warp takes its own chunks and adds the stencil moments to
+  // global memory, so an item's slowest path holds up one warp only.  A
+  // launch shape set by the caller (fk_set_launch, the autotuner) keeps the
+  // shared chunk slots.
+  long long n_live = 0;
+  for (auto& x : it) if (!x.frontera && x.paths > 0) ++n_live;
+  const bool warp_mode = ctx->chunk <= 0 && n_live > 0 && total_paths <= kWarpModeMaxPaths * n_live;
+  const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes, warp_mode, block);
   if (sacc_bytes > 200 * 1024) return fail(ctx, FK_ERR_CAPACITY, "stencil accumulators exceed shared memory");
-  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes);
+  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes, warp_mode);
   const int grid = std::max(1, ctx->num_sms * occ);
-  // Chunk size: at least 4 chunks per CTA of the persistent grid, at most
-  // 32768 paths; an item is split into equal chunks (no small remainder).
+  // Chunk size.  Slots: at least 4 chunks per CTA of the persistent grid, at
+  // most 32768 paths.  Warp mode: about 6 chunks per warp (the last round of
+  // chunks leaves warps idle), 64..4096 paths.  An item is split into equal
+  // chunks (no small remainder).
   long long chunk = ctx->chunk;
-  if (chunk <= 0) {
+  if (chunk <= 0 && warp_mode) {
+    chunk = total_paths / (6LL * grid * (block / 32));
+    chunk = std::max<long long>(64, std::min<long long>(chunk, 4096));
+  } else if (chunk <= 0) {
     chunk = total_paths / (4LL * grid);
     chunk = std::max<long long>(block, std::min<long long>(chunk, 32768));
   }
@@ -352,7 +368,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   a.acc_words = acc_words;
   a.smem_nodes = smem_nodes;
   FK_CUDA(cudaEventRecord(ctx->ev[0], s));
-  if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s));
+  if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s, warp_mode));
   FK_CUDA(cudaEventRecord(ctx->ev[1], s));
 
   // finalize

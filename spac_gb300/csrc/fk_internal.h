@@ -54,12 +54,13 @@ enum { kStatScore = 0, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScor
        kStatCap, kStatXi2, kStatPaths, kNumStats = 12 };
 
 // Path-kernel shared memory: each CTA keeps paths_slots() chunks in flight
-// (3 for FP32 stepping, 2 for FP64), so that its warps move on to the next
-// chunk while the last paths of the previous one finish.  A slot holds the
-// chunk's stencil accumulators followed by its stencil nodes (patch node
-// coordinates in the stepping precision, or arc angles in FP64), each part
-// padded to 16 bytes.
-__host__ __device__ inline int paths_slots(int precision) { return precision == 0 ? 2 : 3; }
+// (kSlotsFP32 for FP32 stepping, 2 for FP64), so that its warps move on to
+// the next chunk while the last paths of the previous one finish.  A slot
+// holds the chunk's stencil accumulators followed by its stencil nodes (patch
+// node coordinates in the stepping precision, or arc angles in FP64), each
+// part padded to 16 bytes.
+constexpr int kSlotsFP32 = 3;
+__host__ __device__ inline int paths_slots(int precision) { return precision == 0 ? 2 : kSlotsFP32; }
 __host__ __device__ inline size_t paths_slot_acc_bytes(int precision, int stencil_kind, int acc_words) {
   const size_t w = (precision == 0 || stencil_kind == 1) ? 8 : 4;
   return (static_cast<size_t>(acc_words) * w + 15) & ~static_cast<size_t>(15);
@@ -125,10 +126,15 @@ struct FinalizeArgs {
 };
 
 // host launchers (fk_paths.cu)
-size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes);
+// warp_mode: every warp works its own chunks and adds the stencil moments to
+// the items' global accumulators (items of few paths); otherwise the CTA's
+// warps share chunk slots with shared-memory accumulators
+size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes, bool warp_mode = false,
+                        int block = 256);
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block,
-                         size_t smem, cudaStream_t s);
-int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem);
+                         size_t smem, cudaStream_t s, bool warp_mode = false);
+int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem,
+                           bool warp_mode = false);
 // host launchers (fk_kernels.cu)
 cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s);
 // batched FP64 full-pivot Gauss-Jordan inverse: matrix b is ns[b] x ns[b],

@@ -144,6 +144,43 @@ __device__ bool wait_slot(const int* ready, int seq, unsigned long long limit_ns
   return ok != 0;
 }
 
+// One warp copies an item's stencil into shared memory: patch node
+// coordinates (stepping precision) and side descriptors, or arc angles.
+template <typename R, int ST>
+__device__ void stage_stencil(const LaunchArgs& a, SlotSh<R>& sl, unsigned char* nodes_mem, int stencil, int lane) {
+  if (ST == 2) {
+    R* snx = reinterpret_cast<R*>(nodes_mem);
+    R* sny = snx + a.smem_nodes;
+    const PatchDev& P = a.patches[stencil];
+    const double* nd = a.patch_nodes + P.node_off;
+    for (int i = lane; i < P.m; i += 32) {
+      snx[i] = R(nd[2 * i]);
+      sny[i] = R(nd[2 * i + 1]);
+    }
+    if (lane < 4) {
+      const int s = lane;
+      sl.sp.side_first[s] = P.side_first[s];
+      sl.sp.side_count[s] = P.side_count[s];
+      sl.sp.side_axis[s] = P.side_axis[s];
+      sl.sp.side_fixed[s] = R(P.side_fixed[s]);
+      sl.sp.side_start[s] = R(P.side_start[s]);
+      sl.sp.side_inv_step[s] = R(1.0 / P.side_step[s]);
+    }
+    if (lane == 0) {
+      sl.sp.m = P.m;
+      sl.sp.k = P.k;
+      sl.sp.closed = P.closed;
+      sl.sp.e2 = R(P.eps2);
+    }
+  }
+  if (ST == 1) {
+    double* sth = reinterpret_cast<double*>(nodes_mem);
+    const ArcDev& A = a.arcs[stencil];
+    for (int i = lane; i < A.n; i += 32) sth[i] = a.arc_theta[A.theta_off + i];
+    if (lane == 0) sl.sarc = A;
+  }
+}
+
 // One warp claims the next chunk of the global queue for a slot, clears the
 // slot's accumulators, stages the chunk's stencil and publishes the slot as
 // sequence position `seq`.
@@ -158,37 +195,7 @@ __device__ void fill_slot(const LaunchArgs& a, SlotSh<R>& sl, unsigned char* mem
     const ItemDev& itg = a.items[ch.item];
     uint4* z = reinterpret_cast<uint4*>(mem);
     for (int i = lane; i < static_cast<int>(acc_bytes / 16); i += 32) z[i] = make_uint4(0u, 0u, 0u, 0u);
-    if (ST == 2) {
-      R* snx = reinterpret_cast<R*>(mem + acc_bytes);
-      R* sny = snx + a.smem_nodes;
-      const PatchDev& P = a.patches[itg.stencil];
-      const double* nd = a.patch_nodes + P.node_off;
-      for (int i = lane; i < P.m; i += 32) {
-        snx[i] = R(nd[2 * i]);
-        sny[i] = R(nd[2 * i + 1]);
-      }
-      if (lane < 4) {
-        const int s = lane;
-        sl.sp.side_first[s] = P.side_first[s];
-        sl.sp.side_count[s] = P.side_count[s];
-        sl.sp.side_axis[s] = P.side_axis[s];
-        sl.sp.side_fixed[s] = R(P.side_fixed[s]);
-        sl.sp.side_start[s] = R(P.side_start[s]);
-        sl.sp.side_inv_step[s] = R(1.0 / P.side_step[s]);
-      }
-      if (lane == 0) {
-        sl.sp.m = P.m;
-        sl.sp.k = P.k;
-        sl.sp.closed = P.closed;
-        sl.sp.e2 = R(P.eps2);
-      }
-    }
-    if (ST == 1) {
-      double* sth = reinterpret_cast<double*>(mem + acc_bytes);
-      const ArcDev& A = a.arcs[itg.stencil];
-      for (int i = lane; i < A.n; i += 32) sth[i] = a.arc_theta[A.theta_off + i];
-      if (lane == 0) sl.sarc = A;
-    }
+    stage_stencil<R, ST>(a, sl, mem + acc_bytes, itg.stencil, lane);
     if (lane == 0) {
       sl.chunk = c;
       sl.next = 0u;
@@ -249,17 +256,25 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
 
 // FP64 stepping is bound by the FP64 pipe, not by latency: it trades
 // occupancy for registers (2 CTAs of 256 per SM instead of 3).
-template <typename R, int PROB, int ST>
+//
+// WM (warp mode, for items of few paths): every warp claims its own chunk
+// from the queue, stages the item's stencil in its own shared-memory
+// corner and adds the stencil moments straight to the item's FP64
+// accumulators with global atomics; no warp ever waits for another, so an
+// item's longest path delays only its own warp.  Otherwise the CTA's warps
+// share the chunk slots described above.
+template <typename R, int PROB, int ST, bool WM>
 __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) paths_kernel(const LaunchArgs a) {
-  using SAcc = typename SAccType<R, ST>::type;
+  using SAcc = typename std::conditional<WM, double, typename SAccType<R, ST>::type>::type;
   using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
   constexpr int kPrec = std::is_same<R, double>::value ? 0 : 1;
-  constexpr int S = kPrec == 0 ? 2 : 3;  // paths_slots(kPrec)
+  constexpr int S = WM ? kMaxBlockWarps : (kPrec == 0 ? 2 : kSlotsFP32);  // slots, or one per warp
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ SlotSh<R> slots[S];
   __shared__ ExitQueue<R> sq[kMaxBlockWarps];
-  const size_t acc_bytes = paths_slot_acc_bytes(kPrec, ST, a.acc_words);
-  const size_t slot_bytes = paths_slot_bytes(kPrec, ST, a.acc_words, a.smem_nodes);
+  const size_t acc_bytes = WM ? 0 : paths_slot_acc_bytes(kPrec, ST, a.acc_words);
+  const size_t slot_bytes = WM ? paths_slot_bytes(kPrec, ST, 0, a.smem_nodes)
+                               : paths_slot_bytes(kPrec, ST, a.acc_words, a.smem_nodes);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const bool cv = a.cv != 0;         // any control term
@@ -267,36 +282,54 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
   const bool cv_table = a.cv == 2;   // F from the learned gradient table
   const unsigned long long limit_ns = 60000000000ull + 1000ull * static_cast<unsigned long long>(a.max_steps);
 
-  if (threadIdx.x < S) slots[threadIdx.x].ready = -1;
-  __syncthreads();
-  for (int s = warp; s < S; s += nwarps) fill_slot<R, ST>(a, slots[s], smem_raw + s * slot_bytes, acc_bytes, s, nwarps, lane);
+  if (!WM) {
+    if (threadIdx.x < S) slots[threadIdx.x].ready = -1;
+    __syncthreads();
+    for (int s = warp; s < S; s += nwarps)
+      fill_slot<R, ST>(a, slots[s], smem_raw + s * slot_bytes, acc_bytes, s, nwarps, lane);
+  }
 
   ExitQueue<R>& q = sq[warp];
   // Slots known to hold no further chunk: a slot whose chunk queue came up
   // empty is never refilled, so the walk ends once every slot is dead.
   unsigned dead = 0u;
-  for (int g = 0; dead != (1u << S) - 1u; ++g) {
-    const int si = g % S;
-    if (dead & (1u << si)) continue;
+  for (int g = 0;; ++g) {
+    int si, c;
+    if (WM) {
+      // this warp's next chunk
+      si = warp;
+      int cc = 0;
+      if (lane == 0) cc = atomicAdd(a.queue, 1);
+      c = __shfl_sync(kFull, cc, 0);
+      if (c >= a.n_chunks) break;
+      stage_stencil<R, ST>(a, slots[si], smem_raw + si * slot_bytes, a.items[a.chunks[c].item].stencil, lane);
+      __syncwarp();
+    } else {
+      if (dead == (1u << S) - 1u) break;
+      si = g % S;
+      if (dead & (1u << si)) continue;
+      if (!wait_slot(&slots[si].ready, g, limit_ns, lane)) {
+        if (lane == 0) atomicExch(a.queue + 1, 1);
+        break;
+      }
+      c = ld_volatile(&slots[si].chunk);
+      if (c < 0) {
+        dead |= 1u << si;
+        continue;
+      }
+    }
     SlotSh<R>& sl = slots[si];
-    if (!wait_slot(&sl.ready, g, limit_ns, lane)) {
-      if (lane == 0) atomicExch(a.queue + 1, 1);
-      break;
-    }
-    const int c = ld_volatile(&sl.chunk);
-    if (c < 0) {
-      dead |= 1u << si;
-      continue;
-    }
     unsigned char* mem = smem_raw + si * slot_bytes;
-    SAcc* sacc = reinterpret_cast<SAcc*>(mem);
+    const ChunkDev ch = a.chunks[c];
+    const ItemDev& itg = a.items[ch.item];
+    // stencil moments: the slot's shared accumulators, or (warp mode) the
+    // item's FP64 accumulators in global memory
+    SAcc* sacc = WM ? reinterpret_cast<SAcc*>(a.acc + itg.acc_off) : reinterpret_cast<SAcc*>(mem);
     const R* snx = reinterpret_cast<const R*>(mem + acc_bytes);
     const R* sny = snx + a.smem_nodes;
     const double* sth = reinterpret_cast<const double*>(mem + acc_bytes);
     const PatchSh<R>& sp = sl.sp;
     const ArcDev& sarc = sl.sarc;
-    const ChunkDev ch = a.chunks[c];
-    const ItemDev& itg = a.items[ch.item];
     const unsigned n_ch = ch.p1 - ch.p0;
 
     // the item's BVP (independent problems of one functor share a launch)
@@ -328,9 +361,10 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
     R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0;
     int k = 0;
     uint32_t w2 = 0, w3 = 0;
-    // every lane's first path of the chunk (chunk-local index)
-    unsigned base = 0;
-    if (lane == 0) base = atomicAdd(&sl.next, 32u);
+    // every lane's first path of the chunk (chunk-local index); in warp mode
+    // the warp owns the chunk and counts its paths in a register
+    unsigned base = 0, wnext = 32u;
+    if (!WM && lane == 0) base = atomicAdd(&sl.next, 32u);
     unsigned pl = __shfl_sync(kFull, base, 0) + lane;
     bool active = pl < n_ch;
     int qn = 0;  // queued exits of this warp (warp-uniform)
@@ -476,8 +510,13 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         const int rank = __popc(em & ((1u << lane) - 1u));
         const int leader = __ffs(em) - 1;
         unsigned nb = 0;
-        if (lane == leader) nb = atomicAdd(&sl.next, static_cast<unsigned>(__popc(em)));
-        nb = __shfl_sync(kFull, nb, leader);
+        if (WM) {
+          nb = wnext;
+          wnext += static_cast<unsigned>(__popc(em));
+        } else {
+          if (lane == leader) nb = atomicAdd(&sl.next, static_cast<unsigned>(__popc(em)));
+          nb = __shfl_sync(kFull, nb, leader);
+        }
         if (exits) {
           const int e = qn + rank;
           q.x[e] = ex; q.y[e] = ey; q.Y[e] = Y; q.Z[e] = Z; q.xi[e] = xi;
@@ -518,6 +557,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
       if (n_done) atomicAdd(&sums[kStatPaths], static_cast<double>(n_done));
     }
     __syncwarp();
+    if (WM) continue;  // the warp's moments are already in global memory
     __threadfence_block();
     int left = 0;
     if (lane == 0) left = atomicSub(&sl.warps_left, 1);
@@ -538,45 +578,47 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
   }
 }
 
-template <typename R, int PROB>
+template <typename R, int PROB, bool WM>
 const void* paths_fn(int st) {
   switch (st) {
-    case 1: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 1>);
-    case 2: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2>);
-    default: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 0>);
+    case 1: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 1, WM>);
+    case 2: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2, WM>);
+    default: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 0, WM>);
   }
 }
-template <typename R>
+template <typename R, bool WM>
 const void* paths_fn_r(int problem, int st) {
   switch (problem) {
-    case 1: return paths_fn<R, 1>(st);
-    case 2: return paths_fn<R, 2>(st);
-    case 3: return paths_fn<R, 3>(st);
-    default: return paths_fn<R, 0>(st);
+    case 1: return paths_fn<R, 1, WM>(st);
+    case 2: return paths_fn<R, 2, WM>(st);
+    case 3: return paths_fn<R, 3, WM>(st);
+    default: return paths_fn<R, 0, WM>(st);
   }
 }
-const void* select_paths(int problem, int precision, int st) {
-  return precision == 1 ? paths_fn_r<float>(problem, st) : paths_fn_r<double>(problem, st);
+const void* select_paths(int problem, int precision, int st, bool warp_mode) {
+  if (warp_mode) return precision == 1 ? paths_fn_r<float, true>(problem, st) : paths_fn_r<double, true>(problem, st);
+  return precision == 1 ? paths_fn_r<float, false>(problem, st) : paths_fn_r<double, false>(problem, st);
 }
 
 }  // namespace
 
-size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes) {
+size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes, bool warp_mode, int block) {
+  if (warp_mode) return static_cast<size_t>(block / 32) * paths_slot_bytes(precision, stencil_kind, 0, smem_nodes);
   return static_cast<size_t>(paths_slots(precision)) * paths_slot_bytes(precision, stencil_kind, acc_words, smem_nodes);
 }
 
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block, size_t smem,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool warp_mode) {
   if (block < 32 || block > 256 || block % 32 != 0) return cudaErrorInvalidValue;
-  const void* fn = select_paths(problem, precision, a.stencil_kind);
+  const void* fn = select_paths(problem, precision, a.stencil_kind, warp_mode);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<LaunchArgs*>(&a)};
   return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, s);
 }
 
-int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int, int block, size_t smem) {
-  const void* fn = select_paths(problem, precision, stencil_kind);
+int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int, int block, size_t smem, bool warp_mode) {
+  const void* fn = select_paths(problem, precision, stencil_kind, warp_mode);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 1;

@@ -148,7 +148,10 @@ def stats_dict(s):
 
 
 def stats_array(arr):
-    return {k: np.array([getattr(s, k) for s in arr]) for k in STAT_FIELDS}
+    """fk_stats array -> dict of per-item numpy columns (a copy of the buffer, no per-item Python work)."""
+    n = len(arr)
+    flat = np.frombuffer(arr, dtype=np.float64, count=n * len(STAT_FIELDS)).reshape(n, len(STAT_FIELDS)).copy()
+    return {k: flat[:, i] for i, k in enumerate(STAT_FIELDS)}
 
 
 class Context:

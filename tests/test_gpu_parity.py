@@ -24,6 +24,16 @@ def _oracle_session(orc, gpu):
     return orc.Session(orc.RNG_PHILOX, seed=SEED)
 
 
+@pytest.fixture(params=["warp", "slots"])
+def launch(request, gpu):
+    """Both path-kernel modes: items of few paths run in warp mode by default;
+    a caller-set launch shape forces the shared chunk slots."""
+    if request.param == "slots":
+        gpu.set_launch(256, 128)
+    yield request.param
+    gpu.set_launch(0, 0)
+
+
 CASES = [  # problem, cv, dom, points, sub (shape, params) or None, h
     (0, 0, (0, 0, 1, 1), [(0.3, 0.4), (0.05, 0.9), (0.5, 0.5)], None, 1e-3),
     (0, 1, (0, 0, 1, 1), [(0.7, 0.2)], None, 2e-3),
@@ -35,7 +45,7 @@ CASES = [  # problem, cv, dom, points, sub (shape, params) or None, h
 
 
 @pytest.mark.parametrize("case", range(len(CASES)))
-def test_point_solves_fp64_match_oracle(gpu, orc, fk, case):
+def test_point_solves_fp64_match_oracle(gpu, orc, fk, case, launch):
     problem, cv, dom, pts, sub, h = CASES[case]
     prob = (dom[1], dom[2], dom[0], 0) if problem == fk.DISK else (0, 0, 0, 0)
     dshape = fk.CIRCLE if problem == fk.DISK else fk.RECT
@@ -186,7 +196,7 @@ def _patch_rect(gpu, mesh, s):
     return gpu._rects[s]
 
 
-def test_square_patch_assembly_matches_oracle(gpu, orc, fk):
+def test_square_patch_assembly_matches_oracle(gpu, orc, fk, launch):
     n_sub, nps, e, eps_sp, k = 3, 9, 0.25, 1.0, 6
     mesh = gpu.mesh_square_patches((0, 0, 1, 1), n_sub, nps, e, eps_sp, k)
     info = gpu.mesh_info(mesh)
@@ -205,7 +215,7 @@ def test_square_patch_assembly_matches_oracle(gpu, orc, fk):
         assert np.allclose(r["B"], B, rtol=RTOL, atol=1e-12)
 
 
-def test_circle_assembly_matches_oracle(gpu, orc, fk):
+def test_circle_assembly_matches_oracle(gpu, orc, fk, launch):
     m, arcs = _golden_arcs("unit3")
     mesh = gpu.mesh_circles((0, 0, 1, 1), 3, 1.2, 0.121, 20)
     b = gpu.register_bvp(fk.FRANKE)
