@@ -306,12 +306,13 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes, warp_mode);
   const int grid = std::max(1, ctx->num_sms * occ);
   // Chunk size.  Slots: at least 4 chunks per CTA of the persistent grid, at
-  // most 32768 paths.  Warp mode: about 6 chunks per warp (the last round of
-  // chunks leaves warps idle), 64..4096 paths.  An item is split into equal
-  // chunks (no small remainder).
+  // most 32768 paths.  Warp mode: about 2 chunks per warp, 64..4096 paths
+  // (measured on the 8x8 assembly and on point solves, finer chunks cost
+  // more in per-chunk work than they save in the last round).  An item is
+  // split into equal chunks (no small remainder).
   long long chunk = ctx->chunk;
   if (chunk <= 0 && warp_mode) {
-    chunk = total_paths / (6LL * grid * (block / 32));
+    chunk = total_paths / (2LL * grid * (block / 32));
     chunk = std::max<long long>(64, std::min<long long>(chunk, 4096));
   } else if (chunk <= 0) {
     chunk = total_paths / (4LL * grid);

@@ -10,7 +10,8 @@
 // CTA-wide barrier between chunks, so the tail of one chunk overlaps the
 // next.  The last warp to leave a chunk flushes the chunk's stencil moments
 // into the item's FP64 accumulators and refills the slot from the global
-// chunk queue.
+// chunk queue.  Items of few paths run in warp mode instead: each warp takes
+// its own chunks and adds the moments to global memory (see paths_kernel).
 //
 // An exiting lane only pushes its exit (X_tau, Y, Z, xi, steps, flags) onto
 // its warp's shared-memory queue and starts the next path; once 32 exits are
@@ -79,6 +80,20 @@ __device__ __forceinline__ double warp_reduce(const AccK& a, int lane) {
     c = c + c2 + e;
   }
   return lane == 0 ? static_cast<double>(s) + static_cast<double>(c) : 0.0;
+}
+
+// FP32 -> FP64 by bit manipulation on the integer pipes (the F2F conversion
+// runs on the FP64 pipe, a 64th of the FP32 rate on this part).  Exact for
+// normal numbers and infinities; subnormal inputs (below 1.2e-38, far under
+// any stencil weight that is added) become zero.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u) return (u & 0x80000000u) ? -0.0 : 0.0;
+  const unsigned e64 = (e == 0xffu) ? 0x7ffu : e + 896u;
+  const unsigned hi = (u & 0x80000000u) | (e64 << 20) | ((u & 0x7fffffu) >> 3);
+  const unsigned lo = (u & 0x7u) << 29;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
 template <typename R, int ST>
@@ -416,7 +431,13 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
             if (idx >= m) idx -= m;
             const R dx = ex - snx[idx], dy = ey - sny[idx];
             const R arg = e2 * (dx * dx + dy * dy);
-            if (arg < R(kPhiCut)) atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(Yv * fexp(-arg)));
+            if (arg < R(kPhiCut)) {
+              const R wv = Yv * fexp(-arg);
+              if constexpr (WM && std::is_same<R, float>::value)
+                atomicAdd(&sacc[L * kk + j], f32_to_f64(wv));  // the item's FP64 accumulator in global memory
+              else
+                atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(wv));
+            }
             if (++j == kk) j = 0;
           }
         }
