@@ -390,8 +390,8 @@ def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
     return res
 
 
-def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=1000, pilot_h=5e-4, train_steps=1000,
-                   table=512, lr=3e-2, batch=4096):
+def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=500, pilot_h=5e-4, train_steps=1000,
+                   table=128, lr=3e-2, batch=4096):
     """Time to `target` RMS node error on the assembly, plain FK vs the learned
     control variate (both FP32 stepping, same h).
 

@@ -354,6 +354,16 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
     const R s0 = R(itg.sub[0]), s1 = R(itg.sub[1]), s2 = R(itg.sub[2]), s3 = R(itg.sub[3]);
     const bool has_sub = (ST != 0) || itg.sub_shape >= 0;
     const bool sub_circle = (ST == 1) || (ST == 0 && itg.sub_shape == 1);
+    // A subdomain strictly inside the rectangular domain is always nearer (in
+    // Dentro's signed distance) than the domain boundary, wherever the path
+    // is, so the domain distance cannot decide an exit and is not evaluated.
+    bool dom_can_win = true;
+    if (has_sub && PROB != 3) {
+      if (sub_circle)  // (r, cx, cy)
+        dom_can_win = !(s1 - s0 > d0 && s1 + s0 < d2 && s2 - s0 > d1 && s2 + s0 < d3);
+      else             // (x0, y0, x1, y1)
+        dom_can_win = !(s0 > d0 && s1 > d1 && s2 < d2 && s3 < d3);
+    }
     const R st0 = Problem<PROB>::template state<R>(bvp, x0, y0);  // sigma state at the start point
     const uint32_t item = static_cast<uint32_t>(ch.item);
     // learned control variate: grad u_hat table of this item's region
@@ -507,10 +517,16 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         y += co.by * h + co.s * dWy;
         ++k;
         // ---- exit rule (Dentro, FeynmanKacSolver.cpp:68-106)
-        Bnd<R> w = (PROB == 3) ? circle_dist<R>(x, y, d0, d1, d2) : rect_dist<R>(x, y, d0, d1, d2, d3);
-        if (has_sub) {
-          const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
-          if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
+        Bnd<R> w;
+        if (dom_can_win) {
+          w = (PROB == 3) ? circle_dist<R>(x, y, d0, d1, d2) : rect_dist<R>(x, y, d0, d1, d2, d3);
+          if (has_sub) {
+            const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
+            if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
+          }
+        } else {
+          w = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
+          dom_wins = false;
         }
         // sigma at the new point (kept for the next step) or at the
         // projection: one evaluation at the selected point, no divergence
