@@ -9,7 +9,8 @@
 //                   input gradient du_hat/dx (value + gradient at points).
 //  mlp_adam_kernel  sums the per-CTA gradient partials in a fixed order,
 //                   Adam update of the FP32 master weights, refresh of the
-//                   BF16 copies (row-major and transposed) used by the GEMMs.
+//                   BF16 copies used by the GEMMs (the backward products read
+//                   weights and activations transposed with ldmatrix.trans).
 //  mlp_train_kernel all training steps in one cooperative launch (pass,
 //                   grid barrier, Adam on each CTA's slice, grid barrier).
 //  mlp_table        grad u_hat on a grid per region (the inference pass),
@@ -60,12 +61,11 @@ constexpr int kDwNT = 4;
 constexpr int kDwCols = 8 * kDwNT;
 static_assert(kThreads / 32 == (W / 16) * (W / kDwCols), "weight-gradient tiling");
 constexpr int LD = 72;          // bf16 leading dimension of [rows][64] tiles (144 B rows)
-constexpr int LDT = kRows + 8;  // bf16 leading dimension of [64][rows] transposed tiles (16 B multiple)
 static_assert(kMT == 1 && kWarpRows % 16 == 0, "rows per warp");
 static_assert(kThreads / 32 == kRowGroups * (W / kColsPerWarp), "warp tiling");
 constexpr int OFF_W1 = 0, OFF_B1 = 128, OFF_W2 = 192, OFF_B2 = OFF_W2 + W * W, OFF_W3 = OFF_B2 + W,
               OFF_B3 = OFF_W3 + W * W, OFF_W4 = OFF_B3 + W, OFF_B4 = OFF_W4 + W, NPARAM = OFF_B4 + 1;
-constexpr int BF_PER_REGION = 4 * W * W;  // W2, W2^T, W3, W3^T
+constexpr int BF_PER_REGION = 2 * W * W;  // W2, W3 (the backward reads them transposed with ldmatrix.trans)
 
 enum { MODE_TRAIN = 0, MODE_LOSSGRAD = 1, MODE_GRADX = 2 };
 
@@ -86,7 +86,7 @@ __device__ __forceinline__ float silu_f(float z, float& dsilu) {
 struct PassArgs {
   int mode, n_regions, ctas_per_region, rows_per_cta;
   const float* params;          // [R][NPARAM]
-  const __nv_bfloat16* wbf;     // [R][4][W*W]
+  const __nv_bfloat16* wbf;     // [R][2][W*W]: W2, W3
   const float4* norm;           // per region: (lo_x, lo_y, scale_x, scale_y)
   // samples (TRAIN / LOSSGRAD): region r owns [sample_off[r], sample_off[r+1])
   const float4* samples;        // (x, y, target, -)
@@ -103,12 +103,11 @@ struct PassArgs {
 };
 
 struct Smem {
-  __nv_bfloat16 w2[W * LD], w2t[W * LD], w3[W * LD], w3t[W * LD];
+  __nv_bfloat16 w2[W * LD], w3[W * LD];
   __nv_bfloat16 h1[kRows * LD], h2[kRows * LD], s1[kRows * LD], s2[kRows * LD];
   // h3 and s3 are adjacent: after the layer-3 backward they hold dp1 in FP32
   __nv_bfloat16 h3[kRows * LD], s3[kRows * LD];
-  __nv_bfloat16 h1t[W * LDT], h2t[W * LDT];
-  __nv_bfloat16 dp[kRows * LD], dpt[W * LDT];
+  __nv_bfloat16 dp[kRows * LD];
   float w1[2 * W], b1[W], b2[W], b3[W], w4[W], b4;
   float z[kRows][2], tgt[kRows], dO[kRows], o[kRows];
   float o_part[kColGroups][kRows];   // output-unit partial sums of the column groups
@@ -130,9 +129,7 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
     const int r = (e8 * 8) / W, c = (e8 * 8) % W;
     const uint4* src = reinterpret_cast<const uint4*>(WB) + e8;
     *reinterpret_cast<uint4*>(&S.w2[r * LD + c]) = __ldcg(src);
-    *reinterpret_cast<uint4*>(&S.w2t[r * LD + c]) = __ldcg(src + W * W / 8);
-    *reinterpret_cast<uint4*>(&S.w3[r * LD + c]) = __ldcg(src + 2 * W * W / 8);
-    *reinterpret_cast<uint4*>(&S.w3t[r * LD + c]) = __ldcg(src + 3 * W * W / 8);
+    *reinterpret_cast<uint4*>(&S.w3[r * LD + c]) = __ldcg(src + W * W / 8);
   }
   for (int e = tid; e < 2 * W; e += kThreads) S.w1[e] = __ldcg(P + OFF_W1 + e);
   for (int e = tid; e < W; e += kThreads) {
@@ -213,7 +210,6 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
       const float hv = silu_f(p, ds);
       S.h1[r * LD + j] = __float2bfloat16_rn(hv);
       S.s1[r * LD + j] = __float2bfloat16_rn(ds);
-      if (train) S.h1t[j * LDT + r] = __float2bfloat16_rn(hv);
     }
     __syncthreads();
     // ---- layers 2 and 3 on the tensor cores, one (16-row, 32-column) tile per warp
@@ -244,7 +240,6 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
             const float hv = silu_f(c[mt][nt][q] + bias[col], ds);
             Hout[r * LD + col] = __float2bfloat16_rn(hv);
             Sout[r * LD + col] = __float2bfloat16_rn(ds);
-            if (layer == 0 && train) S.h2t[col * LDT + r] = __float2bfloat16_rn(hv);
             if (layer == 1) orow[mt][q >> 1] += S.w4[col] * hv;
           }
       if (layer == 1) {
@@ -283,12 +278,12 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
       const int r = e >> 6, j = e & (W - 1);
       const __nv_bfloat16 vb = __float2bfloat16_rn(S.dO[r] * S.w4[j] * __bfloat162float(S.s3[r * LD + j]));
       S.dp[r * LD + j] = vb;
-      if (train) S.dpt[j * LDT + r] = vb;
     }
     __syncthreads();
     // layer-3 backward: dW3 += dp3^T h2, db3, dW4, db4; dh2 = dp3 W3
     if (train) {
-      warp_gemm_tn<1, kDwNT, kRows>(cW3, S.dpt, LDT, mw, S.h2t, LDT, nw, lane);
+      // dW3[out][in] = sum_r dp[r][out] h2[r][in]: both operands read transposed
+      warp_gemm<1, kDwNT, kRows, true, true>(cW3, S.dp, LD, mw, S.h2, LD, nw, lane);
       for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) {
         gW4 += S.dO[r] * __bfloat162float(S.h3[r * LD + cj]);
         gB3 += __bfloat162float(S.dp[r * LD + cj]);
@@ -303,8 +298,9 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
         for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<kMT, kNT, W>(c, S.dp, LD, m0, S.w3t, LD, n0, lane);
-      __syncthreads();  // everyone is done reading dp / dpt of layer 3
+      // dh2[r][in] = sum_out dp[r][out] W3[out][in]: W3 read transposed
+      warp_gemm<kMT, kNT, W, false, true>(c, S.dp, LD, m0, S.w3, LD, n0, lane);
+      __syncthreads();  // everyone is done reading dp of layer 3
 #pragma unroll
       for (int mt = 0; mt < kMT; ++mt)
 #pragma unroll
@@ -315,13 +311,12 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
             const int col = n0 + nt * 8 + 2 * t4 + (q & 1);
             const __nv_bfloat16 vb = __float2bfloat16_rn(c[mt][nt][q] * __bfloat162float(S.s2[r * LD + col]));
             S.dp[r * LD + col] = vb;
-            if (train) S.dpt[col * LDT + r] = vb;
           }
     }
     __syncthreads();
     // layer-2 backward: dW2 += dp2^T h1, db2; dh1 = dp2 W2
     if (train) {
-      warp_gemm_tn<1, kDwNT, kRows>(cW2, S.dpt, LDT, mw, S.h1t, LDT, nw, lane);
+      warp_gemm<1, kDwNT, kRows, true, true>(cW2, S.dp, LD, mw, S.h1, LD, nw, lane);
       for (int r = cq * kQRows; r < (cq + 1) * kQRows; ++r) gB2 += __bfloat162float(S.dp[r * LD + cj]);
     }
     {
@@ -332,7 +327,7 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
         for (int nt = 0; nt < kNT; ++nt)
 #pragma unroll
           for (int q = 0; q < 4; ++q) c[mt][nt][q] = 0.f;
-      warp_gemm_tn<kMT, kNT, W>(c, S.dp, LD, m0, S.w2t, LD, n0, lane);
+      warp_gemm<kMT, kNT, W, false, true>(c, S.dp, LD, m0, S.w2, LD, n0, lane);
       __syncthreads();
       // dp1 = dh1 * silu'(p1), kept in FP32 in the (now free) h3 / s3 area as pairs
       static_assert(sizeof(float) * kRows * W <= 2 * sizeof(__nv_bfloat16) * kRows * LD, "dp1 overlay");
@@ -445,15 +440,10 @@ __device__ __forceinline__ void adam_apply_vals(long long e, int r, int p, float
   params[e] = th;
   __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
   const __nv_bfloat16 tb = __float2bfloat16_rn(th);
-  if (p >= OFF_W2 && p < OFF_W2 + W * W) {
-    const int q = p - OFF_W2, o = q / W, i = q % W;
-    B[q] = tb;
-    B[W * W + i * W + o] = tb;
-  } else if (p >= OFF_W3 && p < OFF_W3 + W * W) {
-    const int q = p - OFF_W3, o = q / W, i = q % W;
-    B[2 * W * W + q] = tb;
-    B[3 * W * W + i * W + o] = tb;
-  }
+  if (p >= OFF_W2 && p < OFF_W2 + W * W)
+    B[p - OFF_W2] = tb;
+  else if (p >= OFF_W3 && p < OFF_W3 + W * W)
+    B[W * W + (p - OFF_W3)] = tb;
 }
 __device__ __forceinline__ void adam_apply(long long e, int r, int p, float gsum, float* params, __nv_bfloat16* wbf,
                                            float* m, float* v, float lr, float b1, float b2, float eps, float bc1,
@@ -642,13 +632,11 @@ __global__ void mlp_refresh_bf16(const float* params, __nv_bfloat16* wbf, int n_
   const long long total = static_cast<long long>(n_regions) * W * W;
   for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
        e += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const int r = static_cast<int>(e / (W * W)), q = static_cast<int>(e % (W * W)), o = q / W, i = q % W;
+    const int r = static_cast<int>(e / (W * W)), q = static_cast<int>(e % (W * W));
     const float* P = params + static_cast<long long>(r) * NPARAM;
     __nv_bfloat16* B = wbf + static_cast<long long>(r) * BF_PER_REGION;
     B[q] = __float2bfloat16_rn(P[OFF_W2 + q]);
-    B[W * W + i * W + o] = __float2bfloat16_rn(P[OFF_W2 + q]);
-    B[2 * W * W + q] = __float2bfloat16_rn(P[OFF_W3 + q]);
-    B[3 * W * W + i * W + o] = __float2bfloat16_rn(P[OFF_W3 + q]);
+    B[W * W + q] = __float2bfloat16_rn(P[OFF_W3 + q]);
   }
 }
 

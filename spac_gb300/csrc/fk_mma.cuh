@@ -18,6 +18,14 @@ __device__ __forceinline__ void ldsm_x4(uint32_t r[4], const void* p) {
                : "r"(smem_u32(p)));
 }
 
+// The same four 8x8 tiles, transposed on the way in: each lane supplies the
+// address of a row of the stored (transposed) tile.
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t r[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+
 __device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -31,25 +39,44 @@ __device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], 
 // shared memory with leading dimensions lda / ldb (elements, rows 16-byte
 // aligned).  c[mt][nt][4] is the m16n8 accumulator layout: thread (g =
 // lane/4, t = lane%4) holds rows g and g+8, columns 2t and 2t+1.
-template <int MT, int NT, int K>
-__device__ __forceinline__ void warp_gemm_tn(float (&c)[MT][NT][4], const __nv_bfloat16* A, int lda, int m0,
-                                             const __nv_bfloat16* B, int ldb, int n0, int lane) {
+//
+// AT / BT select the stored layout of each operand: false = K-contiguous
+// (A[m][k], B[n][k]), true = the transpose (A stored as [k][m], B as [k][n]),
+// loaded with ldmatrix.trans so that no transposed copy is ever written.
+template <int MT, int NT, int K, bool AT = false, bool BT = false>
+__device__ __forceinline__ void warp_gemm(float (&c)[MT][NT][4], const __nv_bfloat16* A, int lda, int m0,
+                                          const __nv_bfloat16* B, int ldb, int n0, int lane) {
   static_assert(NT % 2 == 0, "pairs of n8 tiles");
+  const int i = lane >> 3, r8 = lane & 7;  // tile of the x4 load this lane addresses, row within it
 #pragma unroll
   for (int k0 = 0; k0 < K; k0 += 16) {
     uint32_t a[MT][4];
 #pragma unroll
     for (int mt = 0; mt < MT; ++mt) {
-      const int r = m0 + mt * 16 + (lane & 15);
-      const int col = k0 + ((lane >> 4) << 3);
-      ldsm_x4(a[mt], A + r * lda + col);
+      if (AT) {
+        // tiles (m 0-7, k 0-7), (m 8-15, k 0-7), (m 0-7, k 8-15), (m 8-15, k 8-15)
+        const int krow = k0 + r8 + ((i >> 1) << 3);
+        const int mcol = m0 + mt * 16 + ((i & 1) << 3);
+        ldsm_x4_trans(a[mt], A + krow * lda + mcol);
+      } else {
+        const int r = m0 + mt * 16 + (lane & 15);
+        const int col = k0 + ((lane >> 4) << 3);
+        ldsm_x4(a[mt], A + r * lda + col);
+      }
     }
 #pragma unroll
     for (int np = 0; np < NT / 2; ++np) {
       uint32_t b[4];
-      const int n = n0 + np * 16 + (lane & 7) + ((lane >> 4) << 3);
-      const int col = k0 + (((lane >> 3) & 1) << 3);
-      ldsm_x4(b, B + n * ldb + col);
+      if (BT) {
+        // tiles (n 0-7, k 0-7), (n 0-7, k 8-15), (n 8-15, k 0-7), (n 8-15, k 8-15)
+        const int krow = k0 + r8 + ((i & 1) << 3);
+        const int ncol = n0 + np * 16 + ((i >> 1) << 3);
+        ldsm_x4_trans(b, B + krow * ldb + ncol);
+      } else {
+        const int n = n0 + np * 16 + (lane & 7) + ((lane >> 4) << 3);
+        const int col = k0 + (((lane >> 3) & 1) << 3);
+        ldsm_x4(b, B + n * ldb + col);
+      }
 #pragma unroll
       for (int mt = 0; mt < MT; ++mt) {
         mma_bf16_16816(c[mt][2 * np], a[mt], b[0], b[1]);
@@ -57,6 +84,11 @@ __device__ __forceinline__ void warp_gemm_tn(float (&c)[MT][NT][4], const __nv_b
       }
     }
   }
+}
+template <int MT, int NT, int K>
+__device__ __forceinline__ void warp_gemm_tn(float (&c)[MT][NT][4], const __nv_bfloat16* A, int lda, int m0,
+                                             const __nv_bfloat16* B, int ldb, int n0, int lane) {
+  warp_gemm<MT, NT, K, false, false>(c, A, lda, m0, B, ldb, n0, lane);
 }
 
 }  // namespace fk
