@@ -239,6 +239,13 @@ void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
   p.k = k;
   p.closed = M.closed ? 1 : 0;
   p.nwin = p.closed ? p.m : p.m - k + 1;
+  // Along the chain, the distance from an exit point (projected onto a side)
+  // grows monotonically over its own side and the two adjacent ones; nodes of
+  // the opposite side lie at least the patch width W away.  When those are
+  // always beyond the weight cutoff, a walk outward from the exit may stop
+  // at its first cut node (0.9 W leaves a margin for rounding).
+  const double W = 0.9 * std::min(M.rect[2] - M.rect[0], M.rect[3] - M.rect[1]);
+  p.walk = (p.eps2 * W * W >= static_cast<double>(fk::kPhiCut)) ? 1 : 0;
   p.node_off = static_cast<long long>(S.patch_nodes.size());
   p.ainv_off = S.ainv_total;
   S.ainv_total += static_cast<long long>(p.nwin) * k * k;

@@ -39,6 +39,7 @@ struct PatchDev {
   double rect[4];
   double eps2;
   int m, k, closed, nwin;
+  int walk;             // 1: the stencil walk may stop at its first cut node
   long long node_off;   // 2*m doubles (x, y) in chain order
   long long ainv_off;   // nwin * k * k doubles, column-major per window
   // sides: chain index of the first node, node count, axis (0: node x varies),
@@ -60,6 +61,9 @@ enum { kStatScore = 0, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScor
 // node coordinates in the stepping precision, or arc angles in FP64), each
 // part padded to 16 bytes.
 constexpr int kSlotsFP32 = 3;
+
+// Gaussian stencil weights exp(-arg) with arg >= kPhiCut (< 1e-30) are not added.
+constexpr float kPhiCut = 69.0f;
 __host__ __device__ inline int paths_slots(int precision) { return precision == 0 ? 2 : kSlotsFP32; }
 __host__ __device__ inline size_t paths_slot_acc_bytes(int precision, int stencil_kind, int acc_words) {
   const size_t w = (precision == 0 || stencil_kind == 1) ? 8 : 4;

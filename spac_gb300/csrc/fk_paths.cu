@@ -40,7 +40,6 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kNumAcc = 8;   // floating-point sums per thread
-constexpr float kPhiCut = 69.0f;  // Gaussian stencil weights exp(-arg) with arg >= 69 (< 1e-30) are not added
 
 struct AccD {
   double s = 0.0;
@@ -113,7 +112,7 @@ struct ExitQueue {
 // Per-chunk copy of the exit patch in shared memory (stepping precision).
 template <typename R>
 struct PatchSh {
-  int m, k, closed;
+  int m, k, closed, walk;
   int side_first[4], side_count[4], side_axis[4];
   R side_fixed[4], side_start[4], side_inv_step[4];
   R e2;
@@ -185,6 +184,7 @@ __device__ void stage_stencil(const LaunchArgs& a, SlotSh<R>& sl, unsigned char*
       sl.sp.m = P.m;
       sl.sp.k = P.k;
       sl.sp.closed = P.closed;
+      sl.sp.walk = P.walk;
       sl.sp.e2 = R(P.eps2);
     }
   }
@@ -232,7 +232,7 @@ __device__ void fill_slot(const LaunchArgs& a, SlotSh<R>& sl, unsigned char* mem
 // neighbour is closer than the opposite end of the run.
 template <typename R>
 __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restrict__ nx, const R* __restrict__ ny,
-                                          R ex, R ey) {
+                                          R ex, R ey, int& nearest_out) {
   int best_s = -1;
   R best = R(FLT_MAX);
 #pragma unroll
@@ -266,6 +266,7 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
     while (L > 0 && d2(L - 1) < d2(L + k - 1)) --L;
     while (L < m - k && d2(L + k) < d2(L)) ++L;
   }
+  nearest_out = nearest;
   return L;
 }
 
@@ -427,28 +428,40 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
       }
       if (ST == 2) {
         if (sub_exit) {
-          // Gaussian k-nearest moments t_W[j] += Y phi_j, one exit per lane;
-          // each lane starts at its own j so that lanes sharing a window add
-          // to different words
-          const int L = knn_window<R>(sp, snx, sny, ex, ey);
+          // Gaussian k-nearest moments t_W[j] += Y phi_j, one exit per lane
+          int nearest;
+          const int L = knn_window<R>(sp, snx, sny, ex, ey, nearest);
           const int kk = sp.k, m = sp.m;
           const R e2 = sp.e2;
-          // weights below exp(-kPhiCut) ~ 1e-30 are skipped (they are 0 or
-          // denormal in FP32 and far below any tolerance in FP64)
-          int j = lane % kk;
-          for (int jj = 0; jj < kk; ++jj) {
+          // Weights below exp(-kPhiCut) ~ 1e-30 are not added (they are 0 or
+          // denormal in FP32 and far below any tolerance in FP64).  The exit
+          // point lies on the patch boundary next to the window's node
+          // `nearest`; walking the window away from it (down from it, up from
+          // the next node) the distances grow until the opposite side, which
+          // lies beyond the cutoff on patches marked `walk`: each walk then
+          // stops at its first cut node, once past the nodes around the exit.
+          int jn = nearest - L;
+          if (jn < 0) jn += m;
+          auto add = [&](int j) -> bool {
             int idx = L + j;
             if (idx >= m) idx -= m;
             const R dx = ex - snx[idx], dy = ey - sny[idx];
             const R arg = e2 * (dx * dx + dy * dy);
-            if (arg < R(kPhiCut)) {
-              const R wv = Yv * fexp(-arg);
-              if constexpr (WM && std::is_same<R, float>::value)
-                atomicAdd(&sacc[L * kk + j], f32_to_f64(wv));  // the item's FP64 accumulator in global memory
-              else
-                atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(wv));
-            }
-            if (++j == kk) j = 0;
+            if (!(arg < R(kPhiCut))) return false;
+            const R wv = Yv * fexp(-arg);
+            if constexpr (WM && std::is_same<R, float>::value)
+              atomicAdd(&sacc[L * kk + j], f32_to_f64(wv));  // the item's FP64 accumulator in global memory
+            else
+              atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(wv));
+            return true;
+          };
+          if (sp.walk && jn < kk) {
+            for (int j = jn; j >= 0; --j)
+              if (!add(j) && j < jn - 1) break;
+            for (int j = jn + 1; j < kk; ++j)
+              if (!add(j) && j > jn + 1) break;
+          } else {
+            for (int j = 0; j < kk; ++j) add(j);
           }
         }
       } else if (ST == 1) {

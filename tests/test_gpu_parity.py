@@ -196,8 +196,12 @@ def _patch_rect(gpu, mesh, s):
     return gpu._rects[s]
 
 
-def test_square_patch_assembly_matches_oracle(gpu, orc, fk, launch):
-    n_sub, nps, e, eps_sp, k = 3, 9, 0.25, 1.0, 6
+# eps * spacing = 3 puts the opposite side of a patch beyond the weight cutoff,
+# so the kernel walks each window outward from the exit and stops early;
+# eps * spacing = 1 scans whole windows.
+@pytest.mark.parametrize("eps_sp", [1.0, 3.0])
+def test_square_patch_assembly_matches_oracle(gpu, orc, fk, launch, eps_sp):
+    n_sub, nps, e, k = 3, 9, 0.25, 6
     mesh = gpu.mesh_square_patches((0, 0, 1, 1), n_sub, nps, e, eps_sp, k)
     info = gpu.mesh_info(mesh)
     H = 1.0 / n_sub
