@@ -533,6 +533,160 @@ double mlp_grad(const orc_mlp* m, double x, double y, double g[2], double* val) 
   return o;
 }
 
+// ------------------------------------------------- pseudospectral disk -----
+// Dense collocation operator of PseudoespectralCirculoSolver::Inicializa
+// (Solvers/PseudoespectralCirculoSolver.cpp:2-189): Laplacian in polar
+// coordinates on Nc equispaced angles x (N2+1) Chebyshev radii (half of the
+// N_radio+1 points of a diameter, Trefethen's cheb.m), plus c(x) on the
+// diagonal, the Nc rows of the outer ring replaced by identity rows.  Row and
+// column index j*Nc + l: radius j, angle l.
+struct PsDisk {
+  int nc, nr, n2, n;
+  double radius, theta0;
+  std::vector<double> r, theta, L;  // L: n x n row-major
+};
+
+void ps_build(const orc_bvp* B, double cx, double cy, double radius, int nc, int nr, double theta0, PsDisk& P) {
+  const int np = nr + 1;
+  P.nc = nc; P.nr = nr; P.n2 = (nr - 1) / 2; P.radius = radius; P.theta0 = theta0;
+  P.r.resize(np);
+  std::vector<int> cw(np);
+  for (int i = 0; i < np; ++i) {
+    P.r[i] = radius * std::cos(M_PI * i / nr);
+    cw[i] = static_cast<int>(((i == 0 || i == nr) ? 2 : 1) * std::pow(-1, i));
+  }
+  // cheb.m: D_ij = (c_i / c_j) / (r_i - r_j), diagonal = 1 - row sum (incl. its own 1)
+  std::vector<double> D(static_cast<size_t>(np) * np);
+  for (int i = 0; i < np; ++i) {
+    for (int j = 0; j < np; ++j) {
+      const double cij = cw[i] * (1.0 / cw[j]);
+      D[i * np + j] = cij / ((P.r[i] - P.r[j]) + (i == j ? 1.0 : 0.0));
+    }
+    double s = 0.0;
+    for (int j = 0; j < np; ++j) s += D[i * np + j];
+    D[i * np + i] = D[i * np + i] - s;
+  }
+  std::vector<double> DD(static_cast<size_t>(np) * np);
+  for (int i = 0; i < np; ++i)
+    for (int j = 0; j < np; ++j) {
+      double s = D[i * np] * D[j];
+      for (int k = 1; k < np; ++k) s += D[i * np + k] * D[k * np + j];
+      DD[i * np + j] = s;
+    }
+  const int m = P.n2 + 1, M2 = nc / 2;
+  // radial blocks: A1 = D1 + R E1 (same radius), A2 = D2 + R E2 (mirrored radius), 1/r^2
+  std::vector<double> A1(m * m), A2(m * m), rinv(m), r2inv(m);
+  for (int i = 0; i < m; ++i) {
+    rinv[i] = 1.0 / P.r[i];
+    r2inv[i] = rinv[i] * rinv[i];
+  }
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) {
+      A1[i * m + j] = DD[i * np + j] + rinv[i] * D[i * np + j];
+      A2[i * m + j] = DD[i * np + (nr - j)] + rinv[i] * D[i * np + (nr - j)];
+    }
+  // periodic second-derivative matrix (Toeplitz): D2t(l, l') = a((l' - l) mod Nc)
+  const double dt = 2 * M_PI / nc;
+  std::vector<double> a(nc);
+  P.theta.resize(nc);
+  for (int l = 0; l < nc; ++l) {
+    P.theta[l] = l * dt + theta0;
+    a[l] = (l == 0) ? -(M_PI * M_PI / (3 * dt * dt)) - (1.0 / 6)
+                    : 0.5 * std::pow(-1, l + 1) / std::pow(std::sin(dt * l * 0.5), 2);
+  }
+  P.n = m * nc;
+  const int n = P.n;
+  P.L.assign(static_cast<size_t>(n) * n, 0.0);
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j)
+      for (int l = 0; l < nc; ++l)
+        for (int lp = 0; lp < nc; ++lp) {
+          const double e1 = (l == lp) ? A1[i * m + j] : 0.0;
+          const double e2 = (lp == (l + M2) % nc) ? A2[i * m + j] : 0.0;
+          const double e3 = (i == j ? r2inv[i] : 0.0) * a[((lp - l) % nc + nc) % nc];
+          P.L[static_cast<size_t>(i * nc + l) * n + (j * nc + lp)] = (e1 + e2) + e3;
+        }
+  for (int j = 0; j < m; ++j)
+    for (int l = 0; l < nc; ++l) {
+      const double x = P.r[j] * std::cos(P.theta[l]) + cx, y = P.r[j] * std::sin(P.theta[l]) + cy;
+      const size_t d = static_cast<size_t>(j * nc + l);
+      P.L[d * n + d] += coefficients(B, x, y).c;
+    }
+  for (int l = 0; l < nc; ++l) {
+    for (int k = 0; k < n; ++k) P.L[static_cast<size_t>(l) * n + k] = 0.0;
+    P.L[static_cast<size_t>(l) * n + l] = 1.0;
+  }
+}
+
+// Gaussian elimination with partial pivoting on A (n x n row-major, copied)
+// for the columns of X (n x nrhs row-major), solved in place.
+void ps_solve(int n, std::vector<double> A, int nrhs, std::vector<double>& X) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(A[static_cast<size_t>(i) * n + k]) > std::fabs(A[static_cast<size_t>(p) * n + k])) p = i;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) std::swap(A[static_cast<size_t>(k) * n + j], A[static_cast<size_t>(p) * n + j]);
+      for (int j = 0; j < nrhs; ++j) std::swap(X[static_cast<size_t>(k) * nrhs + j], X[static_cast<size_t>(p) * nrhs + j]);
+    }
+    const double piv = A[static_cast<size_t>(k) * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      const double f = A[static_cast<size_t>(i) * n + k] / piv;
+      if (f == 0.0) continue;
+      for (int j = k; j < n; ++j) A[static_cast<size_t>(i) * n + j] -= f * A[static_cast<size_t>(k) * n + j];
+      for (int j = 0; j < nrhs; ++j) X[static_cast<size_t>(i) * nrhs + j] -= f * X[static_cast<size_t>(k) * nrhs + j];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k)
+    for (int j = 0; j < nrhs; ++j) {
+      double s = X[static_cast<size_t>(k) * nrhs + j];
+      for (int q = k + 1; q < n; ++q) s -= A[static_cast<size_t>(k) * n + q] * X[static_cast<size_t>(q) * nrhs + j];
+      X[static_cast<size_t>(k) * nrhs + j] = s / A[static_cast<size_t>(k) * n + k];
+    }
+}
+
+// Interpolador_PS::Interpola (BVP/Interpolador_PS.cpp:34-61) of the grid
+// values z (index j*Nc + l): Fourier interpolation in the angle along the
+// diameter through the point (the opposite half through cos(k pi)), then
+// barycentric interpolation in the radius with the weights of
+// Interpolador_PS::Inicializa (:18-33) on the Chebyshev diameter.
+double ps_interpola(const PsDisk& P, const double* z, int zstride, double cx, double cy, double px, double py) {
+  const int N = P.nc, n = N / 2, half = P.n2 + 1, m = 2 * half;
+  const double dx = px - cx, dy = py - cy;
+  const double rp = std::sqrt(dx * dx + dy * dy) / P.radius;
+  double tp = std::atan2(dy, dx);
+  tp = (tp >= 0) ? tp : tp + 2.0 * M_PI;
+  std::vector<double> head(half, 0.0), tail(half, 0.0);
+  for (int l = 0; l < N; ++l)
+    for (int k = -n; k < n; ++k) {
+      const double ck = std::cos(k * (tp - P.theta[l]));
+      const double sk = std::cos(k * M_PI);
+      for (int j = 0; j < half; ++j) {
+        const double v = ck * z[static_cast<size_t>(j * N + l) * zstride];
+        head[j] = head[j] + v;
+        tail[j] = tail[j] + sk * v;
+      }
+    }
+  // u = normN * reverse(head, reverse(tail)): u_i = tail_i (i < half), head_{m-1-i}
+  const double normN = 1.0 / N;
+  std::vector<double> u(m), diam(m), c(m);
+  for (int i = 0; i < half; ++i) {
+    u[i] = normN * tail[i];
+    u[m - 1 - i] = normN * head[i];
+    diam[i] = -P.r[i] / P.radius;
+    diam[m - 1 - i] = P.r[i] / P.radius;
+  }
+  const double its = -1.0 + 1.0 / m;
+  for (int i = 0; i < m; ++i) c[i] = std::pow(-1, i) * std::sin(M_PI * (its + (2.0 / m) * i + 1) / 2);
+  double num = 0, den = 0;
+  for (int i = 0; i < m; ++i) {
+    const double t = c[i] / (rp - diam[i]);
+    num = num + t * u[i];
+    den = den + t;
+  }
+  return num / den;
+}
+
 }  // namespace
 
 extern "C" {
@@ -756,6 +910,39 @@ int orc_actualiza_gb(int row, int nG, const int* cols, const double* G, double b
     if (colidx[j] == cols[0]) break;
   if (j == rowptr[row + 1]) return -1;
   for (int a = 0; a < nG; ++a) val[j + a] += G[a];
+  return 0;
+}
+
+int orc_ps_disk(const orc_bvp* b, double cx, double cy, double radius, int n_circle, int n_radial, double theta0,
+                int n_periph, const double* periph_theta, int n_inner, const double* inner_xy, double* G,
+                double* Bv) {
+  // PseudoespectralCirculoSolver::Inicializa + Resuelve(BVP, nudos_interior,
+  // nudos_periferia) (Solvers/PseudoespectralCirculoSolver.cpp:2-189, :215-260)
+  if (n_circle < 2 || n_circle % 2 || n_radial < 3 || n_radial % 2 == 0) return -1;
+  PsDisk P;
+  ps_build(b, cx, cy, radius, n_circle, n_radial, theta0, P);
+  const int n = P.n, nrhs = n_periph + 1;
+  std::vector<double> X(static_cast<size_t>(n) * nrhs, 0.0);
+  for (int q = n_circle; q < n; ++q) {
+    const int j = q / n_circle, l = q % n_circle;
+    const double x = P.r[j] * std::cos(P.theta[l]) + cx, y = P.r[j] * std::sin(P.theta[l]) + cy;
+    X[static_cast<size_t>(q) * nrhs] = (-1.0) * coefficients(b, x, y).f;
+  }
+  // Cardinal_Fourier (BVP/BVP.cpp:25-29) of each periphery node on the outer ring
+  const int nh = n_periph / 2;
+  for (int i = 0; i < n_periph; ++i)
+    for (int l = 0; l < n_circle; ++l) {
+      double acc = 0.0;
+      for (int k = -nh; k < nh; ++k) acc += std::cos(k * (P.theta[l] - periph_theta[i]));
+      X[static_cast<size_t>(l) * nrhs + 1 + i] = acc / (2 * nh);
+    }
+  ps_solve(n, P.L, nrhs, X);
+  for (int p = 0; p < n_inner; ++p) {
+    const double px = inner_xy[2 * p], py = inner_xy[2 * p + 1];
+    Bv[p] = ps_interpola(P, X.data(), nrhs, cx, cy, px, py);
+    for (int i = 0; i < n_periph; ++i)
+      G[static_cast<size_t>(p) * n_periph + i] = (-1.0) * ps_interpola(P, X.data() + 1 + i, nrhs, cx, cy, px, py);
+  }
   return 0;
 }
 

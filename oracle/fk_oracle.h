@@ -112,6 +112,15 @@ int orc_knn_weights(const orc_knn* st, double x, double y, int* idx, double* w);
 int orc_actualiza_gb(int row, int nG, const int* cols, const double* G, double b, const int* rowptr,
                      const int* colidx, double* val, double* B);
 
+/* PseudoespectralCirculoSolver::Inicializa(centro, radio, n_circle, n_radial,
+ * theta0, bvp) + Resuelve(bvp, nudos_interior, nudos_periferia): n_periph
+ * periphery nodes at angles periph_theta, n_inner interior nodes at inner_xy.
+ * G (n_inner x n_periph, row-major) = nudos_interior[p].G[periphery i],
+ * B[p] = nudos_interior[p].B.  n_circle even, n_radial odd. */
+int orc_ps_disk(const orc_bvp* b, double cx, double cy, double radius, int n_circle, int n_radial, double theta0,
+                int n_periph, const double* periph_theta, int n_inner, const double* inner_xy, double* G,
+                double* B);
+
 /* --- learned control variate: MLP 2 -> W -> W -> W -> 1 with SiLU ---------- */
 typedef struct {
   int width;

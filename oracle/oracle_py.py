@@ -94,6 +94,8 @@ def load():
         L.orc_mlp_eval.argtypes = [C.POINTER(Mlp), C.c_double, C.c_double, _dp]
         L.orc_mlp_loss_grad.argtypes = [C.POINTER(Mlp), C.c_int, _dp, _dp, _dp]
         L.orc_mlp_loss_grad.restype = C.c_double
+        L.orc_ps_disk.argtypes = [C.POINTER(Bvp), C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_double,
+                                  C.c_int, _dp, C.c_int, _dp, _dp, _dp]
         _O = L
     return _O
 
@@ -195,6 +197,33 @@ def full_pivot_inverse(A):
     out = np.zeros(n * n)
     L.orc_full_pivot_inverse(n, a.ctypes.data_as(_dp), out.ctypes.data_as(_dp))
     return out.reshape((n, n), order="F")
+
+
+def ps_disk(b, cx, cy, radius, n_circle, n_radial, theta0, periph_theta, inner_xy):
+    """PseudoespectralCirculoSolver::Inicializa + Resuelve(bvp, interior, periphery):
+    returns G (n_inner x n_periph) and B (n_inner)."""
+    L = load()
+    pth = np.ascontiguousarray(periph_theta, dtype=np.float64)
+    xy = np.ascontiguousarray(inner_xy, dtype=np.float64).reshape(-1, 2)
+    G = np.zeros((len(xy), len(pth)))
+    B = np.zeros(len(xy))
+    rc = L.orc_ps_disk(C.byref(b), cx, cy, radius, n_circle, n_radial, theta0, len(pth), pth.ctypes.data_as(_dp),
+                       len(xy), xy.ctypes.data_as(_dp), G.ctypes.data_as(_dp), B.ctypes.data_as(_dp))
+    if rc != 0:
+        raise ValueError("orc_ps_disk: invalid sizes")
+    return G, B
+
+
+def actualiza_gb(row, cols, G, b, rowptr, col, val, B):
+    """SistemaLineal::Actualiza_GB(nudo) on CSR arrays (val and B updated in place);
+    cols ascending, as the keys of the node's std::map."""
+    L = load()
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    assert rowptr.dtype == np.int32 and col.dtype == np.int32 and val.flags.c_contiguous and B.flags.c_contiguous
+    return L.orc_actualiza_gb(row, len(cols), cols.ctypes.data_as(_ip), G.ctypes.data_as(_dp), b,
+                              rowptr.ctypes.data_as(_ip), col.ctypes.data_as(_ip), val.ctypes.data_as(_dp),
+                              B.ctypes.data_as(_dp))
 
 
 def rectangulo(p, x, y):

@@ -22,6 +22,7 @@
 #include "Dominios/Circulo.hpp"
 #include "Dominios/Rectangulo.hpp"
 #include "Solvers/FeynmanKacSolver.hpp"
+#include "Solvers/PseudoespectralCirculoSolver.hpp"
 #include "Mesh/Malla.hpp"
 
 // Defined in ref_harness_monegros.cpp (separate TU: the Monegros headers
@@ -137,6 +138,7 @@ struct Last {
 } g_last;
 
 std::string g_out_dir;
+int g_ps_radial = 0;  // N_radio of the pseudospectral disk solves; 0 = interior circles skipped
 
 void stats_of(const FeynmanKacSolver& s, double out[9]) {
   out[0] = s.phi;
@@ -224,11 +226,51 @@ double ref_calcula_psi(int n, const double* theta, double c2, double* iPsi) {
   return k;
 }
 
+// PseudoespectralCirculoSolver::Inicializa + Resuelve(BVP, nudos_interior,
+// nudos_periferia) (Solvers/PseudoespectralCirculoSolver.cpp:2-260) on one
+// disk: periphery nodes at angles periph_theta (global ids 0..n_periph-1),
+// interior nodes at inner_xy.  G (n_inner x n_periph, row-major) receives
+// nudos_interior[i].G[j], B[i] nudos_interior[i].B.
+int ref_ps_disk(int problem, double cx, double cy, double radius, int n_circle, int n_radial, double theta0,
+                int n_periph, const double* periph_theta, int n_inner, const double* inner_xy, double* G,
+                double* B) {
+  BVP bvp;
+  fill_bvp(bvp, problem, 0);
+  std::vector<Nudo> inner(n_inner), periph(n_periph);
+  for (int j = 0; j < n_periph; ++j) {
+    periph[j].Resetea();
+    periph[j].indice_global = j;
+    periph[j].posicion_angular = periph_theta[j];
+  }
+  for (int i = 0; i < n_inner; ++i) {
+    inner[i].Resetea();
+    inner[i].indice_global = n_periph + i;
+    inner[i].posicion_cartesiana = Eigen::Vector2d(inner_xy[2 * i], inner_xy[2 * i + 1]);
+  }
+  PseudoespectralCirculoSolver ps;
+  ps.Inicializa(Eigen::Vector2d(cx, cy), radius, n_circle, n_radial, theta0, bvp);
+  ps.Resuelve(bvp, inner, periph);
+  for (int i = 0; i < n_inner; ++i) {
+    B[i] = inner[i].B;
+    for (int j = 0; j < n_periph; ++j) {
+      auto it = inner[i].G.find(j);
+      G[static_cast<size_t>(i) * n_periph + j] = it == inner[i].G.end() ? 0.0 : it->second;
+    }
+  }
+  return 0;
+}
+
+// N_radio for the interior circles of the next ref_assemble_circles (0 =
+// interior circles skipped).
+void ref_set_ps_radial(int n_radial) { g_ps_radial = n_radial; }
+
 // Builds the reference mesh (Malla::Construye_Cuadrado, Malla.cpp:12-83) and
-// assembles G/B the way main_test_serial.cpp:54-80 does for perimeter
-// circles, with FK node solves (Solve_OMP_Analytic(nudo,...),
-// FeynmanKacSolver.cpp:344-355) and SistemaLineal::Actualiza_GB.  Interior
-// circles (pseudospectral rows in the reference) are skipped.  Nodes of full
+// assembles G/B the way main_test_serial.cpp:54-80 does: FK node solves
+// (Solve_OMP_Analytic(nudo,...), FeynmanKacSolver.cpp:344-355) for the
+// interior nodes of perimeter circles and SistemaLineal::Actualiza_GB; interior
+// circles are solved by PseudoespectralCirculoSolver when ref_set_ps_radial
+// set N_radio (Actualiza_GB(Interfaz&)), else skipped.  do_solve: 0 = mesh
+// only, 1 = both kinds of rows, 2 = pseudospectral rows only.  Nodes of full
 // circles get frontera = false explicitly (left uninitialised by Nudo()).
 int ref_assemble_circles(void* session, int problem, int use_F, const double dom[4], int Nl,
                          double superposicion, double theta0, int nodes_per_circle, double c2_corner,
@@ -288,7 +330,7 @@ int ref_assemble_circles(void* session, int problem, int use_F, const double dom
   if (do_solve) {
     int idx = 0;
     for (auto& itf : mesh.Interfaces) {
-      if (itf.es_perimeter) {
+      if (itf.es_perimeter && do_solve == 1) {
         pc[0] = itf.radio; pc[1] = itf.centro(0); pc[2] = itf.centro(1);
         bvp.frontera_subdominio.Inicializa(pc, Circulo, Stopping, Stopping);
         for (auto& nd : itf.nudos_interior) {
@@ -303,6 +345,12 @@ int ref_assemble_circles(void* session, int problem, int use_F, const double dom
           g_last.items.push_back(r);
           S.Actualiza_GB(nd);
         }
+      } else if (!itf.es_perimeter && g_ps_radial > 0) {
+        PseudoespectralCirculoSolver ps;
+        ps.Inicializa(itf.centro, itf.radio, itf.nudos_circunferencia.size(), g_ps_radial,
+                      itf.nudos_circunferencia[0].posicion_angular, bvp);
+        ps.Resuelve(bvp, itf.nudos_interior, itf.nudos_circunferencia);
+        S.Actualiza_GB(itf);
       }
       ++idx;
     }

@@ -3,6 +3,8 @@ implementation itself: SpAc's own hot-path sources compiled unmodified
 against oracle/shim (oracle/Makefile target `ref`, library oracle/_ref/).
 
 Run where the reference sources exist:  python tests/golden/make_golden.py
+(`python tests/golden/make_golden.py ps` writes only the pseudospectral disk
+fixtures ps_disks.npz and ps_rows_*.npz.)
 The random stream is the shim's sequential stream with one OpenMP thread,
 which the oracle reproduces in its sequential mode.
 """
@@ -28,6 +30,15 @@ ASSEMBLIES = [  # (mesh name, problem, use_F, N, h)
     ("unit3", 0, 0, 64, 1e-3),
     ("unit3", 2, 1, 64, 1e-3),
 ]
+# pseudospectral disks (PseudoespectralCirculoSolver): (problem, cx, cy, R, N_circunferencia, N_radio, theta0,
+# periphery angle offset from the angular grid, interior nodes)
+PS_DISKS = [
+    (0, 0.5, 0.5, 0.3, 16, 11, 0.1, 0.0, 12),
+    (1, -72.0, -38.0, 5.0, 20, 15, 0.3, 0.0, 9),
+    (2, 0.4, 0.6, 0.25, 12, 9, 0.0, 0.2, 7),
+    (0, 0.3, 0.7, 0.2, 44, 43, 0.1428, 0.0, 16),   # the serial driver's sizes (main_test_serial.cpp:48,70)
+]
+PS_ROWS = [("unit3", 0, 11), ("serial", 0, 43)]  # (mesh, problem, N_radio): interior-circle rows only
 POINTS = [  # (problem, use_F, dom, (x, y), sub_kind, sub, N, h)
     (0, 0, (0, 0, 1, 1), (0.31, 0.4), 0, None, 200, 1e-3),
     (0, 1, (0, 0, 1, 1), (0.8, 0.85), 0, None, 200, 1e-2),
@@ -56,12 +67,12 @@ def ref():
     return L
 
 
-def mesh_and_assembly(L, name, problem, use_F, N, h, solve):
+def mesh_and_assembly(L, name, problem, use_F, N, h, solve, do_solve=1):
     cfg = {m[0]: m for m in MESHES}[name]
     _, dom, Nl, sup, th0, npc = cfg
     s = L.ref_solver_new(1)
     d = (C.c_double * 4)(*dom)
-    L.ref_assemble_circles(s, problem, use_F, d, Nl, sup, th0, npc, 1.5, 1.1, N, h, 1 if solve else 0)
+    L.ref_assemble_circles(s, problem, use_F, d, Nl, sup, th0, npc, 1.5, 1.1, N, h, do_solve if solve else 0)
     nr, nnz, ni, nn, nf = (C.c_int() for _ in range(5))
     L.ref_last_sizes(C.byref(nr), C.byref(nnz), C.byref(ni), C.byref(nn), C.byref(nf))
     rp = np.zeros(nr.value + 1, np.int32)
@@ -120,8 +131,8 @@ def mesh_and_assembly(L, name, problem, use_F, N, h, solve):
             it_G.append(G[:ii[3]])
         out["item_int"] = np.array(it_i, np.int32)       # row, iface, frontera, nG
         out["item_dbl"] = np.array(it_d)                 # B, phi, phiphi, phi_VR, phiphi_VR, xi, xixi, xiphi, APL, RNGC
-        out["item_cols"] = np.concatenate(it_cols)
-        out["item_G"] = np.concatenate(it_G)
+        out["item_cols"] = np.concatenate(it_cols) if it_cols else np.zeros(0, np.int32)
+        out["item_G"] = np.concatenate(it_G) if it_G else np.zeros(0)
         out["val"] = val
         out["B"] = B
         out["params"] = np.array([problem, use_F, N, h])
@@ -129,9 +140,43 @@ def mesh_and_assembly(L, name, problem, use_F, N, h, solve):
     return out
 
 
+def ps_fixtures(L):
+    L.ref_ps_disk.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int,
+                              _dp, C.c_int, _dp, _dp, _dp]
+    L.ref_set_ps_radial.argtypes = [C.c_int]
+    rng = np.random.default_rng(2027)
+    cases, th, xy, G, B = [], [], [], [], []
+    for problem, cx, cy, R, nc, nr, th0, off, n_in in PS_DISKS:
+        pth = th0 + off + 2 * np.pi * np.arange(nc) / nc
+        rr = 0.92 * R * np.sqrt(rng.random(n_in))
+        aa = 2 * np.pi * rng.random(n_in)
+        pts = np.ascontiguousarray(np.stack([cx + rr * np.cos(aa), cy + rr * np.sin(aa)], 1))
+        g = np.zeros((n_in, nc))
+        b = np.zeros(n_in)
+        L.ref_ps_disk(problem, cx, cy, R, nc, nr, th0, nc, pth.ctypes.data_as(_dp), n_in, pts.ctypes.data_as(_dp),
+                      g.ctypes.data_as(_dp), b.ctypes.data_as(_dp))
+        cases.append([problem, cx, cy, R, nc, nr, th0, nc, n_in])
+        th.append(pth)
+        xy.append(pts)
+        G.append(g.ravel())
+        B.append(b)
+    np.savez_compressed(os.path.join(HERE, "ps_disks.npz"), cases=np.array(cases), periph_theta=np.concatenate(th),
+                        inner_xy=np.concatenate(xy), G=np.concatenate(G), B=np.concatenate(B))
+    for name, problem, nr in PS_ROWS:
+        L.ref_set_ps_radial(nr)
+        a = mesh_and_assembly(L, name, problem, 0, 1, 1e-3, True, do_solve=2)
+        L.ref_set_ps_radial(0)
+        np.savez_compressed(os.path.join(HERE, f"ps_rows_{name}.npz"), val=a["val"], B=a["B"], val0=a["val0"],
+                            params=np.array([problem, nr]))
+
+
 def main():
     L = ref()
     L.ref_solver_free.argtypes = [C.c_void_p]
+    if sys.argv[1:] == ["ps"]:
+        ps_fixtures(L)
+        print("pseudospectral fixtures written to", HERE)
+        return 0
     for name, dom, Nl, sup, th0, npc in MESHES:
         m = mesh_and_assembly(L, name, 0, 0, 1, 1e-3, False)
         np.savez_compressed(os.path.join(HERE, f"mesh_{name}.npz"), dom=np.array(dom),
@@ -191,6 +236,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "functors.npz"), probe=probe, rect=np.array(rect), circ=np.array(circ),
                         d_rect=np.array(d_rect), d_circ=np.array(d_circ), coefs=np.array(coefs),
                         circ_center=np.array(list(o5)))
+    ps_fixtures(L)
     print("golden fixtures written to", HERE)
 
 
