@@ -34,6 +34,7 @@ extern "C" {
 #define FK_ERR_NOT_FOUND (-5)
 #define FK_ERR_NO_DEVICE (-6)
 #define FK_ERR_CAPACITY (-7)
+#define FK_ERR_NUMERIC (-8)   /* a disk solve met a singular mode matrix or did not converge */
 
 /* BVP coefficient sets compiled as fused device functors.  Each is the GPU
  * twin of a set of reference coefficient function pointers (BVP/BVP.hpp:17-28):
@@ -212,6 +213,40 @@ int fk_mesh_csr(fk_ctx* ctx, int mesh_id, int* rowptr, int* col, double* val0);
 int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsigned* paths_per_item,
                 double h, int precision, double* val, double* B, double* item_G, double* item_B,
                 fk_stats* item_stats);
+
+/* ---- pseudospectral disk rows ---------------------------------------------
+ * PseudoespectralCirculoSolver::Inicializa(centro, radio, N_circunferencia,
+ * N_radio, theta_0, BVP) + Resuelve(BVP, nudos_interior, nudos_periferia)
+ * (Solvers/PseudoespectralCirculoSolver.cpp:2-189, :215-260) with
+ * Interpolador_PS::Interpola (BVP/Interpolador_PS.cpp:34-61): the
+ * deterministic FP64 rows of the interior nodes of a disk, against the
+ * disk's periphery nodes.  The collocation system (Laplacian in polar
+ * coordinates + c, outer ring = identity rows; sigma and b of the BVP are not
+ * used, as in the reference) is solved on the GPU per Fourier mode; with a
+ * c that varies over the disk the solve iterates on the constant-c operator
+ * and returns FK_ERR_NUMERIC if that does not converge. */
+typedef struct {
+  double cx, cy, radius;
+  double theta0;               /* angle of the first grid ray (nudos_circunferencia[0].posicion_angular) */
+  int n_circle;                /* N_circunferencia: grid angles, even, 2..128 */
+  int n_radial;                /* N_radio: Chebyshev intervals on a diameter, odd, 3..63 */
+  int n_periph;                /* periphery nodes (nudos_periferia), 2..128 */
+  const double* periph_theta;  /* their posicion_angular */
+  int n_inner;                 /* interior nodes (nudos_interior) */
+  const double* inner_xy;      /* their posicion_cartesiana, (x, y) pairs */
+} fk_disk_desc;
+/* Batched disk solves.  For disk d, G receives n_inner x n_periph entries
+ * (row-major, nudos_interior[p].G[periphery i]) at offset sum of the earlier
+ * disks' n_inner * n_periph, and B the n_inner values nudos_interior[p].B at
+ * offset sum of the earlier n_inner.  fk_last_timing: [0] grid, mode and
+ * solve kernels, [1] interpolation kernel, [2] launches. */
+int fk_solve_disks_ps(fk_ctx* ctx, int bvp_id, int n_disks, const fk_disk_desc* disks, double* G, double* B);
+/* Circle meshes: n_radial > 0 makes fk_assemble also fill the rows of the
+ * interior nodes of every full (non-perimeter) circle by the disk solve
+ * with N_radio = n_radial, added into val and B as
+ * SistemaLineal::Actualiza_GB(Interfaz&) (Mesh/SistemaLineal.cpp:90-95), as
+ * the reference drivers do (main_test_serial.cpp:67-80); 0 switches it off. */
+int fk_mesh_set_disk_solver(fk_ctx* ctx, int mesh_id, int n_radial);
 
 /* ---- host-side consumers of the assembled system (no GPU needed) -----------
  * Restarted GMRES(restart) with right Jacobi preconditioning on a CSR system,

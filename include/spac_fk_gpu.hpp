@@ -58,6 +58,43 @@ std::uintptr_t key_of(Fn f) {
   return reinterpret_cast<std::uintptr_t>(f);
 }
 
+// Frontera -> (shape, parameters) through the distance registry.
+template <class FronteraT>
+bool shape_of(const FronteraT& fr, int* shape, double p[4], bool required) {
+  auto& reg = distance_registry();
+  const auto f = reg.find(key_of(fr.Distancia));
+  if (f == reg.end()) {
+    if (required) throw std::runtime_error("spac_fk_gpu: unregistered Frontera distance function");
+    return false;
+  }
+  *shape = f->second;
+  const size_t np = fr.parametros.size();
+  if ((*shape == FK_SHAPE_RECT && np < 4) || (*shape == FK_SHAPE_CIRCLE && np < 3))
+    throw std::runtime_error("spac_fk_gpu: Frontera parameters too short for its shape");
+  for (size_t i = 0; i < 4; ++i) p[i] = i < np ? fr.parametros[i] : 0.0;
+  return true;
+}
+
+// BVP -> fk_bvp_desc through the problem registry (u's function) and BVP::F
+// (the exact-gradient control variate when it is the registered F_exact).
+// need_domain: the domain's distance function must be registered.
+template <class BVPT>
+fk_bvp_desc describe_bvp(const BVPT& P, bool need_domain) {
+  auto& reg = problem_registry();
+  const auto f = reg.find(key_of(P.u.funcion));
+  if (f == reg.end()) throw std::runtime_error("spac_fk_gpu: unregistered BVP (its u function)");
+  const ProblemBinding& b = f->second;
+  fk_bvp_desc d;
+  d.problem = b.problem;
+  d.cv = (b.F_exact != 0 && key_of(P.F.funcion) == b.F_exact) ? FK_CV_EXACT : FK_CV_NONE;
+  d.mlp_id = -1;
+  d.dom_shape = FK_SHAPE_RECT;
+  for (int i = 0; i < 4; ++i) d.dom[i] = 0.0;
+  shape_of(P.frontera_dominio, &d.dom_shape, d.dom, need_domain);
+  for (int i = 0; i < 4; ++i) d.prob[i] = b.prob[i];
+  return d;
+}
+
 }  // namespace spac_fk_gpu
 
 class FeynmanKacSolverGPU {
@@ -161,35 +198,12 @@ class FeynmanKacSolverGPU {
 
   template <class FronteraT>
   static bool shape_of(const FronteraT& fr, int* shape, double p[4], bool required) {
-    auto& reg = spac_fk_gpu::distance_registry();
-    const auto f = reg.find(spac_fk_gpu::key_of(fr.Distancia));
-    if (f == reg.end()) {
-      if (required) throw std::runtime_error("FeynmanKacSolverGPU: unregistered Frontera distance function");
-      return false;
-    }
-    *shape = f->second;
-    const size_t np = fr.parametros.size();
-    if ((*shape == FK_SHAPE_RECT && np < 4) || (*shape == FK_SHAPE_CIRCLE && np < 3))
-      throw std::runtime_error("FeynmanKacSolverGPU: Frontera parameters too short for its shape");
-    for (size_t i = 0; i < 4; ++i) p[i] = i < np ? fr.parametros[i] : 0.0;
-    return true;
+    return spac_fk_gpu::shape_of(fr, shape, p, required);
   }
 
   template <class BVPT>
   int bvp_id(const BVPT& P) {
-    auto& reg = spac_fk_gpu::problem_registry();
-    const auto f = reg.find(spac_fk_gpu::key_of(P.u.funcion));
-    if (f == reg.end()) throw std::runtime_error("FeynmanKacSolverGPU: unregistered BVP (its u function)");
-    const spac_fk_gpu::ProblemBinding& b = f->second;
-    const std::uintptr_t F = spac_fk_gpu::key_of(P.F.funcion);
-    int cv = FK_CV_NONE;
-    if (b.F_exact != 0 && F == b.F_exact) cv = FK_CV_EXACT;
-    fk_bvp_desc d;
-    d.problem = b.problem;
-    d.cv = cv;
-    d.mlp_id = -1;
-    shape_of(P.frontera_dominio, &d.dom_shape, d.dom, true);
-    for (int i = 0; i < 4; ++i) d.prob[i] = b.prob[i];
+    const fk_bvp_desc d = spac_fk_gpu::describe_bvp(P, true);
     const auto key = std::make_tuple(d.problem, d.cv, d.dom_shape, d.dom[0], d.dom[1], d.dom[2], d.dom[3], d.prob[0],
                                      d.prob[1], d.prob[2], d.prob[3]);
     const auto it = bvps_.find(key);
@@ -238,6 +252,90 @@ class FeynmanKacSolverGPU {
     xiphi = s.xiphi;
     APL = s.APL;
     RNGC = s.RNGC;
+  }
+};
+
+// PseudoespectralCirculoSolver on the GPU (Solvers/PseudoespectralCirculoSolver.hpp:8-18):
+// Inicializa records the disk, Resuelve(BVP, nudos_interior, nudos_periferia)
+// fills nudos_interior[p].B and nudos_interior[p].G[periphery indice_global]
+// as the reference does (PseudoespectralCirculoSolver.cpp:215-260), through
+// fk_solve_disks_ps.  The BVP goes through the same registry as
+// FeynmanKacSolverGPU (Register_Problem); its domain distance need not be
+// registered.  The reference's Resuelve(BVP) (grid values of the Dirichlet
+// problem with boundary data g, kept in interpolador.valores.z) has no
+// counterpart: its solution table is not exposed.
+class PseudoespectralCirculoSolverGPU {
+ public:
+  explicit PseudoespectralCirculoSolverGPU(int device = 0) {
+    if (fk_create(&ctx_, device, 0) != FK_OK)
+      throw std::runtime_error("PseudoespectralCirculoSolverGPU: fk_create failed (no usable CUDA device?)");
+  }
+  ~PseudoespectralCirculoSolverGPU() {
+    if (ctx_) fk_destroy(ctx_);
+  }
+  PseudoespectralCirculoSolverGPU(const PseudoespectralCirculoSolverGPU&) = delete;
+  PseudoespectralCirculoSolverGPU& operator=(const PseudoespectralCirculoSolverGPU&) = delete;
+
+  // Inicializa(centro, radio, N_circunferencia, N_radio, theta_0, BVP)  (:2-189)
+  template <class Vec2, class BVPT>
+  void Inicializa(const Vec2& centro, double radio, unsigned int N_circunferencia, unsigned int N_radio,
+                  double theta_0, const BVPT& Problema) {
+    (void)Problema;
+    cx_ = centro[0];
+    cy_ = centro[1];
+    radius_ = radio;
+    n_circle_ = static_cast<int>(N_circunferencia);
+    n_radial_ = static_cast<int>(N_radio);
+    theta0_ = theta_0;
+  }
+
+  // Resuelve(BVP, nudos_interior, nudos_periferia)  (:215-260)
+  template <class BVPT, class NudoT>
+  void Resuelve(const BVPT& Problema, std::vector<NudoT>& nudos_interior, std::vector<NudoT> nudos_periferia) {
+    const fk_bvp_desc desc = spac_fk_gpu::describe_bvp(Problema, false);
+    const auto key = std::make_tuple(desc.problem, desc.prob[0], desc.prob[1], desc.prob[2], desc.prob[3]);
+    auto found = bvps_.find(key);
+    if (found == bvps_.end()) {
+      int id = -1;
+      check(fk_register_bvp(ctx_, &desc, &id));
+      found = bvps_.emplace(key, id).first;
+    }
+    const int bvp = found->second;
+    const int np = static_cast<int>(nudos_periferia.size()), ni = static_cast<int>(nudos_interior.size());
+    std::vector<double> theta(np), xy(2 * static_cast<size_t>(ni)), G(static_cast<size_t>(ni) * np), B(ni);
+    for (int i = 0; i < np; ++i) theta[i] = nudos_periferia[i].posicion_angular;
+    for (int p = 0; p < ni; ++p) {
+      xy[2 * p] = nudos_interior[p].posicion_cartesiana[0];
+      xy[2 * p + 1] = nudos_interior[p].posicion_cartesiana[1];
+    }
+    fk_disk_desc d;
+    d.cx = cx_;
+    d.cy = cy_;
+    d.radius = radius_;
+    d.theta0 = theta0_;
+    d.n_circle = n_circle_;
+    d.n_radial = n_radial_;
+    d.n_periph = np;
+    d.periph_theta = theta.data();
+    d.n_inner = ni;
+    d.inner_xy = xy.data();
+    check(fk_solve_disks_ps(ctx_, bvp, 1, &d, G.data(), B.data()));
+    for (int p = 0; p < ni; ++p) {
+      nudos_interior[p].B = B[p];
+      for (int i = 0; i < np; ++i) nudos_interior[p].G[nudos_periferia[i].indice_global] = G[static_cast<size_t>(p) * np + i];
+    }
+  }
+
+  fk_ctx* context() const { return ctx_; }
+
+ private:
+  fk_ctx* ctx_ = nullptr;
+  std::map<std::tuple<int, double, double, double, double>, int> bvps_;  // registered problems
+  double cx_ = 0.0, cy_ = 0.0, radius_ = 0.0, theta0_ = 0.0;
+  int n_circle_ = 0, n_radial_ = 0;
+
+  void check(int rc) {
+    if (rc != FK_OK) throw std::runtime_error(std::string("PseudoespectralCirculoSolverGPU: ") + fk_last_error(ctx_));
   }
 };
 

@@ -12,6 +12,7 @@
 #include "../../include/spac_fk.h"
 #include "fk_device.cuh"
 #include "fk_internal.h"
+#include "fk_disk.h"
 #include "fk_mesh.h"
 #include "fk_mlp.h"
 
@@ -61,8 +62,17 @@ struct StencilSet {
   }
 };
 
+// device copies of a disk batch
+struct DiskBufs {
+  DBuf disks, tab, pth, ixy, idisk, irow, cpos;
+  bool uploaded = false;
+};
+
 struct Mesh {
   HostMesh host;
+  int disk_radial = 0;   // fk_mesh_set_disk_solver
+  DiskBatch disk;
+  DiskBufs dbufs;
   StencilSet st;
   std::vector<long long> g_off;  // per item
   long long g_total = 0;
@@ -92,6 +102,8 @@ struct fk_ctx {
   std::vector<std::unique_ptr<fk::Mlp>> mlps;
   // workspace
   fk::DBuf w_items, w_chunks, w_stats, w_acc, w_queue, w_gout, w_bout, w_sout, w_val, w_B, w_goff, w_row, w_tmp;
+  fk::DBuf w_dgrid, w_dcbar, w_dvar, w_dminv, w_dz, w_dG, w_dB, w_dflags;
+  fk::DiskBufs w_disk;
 };
 
 namespace {
@@ -817,6 +829,68 @@ static int upload_mesh(fk_ctx* ctx, fk::Mesh* M) {
   return FK_OK;
 }
 
+// Disk rows: uploads the batch once, runs the four disk kernels on the
+// context stream into G/B (device, may be null) and/or the CSR values and B
+// (device, may be null), and checks the kernels' error flags.
+static int run_disks(fk_ctx* ctx, int bvp_id, const fk::DiskBatch& b, fk::DiskBufs& u, double* G, double* B,
+                     double* val, double* Bcsr, bool timed) {
+  cudaStream_t s = ctx->stream;
+  if (!u.uploaded) {
+    FK_CUDA(fk::upload(u.disks, b.disks, s));
+    FK_CUDA(fk::upload(u.tab, b.tab, s));
+    FK_CUDA(fk::upload(u.pth, b.periph_theta, s));
+    FK_CUDA(fk::upload(u.ixy, b.inner_xy, s));
+    FK_CUDA(fk::upload(u.idisk, b.inner_disk, s));
+    FK_CUDA(fk::upload(u.irow, b.inner_row, s));
+    FK_CUDA(fk::upload(u.cpos, b.csr_pos, s));
+    u.uploaded = true;
+  }
+  const int nd = static_cast<int>(b.disks.size());
+  FK_CUDA(ctx->w_dgrid.ensure(std::max<long long>(b.grid_total, 1) * sizeof(double)));
+  FK_CUDA(ctx->w_dcbar.ensure(std::max(nd, 1) * sizeof(double)));
+  FK_CUDA(ctx->w_dvar.ensure(std::max(nd, 1) * sizeof(int)));
+  FK_CUDA(ctx->w_dminv.ensure(std::max<long long>(b.minv_total, 1) * sizeof(double)));
+  FK_CUDA(ctx->w_dz.ensure(std::max<long long>(b.z_total, 1) * sizeof(double)));
+  FK_CUDA(ctx->w_dflags.ensure(2 * sizeof(int)));
+  FK_CUDA(cudaMemsetAsync(ctx->w_dflags.p, 0, 2 * sizeof(int), s));
+  fk::DiskArgs a;
+  a.bvp = ctx->d_bvps.as<fk::BvpDev>() + bvp_id;
+  a.disks = u.disks.as<fk::DiskDev>();
+  a.n_disks = nd;
+  a.tab = u.tab.as<double>();
+  a.periph_theta = u.pth.as<double>();
+  a.inner_xy = u.ixy.as<double>();
+  a.inner_disk = u.idisk.as<int>();
+  a.grid = ctx->w_dgrid.as<double>();
+  a.cbar = ctx->w_dcbar.as<double>();
+  a.varying = ctx->w_dvar.as<int>();
+  a.minv = ctx->w_dminv.as<double>();
+  a.z = ctx->w_dz.as<double>();
+  a.G = G;
+  a.B = B;
+  const bool csr = val && b.has_csr;
+  a.inner_row = csr ? u.irow.as<int>() : nullptr;
+  a.csr_pos = csr ? u.cpos.as<int>() : nullptr;
+  a.val = csr ? val : nullptr;
+  a.Bcsr = csr ? Bcsr : nullptr;
+  a.flags = ctx->w_dflags.as<int>();
+  FK_CUDA(fk::disk_launch(ctx->bvps[bvp_id].problem, a, b, s, timed ? ctx->ev : nullptr));
+  int flags[2];
+  FK_CUDA(cudaMemcpyAsync(flags, ctx->w_dflags.p, sizeof(flags), cudaMemcpyDeviceToHost, s));
+  FK_CUDA(cudaStreamSynchronize(s));
+  if (timed) {
+    float t0 = 0, t1 = 0;
+    cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[2]);
+    ctx->timing[0] = t0;
+    ctx->timing[1] = t1;
+    ctx->timing[2] = 4;
+  }
+  if (flags[0]) return fail(ctx, FK_ERR_NUMERIC, "disk solve: singular Fourier-mode matrix");
+  if (flags[1]) return fail(ctx, FK_ERR_NUMERIC, "disk solve: iteration on the varying c did not converge");
+  return FK_OK;
+}
+
 int fk_mesh_get_info(fk_ctx* ctx, int mesh_id, fk_mesh_info* info) {
   fk::Mesh* M = get_mesh(ctx, mesh_id);
   if (!M || !info) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
@@ -874,6 +948,77 @@ int fk_mesh_csr(fk_ctx* ctx, int mesh_id, int* rowptr, int* col, double* val0) {
   return FK_OK;
 }
 
+int fk_solve_disks_ps(fk_ctx* ctx, int bvp_id, int n_disks, const fk_disk_desc* disks, double* G, double* B) {
+  if (!ctx || n_disks < 0 || (n_disks > 0 && !disks)) return fail(ctx, FK_ERR_ARG, "null argument");
+  int rc = check_bvp(ctx, bvp_id);
+  if (rc) return rc;
+  if ((rc = need_device(ctx))) return rc;
+  std::vector<fk::DiskHost> in(n_disks);
+  for (int d = 0; d < n_disks; ++d) {
+    const fk_disk_desc& q = disks[d];
+    if (q.n_periph < 0 || q.n_inner < 0 || (q.n_periph > 0 && !q.periph_theta) || (q.n_inner > 0 && !q.inner_xy))
+      return fail(ctx, FK_ERR_ARG, "disk: null node arrays");
+    fk::DiskHost& h = in[d];
+    h.cx = q.cx; h.cy = q.cy; h.radius = q.radius; h.theta0 = q.theta0;
+    h.n_circle = q.n_circle; h.n_radial = q.n_radial;
+    h.periph_theta.assign(q.periph_theta, q.periph_theta + q.n_periph);
+    h.inner_xy.assign(q.inner_xy, q.inner_xy + 2 * static_cast<size_t>(q.n_inner));
+  }
+  fk::DiskBatch b;
+  if (!fk::disk_prepare(in, b, ctx->err)) return FK_ERR_ARG;
+  if (ctx->bvps.size() * sizeof(fk::BvpDev) > ctx->d_bvps.bytes) {
+    FK_CUDA(fk::upload(ctx->d_bvps, ctx->bvps, ctx->stream));
+  }
+  cudaStream_t s = ctx->stream;
+  FK_CUDA(ctx->w_dG.ensure(std::max<long long>(b.g_total, 1) * sizeof(double)));
+  FK_CUDA(ctx->w_dB.ensure(std::max<long long>(b.n_inner, 1) * sizeof(double)));
+  ctx->w_disk.uploaded = false;
+  rc = run_disks(ctx, bvp_id, b, ctx->w_disk, ctx->w_dG.as<double>(), ctx->w_dB.as<double>(), nullptr, nullptr, true);
+  if (rc) return rc;
+  FK_CUDA(copy_out(G, ctx->w_dG.p, b.g_total * sizeof(double), s));
+  FK_CUDA(copy_out(B, ctx->w_dB.p, b.n_inner * sizeof(double), s));
+  FK_CUDA(cudaStreamSynchronize(s));
+  return FK_OK;
+}
+
+int fk_mesh_set_disk_solver(fk_ctx* ctx, int mesh_id, int n_radial) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (M->host.kind != 1) return fail(ctx, FK_ERR_ARG, "disk rows need a circle mesh");
+  if (n_radial < 0) return fail(ctx, FK_ERR_ARG, "n_radial must be >= 0");
+  M->disk_radial = 0;
+  M->disk = fk::DiskBatch();
+  M->dbufs.uploaded = false;
+  if (n_radial == 0) return FK_OK;
+  const fk::HostMesh& hm = M->host;
+  std::vector<fk::DiskHost> in;
+  for (const fk::MeshStencil& S : hm.stencils) {
+    if (S.perimeter || S.inner.empty()) continue;
+    fk::DiskHost h;
+    h.cx = S.cx; h.cy = S.cy; h.radius = S.radius;
+    h.theta0 = S.nodes.empty() ? 0.0 : S.nodes[0].theta;
+    h.n_circle = static_cast<int>(S.nodes.size());
+    h.n_radial = n_radial;
+    for (const fk::MeshNode& nd : S.nodes) h.periph_theta.push_back(nd.theta);
+    for (const fk::MeshNode& in_nd : S.inner) {
+      h.inner_xy.push_back(in_nd.x);
+      h.inner_xy.push_back(in_nd.y);
+      h.inner_row.push_back(in_nd.gid);
+      const int* row_begin = hm.col.data() + hm.rowptr[in_nd.gid];
+      const int* row_end = hm.col.data() + hm.rowptr[in_nd.gid + 1];
+      for (const fk::MeshNode& c : S.nodes) {
+        const int* p = std::lower_bound(row_begin, row_end, c.gid);
+        if (p == row_end || *p != c.gid) return fail(ctx, FK_ERR_NOT_FOUND, "circle node missing from the CSR row");
+        h.csr_pos.push_back(static_cast<int>(p - hm.col.data()));
+      }
+    }
+    in.push_back(std::move(h));
+  }
+  if (!fk::disk_prepare(in, M->disk, ctx->err)) return FK_ERR_ARG;
+  M->disk_radial = n_radial;
+  return FK_OK;
+}
+
 int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsigned* paths_per_item, double h,
                 int precision, double* val, double* B, double* item_G, double* item_B, fk_stats* item_stats) {
   fk::Mesh* M = get_mesh(ctx, mesh_id);
@@ -909,6 +1054,11 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   rc = run_items(ctx, bvp_id, precision, it, &M->st, &M->g_off, M->g_total, M->d_csr_idx.as<int>(),
                  ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro);
   if (rc) return rc;
+  if (M->disk_radial > 0 && !M->disk.disks.empty()) {
+    rc = run_disks(ctx, bvp_id, M->disk, M->dbufs, nullptr, nullptr, ctx->w_val.as<double>(), ctx->w_B.as<double>(),
+                   false);
+    if (rc) return rc;
+  }
   FK_CUDA(copy_out(val, ctx->w_val.p, hm.nnz * sizeof(double), s));
   FK_CUDA(copy_out(B, ctx->w_B.p, hm.n_rows * sizeof(double), s));
   FK_CUDA(copy_out(item_G, ro.item_G, M->g_total * sizeof(double), s));

@@ -49,6 +49,12 @@ class NodeItem(C.Structure):
                 ("frontera", C.c_int), ("row", C.c_int), ("stencil", C.c_int)]
 
 
+class DiskDesc(C.Structure):
+    _fields_ = [("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double), ("theta0", C.c_double),
+                ("n_circle", C.c_int), ("n_radial", C.c_int), ("n_periph", C.c_int), ("periph_theta", _dp),
+                ("n_inner", C.c_int), ("inner_xy", _dp)]
+
+
 class MeshInfo(C.Structure):
     _fields_ = [("n_rows", C.c_int), ("nnz", C.c_int), ("n_items", C.c_int), ("n_nodes", C.c_int),
                 ("n_stencils", C.c_int), ("max_stencil", C.c_int), ("spacing", C.c_double)]
@@ -87,6 +93,8 @@ _SIGS = {
     "fk_mesh_csr": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp]),
     "fk_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint, _up, C.c_double, C.c_int, _dp, _dp, _dp,
                               _dp, C.POINTER(Stats)]),
+    "fk_solve_disks_ps": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(DiskDesc), _dp, _dp]),
+    "fk_mesh_set_disk_solver": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_create": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_ulonglong, _ip]),
     "fk_mlp_num_params": (C.c_int, [C.c_void_p, C.c_int, _ip]),
     "fk_mlp_get_params": (C.c_int, [C.c_void_p, C.c_int, _fp]),
@@ -286,6 +294,35 @@ class Context:
         self.check(self.L.fk_mesh_circles(self.h, pd, n_side, superposicion, theta0, nodes_per_circle, c2_corner,
                                           c2_side, C.byref(i)))
         return i.value
+
+    def mesh_set_disk_solver(self, mesh, n_radial):
+        """fk_mesh_set_disk_solver: interior-circle rows by the pseudospectral disk solve (0 = off)."""
+        self.check(self.L.fk_mesh_set_disk_solver(self.h, mesh, n_radial))
+
+    def solve_disks_ps(self, bvp, disks):
+        """fk_solve_disks_ps.  disks: dicts with cx, cy, radius, theta0, n_circle,
+        n_radial, periph_theta, inner_xy.  Returns [(G (n_inner x n_periph), B)] per disk."""
+        keep, descs = [], (DiskDesc * max(len(disks), 1))()
+        n_g = n_b = 0
+        for i, d in enumerate(disks):
+            th = np.ascontiguousarray(d["periph_theta"], dtype=np.float64)
+            xy = np.ascontiguousarray(d["inner_xy"], dtype=np.float64).reshape(-1, 2)
+            keep += [th, xy]
+            descs[i] = DiskDesc(d["cx"], d["cy"], d["radius"], d["theta0"], d["n_circle"], d["n_radial"], len(th),
+                                th.ctypes.data_as(_dp), len(xy), xy.ctypes.data_as(_dp))
+            n_g += len(th) * len(xy)
+            n_b += len(xy)
+        G = np.zeros(max(n_g, 1))
+        B = np.zeros(max(n_b, 1))
+        self.check(self.L.fk_solve_disks_ps(self.h, bvp, len(disks), descs, G.ctypes.data_as(_dp),
+                                            B.ctypes.data_as(_dp)))
+        out, og, ob = [], 0, 0
+        for d, k in zip(disks, range(0, len(keep), 2)):
+            npp, ni = len(keep[k]), len(keep[k + 1])
+            out.append((G[og:og + ni * npp].reshape(ni, npp).copy(), B[ob:ob + ni].copy()))
+            og += ni * npp
+            ob += ni
+        return out
 
     def mesh_square_patches(self, dom, n_sub, nodes_per_side, enlarge=0.25, eps_spacing=3.0, knn=20):
         dom, pd = _d(dom)

@@ -10,8 +10,12 @@
   large         32 x 32 subdomains, 63 nodes per patch side, h = 2.5e-4,
                 paths added per item until its standard error is below 1e-4,
                 learned control variate with plain FK as the per-item fallback
+  disk_rows     pseudospectral rows of the interior circles of a 32 x 32
+                circle layout: 900 disks of the serial driver's size
+                (44 grid angles, N_radio 43, 44 periphery and 44 interior
+                nodes each, main_test_serial.cpp:48-70), Franke problem
 
-  python -m spac_gb300.workloads point_solves|uneven|large [--scale s]
+  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows [--scale s]
 
 All inputs are seeded synthetic data; nothing is read from disk.
 """
@@ -186,9 +190,41 @@ def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_path
             "paths_per_item_median": float(np.median(done))}
 
 
+def disk_rows(ctx, n_disks=900, n_circle=44, n_radial=43, n_inner=44, seed=7, repeats=5):
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(np.sqrt(n_disks)))
+    H = 1.0 / (side + 1)
+    R = H / np.sqrt(2.0)
+    disks = []
+    for d in range(n_disks):
+        cx, cy = (d // side + 1) * H, (d % side + 1) * H
+        rr = 0.95 * R * np.sqrt(rng.random(n_inner))
+        aa = 2 * np.pi * rng.random(n_inner)
+        disks.append(dict(cx=cx, cy=cy, radius=R, theta0=0.1428, n_circle=n_circle, n_radial=n_radial,
+                          periph_theta=0.1428 + 2 * np.pi * np.arange(n_circle) / n_circle,
+                          inner_xy=np.stack([cx + rr * np.cos(aa), cy + rr * np.sin(aa)], 1)))
+    b = ctx.register_bvp(fk.FRANKE)
+    ctx.solve_disks_ps(b, disks)  # warm-up
+    walls, solve_ms, interp_ms = [], [], []
+    for _ in range(repeats):
+        t = time.perf_counter()
+        out = ctx.solve_disks_ps(b, disks)
+        walls.append(time.perf_counter() - t)
+        tm = ctx.last_timing()
+        solve_ms.append(tm[0])
+        interp_ms.append(tm[1])
+    G0, B0 = out[0]
+    return {"disks": n_disks, "n_circle": n_circle, "n_radial": n_radial, "n_inner": n_inner,
+            "rows": n_disks * n_inner, "wall_s_median": float(np.median(walls)),
+            "solve_kernels_ms_median": float(np.median(solve_ms)),
+            "interp_kernel_ms_median": float(np.median(interp_ms)),
+            "disks_per_s": n_disks / float(np.median(walls)),
+            "row_sum_err": float(np.abs(-G0.sum(1) - 1.0).max())}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["point_solves", "uneven", "large"])
+    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=2026)
     a = ap.parse_args()
@@ -197,6 +233,8 @@ def main():
         r = point_solves(ctx, paths=max(64, int(10000 * a.scale)))
     elif a.workload == "uneven":
         r = uneven(ctx, scale=a.scale)
+    elif a.workload == "disk_rows":
+        r = disk_rows(ctx, n_disks=max(1, int(900 * a.scale)))
     else:
         r = large(ctx, n_sub=max(2, int(round(32 * a.scale))), nodes_per_side=63 if a.scale >= 1 else 31)
     print(json.dumps({"workload": a.workload, **r}))

@@ -4,9 +4,14 @@
 // Usage: drop_in_main <arc file> <seed>
 // Arc file: cx cy radius c2 interior n / n lines "theta gid" / n*n iPsi
 // (column-major) / item count / per item "x y frontera gid".
+// drop_in_main --disk <disk file> drives PseudoespectralCirculoSolverGPU the
+// way main_test_serial.cpp:67-75 drives PseudoespectralCirculoSolver.
+// Disk file: cx cy radius N_circunferencia N_radio theta_0 / n_periph lines
+// "theta gid" / n_inner / n_inner lines "x y gid".
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <string>
 
 #include "ref_types.hpp"
 #include "spac_fk_gpu.hpp"
@@ -18,7 +23,34 @@ static Vector2d franke_F(Vector2d p) { return p; }
 static double rectangulo(std::vector<double>, Vector2d, Vector2d&, Vector2d&) { return 0.0; }
 static double circulo(std::vector<double>, Vector2d, Vector2d&, Vector2d&) { return 0.0; }
 
+static int disk_main(const char* path) {
+  FeynmanKacSolverGPU::Register_Problem(&franke_u, FK_PROBLEM_FRANKE, &franke_F);
+  BVP bvp;
+  bvp.u.funcion = &franke_u;
+  std::ifstream in(path);
+  Vector2d c;
+  double R = 0.0, th0 = 0.0;
+  unsigned nc = 0, nr = 0;
+  int np = 0, ni = 0;
+  in >> c[0] >> c[1] >> R >> nc >> nr >> th0 >> np;
+  std::vector<Nudo> periph(np), inner;
+  for (auto& nd : periph) in >> nd.posicion_angular >> nd.indice_global;
+  in >> ni;
+  inner.resize(ni);
+  for (auto& nd : inner) in >> nd.posicion_cartesiana[0] >> nd.posicion_cartesiana[1] >> nd.indice_global;
+  PseudoespectralCirculoSolverGPU ps(0);
+  ps.Inicializa(c, R, nc, nr, th0, bvp);
+  ps.Resuelve(bvp, inner, periph);
+  for (auto& nd : inner) {
+    std::printf("inner %d %.17g", nd.indice_global, nd.B);
+    for (auto& kv : nd.G) std::printf(" %d:%.17g", kv.first, kv.second);
+    std::printf("\n");
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 3 && std::string(argv[1]) == "--disk") return disk_main(argv[2]);
   if (argc < 3) return 2;
   FeynmanKacSolverGPU::Register_Problem(&franke_u, FK_PROBLEM_FRANKE, &franke_F);
   FeynmanKacSolverGPU::Register_Distance(&rectangulo, FK_SHAPE_RECT);

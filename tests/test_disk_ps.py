@@ -104,3 +104,91 @@ def test_ps_rows_oracle_matches_reference(orc, name):
     tol = ps_tol(len(circles[0][3]), nr)
     assert np.abs(val - g["val"]).max() <= tol * np.abs(g["val"]).max()
     assert np.abs(B - g["B"]).max() <= tol * np.abs(g["B"]).max()
+
+
+# ---- GPU: the disk kernels against the reference's golden outputs ----------
+
+def _desc(d, nr=None):
+    return dict(cx=d["cx"], cy=d["cy"], radius=d["R"], theta0=d["th0"], n_circle=d["nc"],
+                n_radial=nr or d["nr"], periph_theta=d["theta"], inner_xy=d["xy"])
+
+
+@pytest.mark.gpu
+def test_gpu_ps_disks_match_reference(gpu, fk):
+    disks = golden_disks()
+    for problem in sorted({d["problem"] for d in disks}):
+        sel = [d for d in disks if d["problem"] == problem]
+        b = gpu.register_bvp(problem, dom=problem_dom(problem))
+        out = gpu.solve_disks_ps(b, [_desc(d) for d in sel])    # one batched call per problem
+        for d, (G, B) in zip(sel, out):
+            tol = ps_tol(d["nc"], d["nr"])
+            assert np.abs(G - d["G"]).max() <= tol * np.abs(d["G"]).max(), (problem, d["nc"], d["nr"])
+            assert np.abs(B - d["B"]).max() <= tol * np.abs(d["B"]).max(), (problem, d["nc"], d["nr"])
+        t = gpu.last_timing()
+        assert t[0] > 0 and t[1] > 0
+
+
+@pytest.mark.gpu
+def test_gpu_ps_disk_properties(gpu, fk, orc):
+    # the serial driver's sizes on a disk with many interior nodes: -G rows sum
+    # to 1 (c = 0) and B - G u(ring) reproduces the exact solution
+    rng = np.random.default_rng(5)
+    cx, cy, R, nc, nr, th0 = 0.55, 0.45, 0.3, 44, 43, 0.1428
+    th = th0 + 2 * np.pi * np.arange(nc) / nc
+    rr = 0.95 * R * np.sqrt(rng.random(500))
+    aa = 2 * np.pi * rng.random(500)
+    xy = np.stack([cx + rr * np.cos(aa), cy + rr * np.sin(aa)], 1)
+    b = gpu.register_bvp(fk.FRANKE)
+    (G, B), = gpu.solve_disks_ps(b, [dict(cx=cx, cy=cy, radius=R, theta0=th0, n_circle=nc, n_radial=nr,
+                                          periph_theta=th, inner_xy=xy)])
+    assert np.allclose(-G.sum(1), 1.0, atol=1e-9)
+    ob = orc.bvp(0)
+    u_ring = np.array([orc.coefficients(ob, cx + R * np.cos(t), cy + R * np.sin(t))[0] for t in th])
+    u_in = np.array([orc.coefficients(ob, x, y)[0] for x, y in xy])
+    assert np.abs(B - G @ u_ring - u_in).max() < 1e-6
+    # against the oracle on a subset
+    Go, Bo = orc.ps_disk(ob, cx, cy, R, nc, nr, th0, th, xy[:40])
+    tol = ps_tol(nc, nr)
+    assert np.abs(G[:40] - Go).max() <= tol * np.abs(Go).max()
+    assert np.abs(B[:40] - Bo).max() <= tol * np.abs(Bo).max()
+
+
+@pytest.mark.gpu
+def test_gpu_ps_disk_argument_errors(gpu, fk):
+    b = gpu.register_bvp(fk.FRANKE)
+    th = np.linspace(0, 2 * np.pi, 16, endpoint=False)
+    base = dict(cx=0.5, cy=0.5, radius=0.2, theta0=0.0, n_circle=16, n_radial=11, periph_theta=th,
+                inner_xy=np.array([[0.5, 0.55]]))
+    for bad in (dict(n_circle=15), dict(n_radial=10), dict(n_radial=65), dict(radius=0.0),
+                dict(periph_theta=th[:1])):
+        with pytest.raises(fk.FKError):
+            gpu.solve_disks_ps(b, [dict(base, **bad)])
+    # empty interior: nothing to interpolate, no error
+    (G, B), = gpu.solve_disks_ps(b, [dict(base, inner_xy=np.zeros((0, 2)))])
+    assert G.size == 0 and B.size == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["unit3", "serial"])
+def test_gpu_ps_rows_in_assembly(gpu, fk, name):
+    """fk_assemble with the disk solver on: the interior-circle rows added to
+    val and B equal the reference's (PS rows of main_test_serial.cpp:67-80)."""
+    g = np.load(os.path.join(GOLDEN, f"ps_rows_{name}.npz"))
+    problem, nr = (int(v) for v in g["params"])
+    m, circles = full_circles(f"mesh_{name}.npz")
+    Nl, sup, th0, npc, c2c, c2s = m["cfg"]
+    mesh = gpu.mesh_circles(tuple(m["dom"]), int(Nl), sup, th0, int(npc), c2c, c2s)
+    rp, col, v0 = gpu.mesh_csr(mesh)
+    assert np.array_equal(rp, m["rowptr"]) and np.array_equal(col, m["col"])
+    b = gpu.register_bvp(problem, dom=tuple(m["dom"]))
+    gpu.set_stream(91)
+    r0 = gpu.assemble(mesh, b, 8, 1e-3, fk.FP64)
+    gpu.mesh_set_disk_solver(mesh, nr)
+    gpu.set_stream(91)
+    r1 = gpu.assemble(mesh, b, 8, 1e-3, fk.FP64)
+    gpu.mesh_set_disk_solver(mesh, 0)
+    tol = ps_tol(len(circles[0][3]), nr)
+    dval, dB = r1["val"] - r0["val"], r1["B"] - r0["B"]
+    ref_val, ref_B = g["val"] - g["val0"], g["B"]
+    assert np.abs(dval - ref_val).max() <= tol * np.abs(ref_val).max()
+    assert np.abs(dB - ref_B).max() <= tol * np.abs(ref_B).max()

@@ -36,6 +36,12 @@ void drive(FeynmanKacSolverGPU& s, BVP& bvp, Nudo& nudo, Interfaz& interfaz) {
   FeynmanKacSolverGPU::Register_Problem(bvp.u.funcion, FK_PROBLEM_FRANKE, bvp.F.funcion);
   FeynmanKacSolverGPU::Register_Distance(bvp.frontera_dominio.Distancia, FK_SHAPE_RECT);
 }
+// main_test_serial.cpp:67-75 with the GPU class
+void drive_ps(PseudoespectralCirculoSolverGPU& ps, BVP& bvp, Interfaz& it) {
+  ps.Inicializa(it.centro, it.radio, it.nudos_circunferencia.size(), 43,
+                it.nudos_circunferencia[0].posicion_angular, bvp);
+  ps.Resuelve(bvp, it.nudos_interior, it.nudos_circunferencia);
+}
 """
 
 
@@ -127,3 +133,36 @@ def test_drop_in_matches_c_abi(fk):
             # condition ~1e10: G agrees to ~1e-11 between two runs of one path set
             for g, val in zip(arc["gids"], G):
                 assert np.isclose(got[int(g)], val, rtol=1e-9, atol=1e-9), (k, g)
+
+
+@pytest.mark.gpu
+def test_disk_drop_in_matches_c_abi(fk):
+    """PseudoespectralCirculoSolverGPU (Inicializa + Resuelve on Nudo vectors)
+    gives the G entries (keyed by periphery indice_global) and B of the C ABI."""
+    from test_disk_ps import golden_disks
+    d = golden_disks()[0]
+    assert d["problem"] == 0
+    gids = 100 + np.arange(d["nc"])
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = _driver(tmp)
+        path = os.path.join(tmp, "disk.txt")
+        with open(path, "w") as f:
+            f.write("%.17g %.17g %.17g %d %d %.17g %d\n" % (d["cx"], d["cy"], d["R"], d["nc"], d["nr"], d["th0"], d["nc"]))
+            for t, g in zip(d["theta"], gids):
+                f.write("%.17g %d\n" % (t, g))
+            f.write("%d\n" % len(d["xy"]))
+            for k, (x, y) in enumerate(d["xy"]):
+                f.write("%.17g %.17g %d\n" % (x, y, k))
+        out = subprocess.run([exe, "--disk", path], capture_output=True, text=True, check=True)
+    ctx = fk.Context(0, 1)
+    b = ctx.register_bvp(fk.FRANKE)
+    (G, B), = ctx.solve_disks_ps(b, [dict(cx=d["cx"], cy=d["cy"], radius=d["R"], theta0=d["th0"], n_circle=d["nc"],
+                                          n_radial=d["nr"], periph_theta=d["theta"], inner_xy=d["xy"])])
+    lines = [l for l in out.stdout.split("\n") if l.startswith("inner")]
+    assert len(lines) == len(d["xy"])
+    for k, line in enumerate(lines):
+        parts = line.split()
+        assert int(parts[1]) == k and float(parts[2]) == B[k]
+        got = dict((int(p.split(":")[0]), float(p.split(":")[1])) for p in parts[3:])
+        assert sorted(got) == [int(g) for g in gids]
+        assert [got[int(g)] for g in gids] == list(G[k])
