@@ -88,9 +88,13 @@ fk_bvp_desc describe_bvp(const BVPT& P, bool need_domain) {
   d.problem = b.problem;
   d.cv = (b.F_exact != 0 && key_of(P.F.funcion) == b.F_exact) ? FK_CV_EXACT : FK_CV_NONE;
   d.mlp_id = -1;
-  d.dom_shape = FK_SHAPE_RECT;
-  for (int i = 0; i < 4; ++i) d.dom[i] = 0.0;
-  shape_of(P.frontera_dominio, &d.dom_shape, d.dom, need_domain);
+  if (!shape_of(P.frontera_dominio, &d.dom_shape, d.dom, need_domain)) {
+    // no registered domain and none needed (the disk solve never reads it):
+    // a unit domain of the shape the problem functor expects
+    d.dom_shape = (b.problem == FK_PROBLEM_DISK) ? FK_SHAPE_CIRCLE : FK_SHAPE_RECT;
+    const double unit_rect[4] = {0.0, 0.0, 1.0, 1.0}, unit_circle[4] = {1.0, 0.0, 0.0, 0.0};
+    for (int i = 0; i < 4; ++i) d.dom[i] = (d.dom_shape == FK_SHAPE_CIRCLE) ? unit_circle[i] : unit_rect[i];
+  }
   for (int i = 0; i < 4; ++i) d.prob[i] = b.prob[i];
   return d;
 }

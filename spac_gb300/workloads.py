@@ -15,7 +15,13 @@
                 (44 grid angles, N_radio 43, 44 periphery and 44 interior
                 nodes each, main_test_serial.cpp:48-70), Franke problem
 
-  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows [--scale s]
+  serial_driver the reference serial driver end to end (main_test_serial.cpp:
+                38-89): 4 x 4 circles on [0, 1.25]^2 (44 nodes each,
+                superposicion 1), Franke, FK rows (1000 paths, h = 1e-5,
+                FP64) for perimeter circles, pseudospectral rows (N_radio 43)
+                for interior circles, GMRES on the host, node error
+
+  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows|serial_driver [--scale s]
 
 All inputs are seeded synthetic data; nothing is read from disk.
 """
@@ -222,9 +228,33 @@ def disk_rows(ctx, n_disks=900, n_circle=44, n_radial=43, n_inner=44, seed=7, re
             "row_sum_err": float(np.abs(-G0.sum(1) - 1.0).max())}
 
 
+def serial_driver(ctx, paths=1000, h=1e-5, n_radial=43, precision=fk.FP64, repeats=3):
+    dom = (0.0, 0.0, 1.25, 1.25)
+    mesh, t_mesh = _sync_time(lambda: ctx.mesh_circles(dom, 4, 1.0, 0.1428, 44))
+    ctx.mesh_set_disk_solver(mesh, n_radial)
+    b = ctx.register_bvp(fk.FRANKE, dom=dom)
+    rp, col, _ = ctx.mesh_csr(mesh)
+    xy, _ = ctx.mesh_nodes(mesh)
+    u = franke(xy[:, 0], xy[:, 1])
+    ctx.assemble(mesh, b, paths, h, precision)  # warm-up
+    t_asm, t_solve = [], []
+    for _ in range(repeats):
+        r, t = _sync_time(lambda: ctx.assemble(mesh, b, paths, h, precision, items=False, item_G=False))
+        t_asm.append(t)
+        (x, it, res, rc), t = _sync_time(lambda: fk.gmres(rp, col, r["val"], r["B"], tol=1e-12, max_iter=4000,
+                                                            restart=80))
+        t_solve.append(t)
+    info = ctx.mesh_info(mesh)
+    err = x - u
+    return {"rows": info["n_rows"], "nnz": info["nnz"], "fk_items": info["n_items"], "paths": paths, "h": h,
+            "n_radial": n_radial, "mesh_s": t_mesh, "assembly_s_median": float(np.median(t_asm)),
+            "gmres_s_median": float(np.median(t_solve)), "gmres_iters": it, "gmres_rel_resid": res,
+            "rms_node_error": float(np.sqrt(np.mean(err ** 2))), "max_node_error": float(np.abs(err).max())}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows"])
+    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows", "serial_driver"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=2026)
     a = ap.parse_args()
@@ -235,6 +265,8 @@ def main():
         r = uneven(ctx, scale=a.scale)
     elif a.workload == "disk_rows":
         r = disk_rows(ctx, n_disks=max(1, int(900 * a.scale)))
+    elif a.workload == "serial_driver":
+        r = serial_driver(ctx, paths=max(16, int(1000 * a.scale)))
     else:
         r = large(ctx, n_sub=max(2, int(round(32 * a.scale))), nodes_per_side=63 if a.scale >= 1 else 31)
     print(json.dumps({"workload": a.workload, **r}))

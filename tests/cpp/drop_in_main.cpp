@@ -10,6 +10,7 @@
 // "theta gid" / n_inner / n_inner lines "x y gid".
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
 #include <fstream>
 #include <string>
 
@@ -50,7 +51,14 @@ static int disk_main(const char* path) {
 }
 
 int main(int argc, char** argv) {
-  if (argc == 3 && std::string(argv[1]) == "--disk") return disk_main(argv[2]);
+  if (argc == 3 && std::string(argv[1]) == "--disk") {
+    try {
+      return disk_main(argv[2]);
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 3;
+    }
+  }
   if (argc < 3) return 2;
   FeynmanKacSolverGPU::Register_Problem(&franke_u, FK_PROBLEM_FRANKE, &franke_F);
   FeynmanKacSolverGPU::Register_Distance(&rectangulo, FK_SHAPE_RECT);

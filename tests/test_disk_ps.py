@@ -192,3 +192,25 @@ def test_gpu_ps_rows_in_assembly(gpu, fk, name):
     ref_val, ref_B = g["val"] - g["val0"], g["B"]
     assert np.abs(dval - ref_val).max() <= tol * np.abs(ref_val).max()
     assert np.abs(dB - ref_B).max() <= tol * np.abs(ref_B).max()
+
+
+@pytest.mark.gpu
+def test_gpu_serial_driver_pipeline_solves_franke(gpu, fk):
+    """The reference serial driver end to end (main_test_serial.cpp:38-89): FK
+    rows for the interior nodes of perimeter circles, pseudospectral rows for
+    interior circles, then the assembled system solved on the host (GMRES):
+    the node values approximate the exact Franke solution to the FK error."""
+    dom = (0.0, 0.0, 1.25, 1.25)
+    mesh = gpu.mesh_circles(dom, 4, 1.0, 0.1428, 44)
+    gpu.mesh_set_disk_solver(mesh, 43)
+    b = gpu.register_bvp(fk.FRANKE, dom=dom)
+    gpu.set_stream(5)
+    r = gpu.assemble(mesh, b, 4000, 1e-4, fk.FP64)
+    gpu.mesh_set_disk_solver(mesh, 0)
+    rp, col, _ = gpu.mesh_csr(mesh)
+    x, it, res, rc = fk.gmres(rp, col, r["val"], r["B"], tol=1e-12, max_iter=4000, restart=80)
+    assert rc == 0
+    from spac_gb300.workloads import franke
+    xy, _ = gpu.mesh_nodes(mesh)
+    err = x - franke(xy[:, 0], xy[:, 1])
+    assert np.sqrt(np.mean(err ** 2)) < 1e-2 and np.abs(err).max() < 5e-2, (np.sqrt(np.mean(err ** 2)), np.abs(err).max())
