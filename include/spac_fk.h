@@ -293,6 +293,14 @@ int fk_mlp_set_params(fk_ctx* ctx, int mlp_id, const float* params);
  * (length steps, may be NULL) receives the mean batch loss of each step. */
 int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, const int* region,
                  int steps, int batch, double lr, unsigned long long shuffle_seed, float* loss_history);
+/* Training kernel of fk_mlp_train:
+ *  FK_TRAIN_AUTO   the grid trainer where its cooperative launch fits the device, else per-step launches;
+ *  FK_TRAIN_GRID   all steps in one cooperative launch: per step the CTAs' gradient partials,
+ *                  a grid barrier, Adam on each CTA's slice of the parameters (partials summed
+ *                  in a fixed order), a grid barrier (FK_ERR_ARG where the launch does not fit);
+ *  FK_TRAIN_STEPS  one graph-captured pass + Adam launch pair per step. */
+enum { FK_TRAIN_AUTO = 0, FK_TRAIN_GRID = 1, FK_TRAIN_STEPS = 2 };
+int fk_mlp_set_trainer(fk_ctx* ctx, int mlp_id, int trainer);
 /* forward + input gradient at n points: out[3*n] = (u_hat, du/dx, du/dy) */
 int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, const int* region, double* out);
 /* loss and parameter gradient of mean((u_hat - target)^2) over all n samples, region 0 (FP32 grad) */

@@ -1128,6 +1128,14 @@ int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double*
   return rc;
 }
 
+int fk_mlp_set_trainer(fk_ctx* ctx, int mlp_id, int trainer) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  if (trainer < FK_TRAIN_AUTO || trainer > FK_TRAIN_STEPS) return fail(ctx, FK_ERR_ARG, "unknown trainer");
+  M->trainer = trainer;
+  return FK_OK;
+}
+
 int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, const int* region, double* out) {
   fk::Mlp* M = get_mlp(ctx, mlp_id);
   if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");

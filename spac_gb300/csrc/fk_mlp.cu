@@ -794,7 +794,7 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
   const long long capacity = static_cast<long long>(occ) * sms;
   int rows_per_cta = kRows;
   bool persistent = false;
-  if (coop && steps > 0 && capacity > 0) {
+  if (coop && steps > 0 && capacity > 0 && M.trainer != 2) {
     while (rows_per_cta < batch && batch % (2 * rows_per_cta) == 0 &&
            static_cast<long long>(batch / rows_per_cta) * M.n_regions > capacity)
       rows_per_cta *= 2;
@@ -839,6 +839,10 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
   a.inv_batch = 1.f / batch;
   a.partial = M.d_partial;
   a.loss = M.d_loss;
+  if (M.trainer == 1 && steps > 0 && !persistent) {
+    err = "mlp: the grid trainer needs a cooperative launch that fits the device";
+    return FK_ERR_ARG;
+  }
   if (persistent) {
     if (!M.d_sync && cudaMalloc(&M.d_sync, 2 * sizeof(unsigned)) != cudaSuccess) {
       err = "mlp: training buffers";

@@ -27,6 +27,7 @@ struct Mlp {
   float2* d_table = nullptr;        // grad u_hat on a G x G grid per region
   int table_grid = 0;
   long long adam_t = 0;
+  int trainer = 0;                  // fk_mlp_set_trainer: 0 auto, 1 grid-persistent, 2 per-step graph
   Mlp() = default;
   Mlp(const Mlp&) = delete;
   Mlp& operator=(const Mlp&) = delete;

@@ -18,6 +18,7 @@ FRANKE, MONEGROS, ANISO, DISK = 0, 1, 2, 3
 RECT, CIRCLE = 0, 1
 CV_NONE, CV_EXACT, CV_MLP = 0, 1, 2
 FP64, FP32 = 0, 1
+TRAIN_AUTO, TRAIN_GRID, TRAIN_STEPS = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -102,6 +103,7 @@ _SIGS = {
     "fk_mlp_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int, C.c_int, C.c_double,
                                C.c_ulonglong, _fp]),
     "fk_mlp_eval": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp]),
+    "fk_mlp_set_trainer": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_build_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
     "fk_gmres_csr": (C.c_int, [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, _ip, _dp]),

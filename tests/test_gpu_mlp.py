@@ -145,3 +145,46 @@ def test_learned_cv_unbiased_and_variance_reduced(gpu, orc, fk):
         assert np.all(np.abs(s1["phi_VR"] - s0["phi_VR"]) < 4 * se)
         # the score without the control term is the plain estimator on the same paths
         assert np.allclose(s1["phi"], s0["phi"], rtol=0, atol=4 * np.sqrt(v0 / N).max())
+
+
+def _trainer_run(gpu, fk, orc, trainer, steps, batch, regions=1, seed=5):
+    rects = [(0.0, 0.0, 1.0, 1.0)] if regions == 1 else [(0.0, 0.0, 0.5, 1.0), (0.5, 0.0, 1.0, 1.0)]
+    mid, n = _mlp(gpu, fk, rects, seed=seed)
+    gpu.check(gpu.L.fk_mlp_set_trainer(gpu.h, mid, trainer))
+    rng = np.random.default_rng(3)
+    xy = rng.uniform(0, 1, size=(3000, 2))
+    reg = None if regions == 1 else (xy[:, 0] >= 0.5).astype(np.int32)
+    hist = _train(gpu, fk, mid, xy, _franke(orc, xy), steps=steps, batch=batch, lr=1e-2, region=reg)
+    return hist, _params(gpu, fk, mid, n, regions), mid
+
+
+@pytest.mark.parametrize("batch,regions", [(4096, 1), (2048, 1), (8192, 1), (4096, 2)])
+def test_grid_trainer_follows_step_trainer(gpu, orc, fk, batch, regions):
+    """The persistent grid trainer (one cooperative launch, Adam on each CTA's
+    slice between grid barriers) computes the same steps as the per-step
+    launches: both sum the same CTA partials, in different fixed orders, so
+    losses and parameters agree to that rounding, which Adam's normalised
+    steps amplify only where a gradient component is near zero."""
+    steps = 200
+    h_g, p_g, _ = _trainer_run(gpu, fk, orc, fk.TRAIN_GRID, steps, batch, regions)
+    h_s, p_s, _ = _trainer_run(gpu, fk, orc, fk.TRAIN_STEPS, steps, batch, regions)
+    assert np.all(np.isfinite(h_g)) and np.all(np.isfinite(p_g))
+    assert np.abs(h_g[:5] - h_s[:5]).max() <= 1e-3 * h_s[0]
+    assert np.abs(h_g[-20:].mean() - h_s[-20:].mean()) <= 0.05 * h_s[-20:].mean()
+    assert h_g[-20:].mean() < 0.2 * h_g[:5].mean()
+    scale = np.abs(p_s).max()
+    assert np.median(np.abs(p_g - p_s)) <= 1e-3 * scale
+    assert np.abs(p_g - p_s).max() <= 5e-2 * scale
+
+
+def test_grid_trainer_one_step_matches(gpu, orc, fk):
+    """One Adam step from the same weights: the first step moves each weight
+    by lr g / |g| (bias-corrected Adam), so both trainers give the same update
+    except for components whose gradient is ~0."""
+    _, p_g, _ = _trainer_run(gpu, fk, orc, fk.TRAIN_GRID, 1, 4096)
+    _, p_s, _ = _trainer_run(gpu, fk, orc, fk.TRAIN_STEPS, 1, 4096)
+    mid, n = _mlp(gpu, fk, [(0.0, 0.0, 1.0, 1.0)], seed=5)
+    p0 = _params(gpu, fk, mid, n)
+    d_g, d_s = p_g - p0, p_s - p0
+    same = np.abs(d_g - d_s) <= 1e-6 + 1e-3 * np.abs(d_s)
+    assert same.mean() > 0.99
