@@ -235,12 +235,15 @@ struct SolveSmem {
 };
 
 // out = L0^-1 in (in and out may alias): real DFT in the angle for every
-// radius, the inverse mode matrix per frequency, inverse DFT.
+// radius, the inverse mode matrix per frequency, inverse DFT.  ring_only:
+// `in` is zero off the outer ring (radius 0), so only that radius is
+// transformed and only column 0 of each mode inverse is used.
 __device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, const SolveSmem& m, const double* in,
-                            double* out) {
+                            double* out, bool ring_only) {
   const int nc = D.nc, half = D.half, nm = nc / 2 + 1, tid = threadIdx.x, nt = blockDim.x;
-  for (int idx = tid; idx < nm * half; idx += nt) {
-    const int k = idx / half, j = idx - k * half;
+  const int radii = ring_only ? 1 : half;
+  for (int idx = tid; idx < nm * radii; idx += nt) {
+    const int k = idx / radii, j = idx - k * radii;
     double c = 0.0, s = 0.0;
     int q = 0;
     for (int l = 0; l < nc; ++l) {
@@ -250,15 +253,15 @@ __device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, c
       q += k;
       if (q >= nc) q -= nc;
     }
-    m.C[idx] = c;
-    m.S[idx] = s;
+    m.C[k * half + j] = c;
+    m.S[k * half + j] = s;
   }
   __syncthreads();
   for (int idx = tid; idx < nm * half; idx += nt) {
     const int k = idx / half, i = idx - k * half;
     const double* Mi = minv + (static_cast<long long>(k) * half + i) * half;
     double c = 0.0, s = 0.0;
-    for (int j = 0; j < half; ++j) {
+    for (int j = 0; j < radii; ++j) {
       c += Mi[j] * m.C[k * half + j];
       s += Mi[j] * m.S[k * half + j];
     }
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(kSolveThreads) disk_solve_kernel(const DiskArg
   }
   __syncthreads();
   const double* minv = a.minv + D.minv_off;
-  apply_l0inv(D, minv, m, m.rhs, m.z);
+  apply_l0inv(D, minv, m, m.rhs, m.z, rho > 0);  // the cardinal right-hand sides live on the outer ring
   if (a.varying[d]) {
     const double cb = a.cbar[d];
     const double* cg = a.grid + D.grid_off;
@@ -330,7 +333,7 @@ __global__ void __launch_bounds__(kSolveThreads) disk_solve_kernel(const DiskArg
     for (int it = 0; it < kDiskMaxIter && !done; ++it) {
       for (int q = tid; q < n; q += nt) m.w[q] = (q < nc) ? m.rhs[q] : m.rhs[q] - (cg[q] - cb) * m.z[q];
       __syncthreads();
-      apply_l0inv(D, minv, m, m.w, m.w);
+      apply_l0inv(D, minv, m, m.w, m.w, false);
       double dmax = 0.0, zmax = 0.0;
       for (int q = tid; q < n; q += nt) {
         dmax = fmax(dmax, fabs(m.w[q] - m.z[q]));
