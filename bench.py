@@ -329,7 +329,11 @@ def main():
                              "frac": achieved / fp32_peak, "traffic": traffic,
                              "peak_source": f"nominal FP32: 152 SMs x 128 lanes x 2 flop x {smax:.0f} MHz "
                                             f"(sm_max_mhz of MEASURED_PEAKS.json, {src}); no FP32 figure is measured",
-                             "flops_per_step": FLOPS_PER_STEP},
+                             "flops_per_step": FLOPS_PER_STEP,
+                             # the path kernel is bound by instruction issue: ncu pipe figures of the
+                             # committed capture (profiles/paths_kernel_8x8_assembly.md)
+                             "ncu_pipes": {k[len("paths_kernel_"):]: v for k, v in _read_profile_figures().items()
+                                           if k.startswith("paths_kernel_") and not k.endswith("per_launch")}},
                 "clocks": clocks,
                 "time_to_1e-3": ttt,
                 "cpu_baseline": base}
@@ -479,16 +483,25 @@ def _mean_steps(ctx, mesh, bvp, prec, paths):
     return float(ms.mean())
 
 
-def _read_traffic():
-    """DRAM bytes per path-kernel launch from the committed ncu summary, if present."""
+def _read_profile_figures():
+    """Figures of the committed ncu summary (profiles/traffic.txt): name -> value."""
+    out = {}
     p = os.path.join(ROOT, "profiles", "traffic.txt")
     if os.path.exists(p):
         with open(p) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) == 2 and parts[0] == "paths_kernel_dram_bytes_per_launch":
-                    return float(parts[1])
-    return None
+                if len(parts) == 2 and not parts[0].startswith("#"):
+                    try:
+                        out[parts[0]] = float(parts[1])
+                    except ValueError:
+                        pass
+    return out
+
+
+def _read_traffic():
+    """DRAM bytes per path-kernel launch from the committed ncu summary, if present."""
+    return _read_profile_figures().get("paths_kernel_dram_bytes_per_launch")
 
 
 if __name__ == "__main__":
