@@ -395,7 +395,7 @@ def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
 
 
 def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=500, pilot_h=5e-4, train_steps=1000,
-                   table=128, lr=3e-2, batch=4096):
+                   table=128, lr=3e-2, batch=4096, fit_output=True):
     """Time to `target` RMS node error on the assembly, plain FK vs the learned
     control variate (both FP32 stepping, same h).
 
@@ -404,8 +404,9 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=50
     u.  RMS^2 = bias^2 + mean(var)/N: each method's N comes from an untimed
     calibration run.  The learned-CV time includes its pilot (whole-domain
     point solves at pilot_grid^2 collocation points: boundary data only),
-    training (train_steps Adam steps, batch 4096), the gradient table and the
-    assembly with the control term."""
+    training (train_steps Adam steps, batch 4096; with fit_output the output
+    layer is then refitted by least squares on the hidden features), the
+    gradient table and the assembly with the control term."""
     from spac_gb300 import fk
     info = ctx.mesh_info(mesh)
     row, ixy, stn, fr = ctx.mesh_items(mesh)
@@ -451,6 +452,13 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=50
     ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp), None,
                                  train_steps, batch, lr, 777, hist.ctypes.data_as(fk._fp)))
     t_train = time.perf_counter() - t1
+    t_fit = 0.0
+    if fit_output:
+        # output layer refitted by least squares on the trained hidden layers
+        t3 = time.perf_counter()
+        ctx.check(ctx.L.fk_mlp_fit_output(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp),
+                                          tgt.ctypes.data_as(fk._dp), None, 1e-6))
+        t_fit = time.perf_counter() - t3
     t2 = time.perf_counter()
     ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
     t_table = time.perf_counter() - t2
@@ -461,9 +469,10 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=50
     n_cv = max(32, int(np.ceil(1.05 * var_c.mean() / budget)))
     kc = []
     t_run, stc = _assemble_stats(ctx, mesh, b_cv, n_cv, prec, h, kc)
-    t_cv = t_pilot + t_train + t_table + t_run
+    t_cv = t_pilot + t_train + t_fit + t_table + t_run
     out["learned_cv"] = {"paths_per_item": n_cv, "seconds": t_cv, "rms": rms_of(stc), "pilot_s": t_pilot,
-                         "train_s": t_train, "table_s": t_table, "run_s": t_run, "run_kernels_ms": kc,
+                         "train_s": t_train, "train_steps": train_steps, "fit_output_s": t_fit, "table_s": t_table,
+                         "run_s": t_run, "run_kernels_ms": kc,
                          "pilot_kernel_ms": pilot_kernel_ms,
                          "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
                          "train_loss_first_last": [float(hist[0]), float(hist[-1])]}

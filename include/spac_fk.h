@@ -301,6 +301,14 @@ int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double*
  *  FK_TRAIN_STEPS  one graph-captured pass + Adam launch pair per step. */
 enum { FK_TRAIN_AUTO = 0, FK_TRAIN_GRID = 1, FK_TRAIN_STEPS = 2 };
 int fk_mlp_set_trainer(fk_ctx* ctx, int mlp_id, int trainer);
+/* Fits the output layer (W4, b4) of every region exactly: ridge least
+ * squares of the targets on the current last hidden layer over the given
+ * samples (variable projection; the hidden layers stay as trained).  ridge
+ * is relative to the mean diagonal of the feature Gram matrix (1e-6 is a
+ * good default).  FK_ERR_NUMERIC if the regularised Gram matrix is not
+ * positive definite. */
+int fk_mlp_fit_output(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, const int* region,
+                      double ridge);
 /* forward + input gradient at n points: out[3*n] = (u_hat, du/dx, du/dy) */
 int fk_mlp_eval(fk_ctx* ctx, int mlp_id, int n, const double* xy, const int* region, double* out);
 /* loss and parameter gradient of mean((u_hat - target)^2) over all n samples, region 0 (FP32 grad) */

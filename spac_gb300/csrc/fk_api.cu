@@ -1128,6 +1128,17 @@ int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double*
   return rc;
 }
 
+int fk_mlp_fit_output(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double* target, const int* region,
+                      double ridge) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  if (n < 1 || !xy || !target) return fail(ctx, FK_ERR_ARG, "mlp fit: need samples");
+  cudaSetDevice(ctx->device);
+  const int rc = fk::mlp_fit_output(*M, n, xy, target, region, ridge, ctx->stream, ctx->err);
+  if (rc == FK_OK) M->table_grid = 0;
+  return rc;
+}
+
 int fk_mlp_set_trainer(fk_ctx* ctx, int mlp_id, int trainer) {
   fk::Mlp* M = get_mlp(ctx, mlp_id);
   if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");

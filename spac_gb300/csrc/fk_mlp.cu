@@ -100,6 +100,7 @@ struct PassArgs {
   const float2* points;
   const int* point_region;      // may be null (region 0)
   float* out;                   // [n][3]
+  float* feat;                  // GRADX: if set, the layer-3 activations [n][W] instead (forward only)
 };
 
 struct Smem {
@@ -240,7 +241,10 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
             const float hv = silu_f(c[mt][nt][q] + bias[col], ds);
             Hout[r * LD + col] = __float2bfloat16_rn(hv);
             Sout[r * LD + col] = __float2bfloat16_rn(ds);
-            if (layer == 1) orow[mt][q >> 1] += S.w4[col] * hv;
+            if (layer == 1) {
+              orow[mt][q >> 1] += S.w4[col] * hv;
+              if (a.feat && row0 + r < a.n_points) a.feat[static_cast<long long>(row0 + r) * W + col] = hv;
+            }
           }
       if (layer == 1) {
         // output unit: this warp's column half of each row, reduced over the quad
@@ -256,6 +260,7 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
       }
       __syncthreads();
     }
+    if (a.feat) return;  // features only (uniform over the CTA)
     // ---- output gradient and dp3 = dO * w4 * silu'(p3)
     if (tid < kRows) {
       const int r = tid;
@@ -653,6 +658,92 @@ __global__ void mlp_grid_points(const double* rects, int n_regions, int G, float
   }
 }
 
+// Output-layer least squares: Gram matrix of A = [features, 1] and A^T t.
+// gram: (W + 1) x (W + 2) FP64, row i = (A^T A)[i][0..W], (A^T t)[i]; one
+// CTA per 64 samples adds its FP32 partial with FP64 atomics.
+constexpr int kGramRows = 64;
+constexpr int kGramCols = W + 2;
+__global__ void __launch_bounds__(256) mlp_gram_kernel(const float* feat, const float* tgt, int n, double* gram) {
+  __shared__ float A[kGramRows][W + 2];  // features, 1, target
+  const int r0 = blockIdx.x * kGramRows;
+  for (int e = threadIdx.x; e < kGramRows * (W + 2); e += blockDim.x) {
+    const int r = e / (W + 2), c = e % (W + 2), row = r0 + r;
+    float v = 0.f;
+    if (row < n) v = c < W ? feat[static_cast<long long>(row) * W + c] : (c == W ? 1.f : tgt[row]);
+    A[r][c] = v;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < (W + 1) * kGramCols; e += blockDim.x) {
+    const int i = e / kGramCols, j = e % kGramCols;
+    if (j < W + 1 && j < i) continue;  // lower triangle mirrored by the solver
+    float acc = 0.f;
+    for (int r = 0; r < kGramRows; ++r) acc = fmaf(A[r][i], A[r][j], acc);
+    atomicAdd(&gram[e], static_cast<double>(acc));
+  }
+}
+
+// Ridge solve (A^T A + lambda I) w = A^T t by Cholesky in FP64, lambda =
+// ridge x mean diagonal; writes W4 (w[0..W)) and b4 (w[W]) into the region's
+// FP32 parameters.  flag is set if the matrix is not positive definite.
+__global__ void __launch_bounds__(256) mlp_lsq_kernel(const double* gram, float* params, double ridge, int* flag) {
+  constexpr int N = W + 1;
+  __shared__ double M[N][N + 1];
+  __shared__ double rhs[N];
+  __shared__ double s_lam;
+  __shared__ int s_bad;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    double tr = 0.0;
+    for (int i = 0; i < N; ++i) tr += gram[i * kGramCols + i];
+    s_lam = ridge * tr / N;
+    s_bad = 0;
+  }
+  __syncthreads();
+  for (int e = tid; e < N * N; e += blockDim.x) {
+    const int i = e / N, j = e % N;
+    const double v = (j >= i) ? gram[i * kGramCols + j] : gram[j * kGramCols + i];
+    M[i][j] = v + (i == j ? s_lam : 0.0);
+  }
+  for (int i = tid; i < N; i += blockDim.x) rhs[i] = gram[i * kGramCols + W + 1];
+  __syncthreads();
+  // right-looking Cholesky: M = L L^T, L in the lower triangle
+  for (int k = 0; k < N; ++k) {
+    if (tid == 0) {
+      const double d = M[k][k];
+      if (!(d > 0.0)) s_bad = 1;
+      M[k][k] = sqrt(d > 0.0 ? d : 1.0);
+    }
+    __syncthreads();
+    const double piv = M[k][k];
+    for (int i = k + 1 + tid; i < N; i += blockDim.x) M[i][k] /= piv;
+    __syncthreads();
+    for (int e = tid; e < N * N; e += blockDim.x) {
+      const int i = e / N, j = e % N;
+      if (i > k && j > k && j <= i) M[i][j] -= M[i][k] * M[j][k];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    // L y = rhs, L^T w = y
+    for (int i = 0; i < N; ++i) {
+      double v = rhs[i];
+      for (int j = 0; j < i; ++j) v -= M[i][j] * rhs[j];
+      rhs[i] = v / M[i][i];
+    }
+    for (int i = N - 1; i >= 0; --i) {
+      double v = rhs[i];
+      for (int j = i + 1; j < N; ++j) v -= M[j][i] * rhs[j];
+      rhs[i] = v / M[i][i];
+    }
+    if (s_bad) {
+      atomicOr(flag, 1);
+    } else {
+      for (int i = 0; i < W; ++i) params[OFF_W4 + i] = static_cast<float>(rhs[i]);
+      params[OFF_B4] = static_cast<float>(rhs[W]);
+    }
+  }
+}
+
 __global__ void mlp_pack_table(const float* eval, long long n, float2* table) {
   for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < n;
        e += static_cast<long long>(gridDim.x) * blockDim.x)
@@ -1011,6 +1102,66 @@ int mlp_eval_host(Mlp& M, int n, const double* xy, const int* region, double* ou
       for (int q = 0; q < 3; ++q) res[3 * idx[k] + q] = o[3 * k + q];
   }
   for (size_t i = 0; i < res.size(); ++i) out[i] = res[i];
+  return FK_OK;
+}
+
+int mlp_fit_output(Mlp& M, int n, const double* xy, const double* target, const int* region, double ridge,
+                   cudaStream_t s, std::string& err) {
+  if (!(ridge >= 0.0)) { err = "mlp fit: ridge must be >= 0"; return FK_ERR_ARG; }
+  for (int r = 0; r < M.n_regions; ++r) {
+    std::vector<float2> pts;
+    std::vector<float> tg;
+    for (int i = 0; i < n; ++i)
+      if ((region ? region[i] : 0) == r) {
+        pts.push_back(make_float2(static_cast<float>(xy[2 * i]), static_cast<float>(xy[2 * i + 1])));
+        tg.push_back(static_cast<float>(target[i]));
+      }
+    const int m = static_cast<int>(pts.size());
+    if (m == 0) continue;
+    float2* d_pts = nullptr;
+    float *d_feat = nullptr, *d_tgt = nullptr;
+    double* d_gram = nullptr;
+    int* d_flag = nullptr;
+    cudaError_t e = cudaMalloc(&d_pts, m * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&d_feat, static_cast<size_t>(m) * W * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_tgt, m * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_gram, (W + 1) * kGramCols * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_pts, pts.data(), m * sizeof(float2), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_tgt, tg.data(), m * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_gram, 0, (W + 1) * kGramCols * sizeof(double), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), s);
+    if (e == cudaSuccess) {
+      PassArgs a;
+      std::memset(&a, 0, sizeof(a));
+      a.mode = MODE_GRADX;
+      a.n_regions = 1;
+      a.params = M.d_master + static_cast<size_t>(r) * NPARAM;
+      a.wbf = static_cast<const __nv_bfloat16*>(M.d_bf16) + static_cast<size_t>(r) * BF_PER_REGION;
+      a.norm = M.d_norm + r;
+      a.n_points = m;
+      a.points = d_pts;
+      a.feat = d_feat;
+      e = cudaFuncSetAttribute(mlp_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(sizeof(Smem)));
+      if (e == cudaSuccess) {
+        mlp_pass_kernel<<<(m + kRows - 1) / kRows, kThreads, sizeof(Smem), s>>>(a);
+        mlp_gram_kernel<<<(m + kGramRows - 1) / kGramRows, 256, 0, s>>>(d_feat, d_tgt, m, d_gram);
+        mlp_lsq_kernel<<<1, 256, 0, s>>>(d_gram, M.d_master + static_cast<size_t>(r) * NPARAM, ridge, d_flag);
+        e = cudaGetLastError();
+      }
+    }
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_pts);
+    cudaFree(d_feat);
+    cudaFree(d_tgt);
+    cudaFree(d_gram);
+    cudaFree(d_flag);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+    if (flag) { err = "mlp fit: the feature Gram matrix is not positive definite (raise the ridge)"; return FK_ERR_NUMERIC; }
+  }
   return FK_OK;
 }
 

@@ -44,5 +44,7 @@ int mlp_loss_grad(Mlp& M, int n, const double* xy, const double* target, double*
                   std::string& err);
 int mlp_eval_host(Mlp& M, int n, const double* xy, const int* region, double* out, cudaStream_t s, std::string& err);
 int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err);
+int mlp_fit_output(Mlp& M, int n, const double* xy, const double* target, const int* region, double ridge,
+                   cudaStream_t s, std::string& err);
 
 }  // namespace fk

@@ -188,3 +188,46 @@ def test_grid_trainer_one_step_matches(gpu, orc, fk):
     d_g, d_s = p_g - p0, p_s - p0
     same = np.abs(d_g - d_s) <= 1e-6 + 1e-3 * np.abs(d_s)
     assert same.mean() > 0.99
+
+
+def _loss_grad(gpu, fk, mid, n, xy, tgt):
+    xy = np.ascontiguousarray(xy, dtype=np.float64)
+    tgt = np.ascontiguousarray(tgt, dtype=np.float64)
+    loss = C.c_double()
+    g = np.zeros(n, dtype=np.float32)
+    gpu.check(gpu.L.fk_mlp_loss_grad(gpu.h, mid, len(tgt), xy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp),
+                                     C.byref(loss), g.ctypes.data_as(fk._fp)))
+    return loss.value, g
+
+
+@pytest.mark.parametrize("regions", [1, 2])
+def test_fit_output_layer_is_least_squares(gpu, orc, fk, regions):
+    """After fk_mlp_fit_output the output layer is the (ridge 1e-6) least-squares
+    fit on the hidden features: the loss does not increase, and the loss
+    gradient with respect to W4 and b4 nearly vanishes (what remains is the
+    ridge term and the BF16 rounding of the features in the backward pass),
+    while the hidden layers are untouched."""
+    rects = [(0.0, 0.0, 1.0, 1.0)] if regions == 1 else [(0.0, 0.0, 0.5, 1.0), (0.5, 0.0, 1.0, 1.0)]
+    mid, n = _mlp(gpu, fk, rects, seed=9)
+    rng = np.random.default_rng(4)
+    xy = rng.uniform(0, 1, size=(1500, 2))
+    reg = None if regions == 1 else (xy[:, 0] >= 0.5).astype(np.int32)
+    tgt = _franke(orc, xy)
+    _train(gpu, fk, mid, xy, tgt, steps=200, batch=4096, lr=1e-2, region=reg)
+    p_before = _params(gpu, fk, mid, n, regions)
+    if regions == 1:
+        l0, g0 = _loss_grad(gpu, fk, mid, n, xy, tgt)
+    rp = None if reg is None else np.ascontiguousarray(reg).ctypes.data_as(fk._ip)
+    xyc, tc = np.ascontiguousarray(xy), np.ascontiguousarray(tgt)
+    gpu.check(gpu.L.fk_mlp_fit_output(gpu.h, mid, len(tc), xyc.ctypes.data_as(fk._dp), tc.ctypes.data_as(fk._dp), rp,
+                                      1e-6))
+    p_after = _params(gpu, fk, mid, n, regions)
+    off_w4 = n - 65
+    for r in range(regions):
+        a, b = p_before[r * n:(r + 1) * n], p_after[r * n:(r + 1) * n]
+        assert np.array_equal(a[:off_w4], b[:off_w4])          # hidden layers untouched
+        assert not np.array_equal(a[off_w4:], b[off_w4:])      # output layer refitted
+    if regions == 1:
+        l1, g1 = _loss_grad(gpu, fk, mid, n, xy, tgt)
+        assert l1 <= l0 * (1 + 1e-4)
+        assert np.abs(g1[off_w4:]).max() <= 2e-2 * np.abs(g0[off_w4:]).max()
