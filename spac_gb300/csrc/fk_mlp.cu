@@ -416,15 +416,17 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
       out[OFF_B4] = b4;
     }
   }
-  // loss partial (sum of squared errors of this CTA)
-  __shared__ float red[kThreads];
-  red[tid] = lsum;
+  // loss partial (sum of squared errors of this CTA): warp sums, then the warps in order
+  __shared__ float red[kThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if (lane == 0) red[warp] = lsum;
   __syncthreads();
-  for (int o = kThreads / 2; o > 0; o >>= 1) {
-    if (tid < o) red[tid] += red[tid + o];
-    __syncthreads();
+  if (tid == 0) {
+    float l = red[0];
+    for (int w = 1; w < kThreads / 32; ++w) l += red[w];
+    a.loss[region * a.ctas_per_region + cta] = l;
   }
-  if (tid == 0) a.loss[region * a.ctas_per_region + cta] = red[0];
 }
 
 __global__ void __launch_bounds__(kThreads, 1) mlp_pass_kernel(const PassArgs a) {

@@ -128,7 +128,7 @@ def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp
 
 
 def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_paths=256, max_rounds=6,
-          max_paths=4_000_000, train_steps=2000, table=256):
+          max_paths=4_000_000, train_steps=2000, table=256, lr=1e-2, fit_output=False):
     """Adaptive assembly: per item, paths until SE < se_target, learned control
     variate where it lowers the variance, plain FK otherwise."""
     mesh, t_mesh = _sync_time(lambda: ctx.mesh_square_patches((0, 0, 1, 1), n_sub, nodes_per_side, 0.25, 3.0, 20))
@@ -152,7 +152,10 @@ def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_path
     nx = np.ascontiguousarray(nodes_xy)
     tg = np.ascontiguousarray(est)
     ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tg), nx.ctypes.data_as(fk._dp), tg.ctypes.data_as(fk._dp), None,
-                                 train_steps, 4096, 1e-2, 5, None))
+                                 train_steps, 4096, lr, 5, None))
+    if fit_output:
+        ctx.check(ctx.L.fk_mlp_fit_output(ctx.h, mid, len(tg), nx.ctypes.data_as(fk._dp), tg.ctypes.data_as(fk._dp),
+                                          None, 1e-6))
     ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
     b_cv = ctx.register_bvp(fk.FRANKE, cv=fk.CV_MLP, mlp_id=mid)
     rc = ctx.assemble(mesh, b_cv, 0, h, fk.FP32, paths_per_item=p0, item_G=False, csr=False)
