@@ -2,13 +2,15 @@
 // fk_disk.h):
 //   disk_coef_kernel   per disk: c and -f at the N_c x (N2+1) polar grid
 //                      points, whether c varies over the disk and its mean
-//   disk_modes_kernel  per (disk, Fourier mode k): the (N2+1)^2 mode matrix
-//                      M_k and its inverse (Gauss-Jordan, partial pivoting)
+//   disk_modes_kernel  per (disk, Fourier mode k), one warp: the (N2+1)^2 mode
+//                      matrix M_k and its inverse (Gauss-Jordan, partial pivoting)
 //   disk_solve_kernel  per (disk, right-hand side): the right-hand side of
 //                      PseudoespectralCirculoSolver::Resuelve (-f for B, the
 //                      Fourier cardinal function of one periphery node for
-//                      G, BVP/BVP.cpp:25-29), solved by DFT -> modes ->
-//                      inverse DFT, with Richardson sweeps when c varies
+//                      G, BVP/BVP.cpp:25-29); constant c: kept as a spectrum
+//                      (B: DFT -> modes; G: the outer ring's DFT alone);
+//                      varying c: grid values by DFT -> modes -> inverse DFT
+//                      with Richardson sweeps
 //   disk_interp_kernel per interior node (one warp): the linear functional of
 //                      Interpolador_PS::Interpola at the node, applied to
 //                      every solution of its disk: B, and G = -interpolant;
@@ -30,7 +32,6 @@ namespace fk {
 namespace {
 
 constexpr int kCoefThreads = 256;
-constexpr int kModeThreads = 128;
 constexpr int kSolveThreads = 256;
 constexpr int kInterpSmemBudget = 200 * 1024;
 
@@ -162,22 +163,23 @@ __global__ void __launch_bounds__(kCoefThreads) disk_coef_kernel(const DiskArgs 
 }
 
 // ----------------------------------------------------------------- modes ----
-__global__ void __launch_bounds__(kModeThreads) disk_modes_kernel(const DiskArgs a) {
-  constexpr int kW = 2 * 32 + 1;
-  __shared__ double S[32][kW];
-  __shared__ double fac[32];
-  __shared__ int s_piv;
-  __shared__ double s_pv;
-  const int d = blockIdx.x, k = blockIdx.y;
+// One warp per (disk, mode): M_k and [M_k | I] reduced by Gauss-Jordan with
+// partial pivoting (first maximum wins), rows of `half` doubles in shared memory.
+constexpr int kModeWarps = 8;
+__global__ void __launch_bounds__(32 * kModeWarps) disk_modes_kernel(const DiskArgs a, int max_half) {
+  extern __shared__ double smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int d = blockIdx.x, k = blockIdx.y * kModeWarps + warp;
   const DiskDev D = a.disks[d];
-  if (k > D.nc / 2) return;
-  const int half = D.half, w = 2 * half, tid = threadIdx.x;
+  if (k > D.nc / 2) return;  // whole warp; no block-wide barrier below
+  const int half = D.half, w = 2 * half, ld = 2 * max_half + 1;
+  double* S = smem + static_cast<long long>(warp) * max_half * ld;
   const double* T = a.tab + D.tab_off;
   const double* A1 = T + tab_a1(half);
   const double* A2 = T + tab_a2(half);
   const double* r2inv = T + tab_r2inv(half);
   const double mu = a.tab[D.mu_off + k], sgn = (k & 1) ? -1.0 : 1.0, cb = a.cbar[d];
-  for (int idx = tid; idx < half * w; idx += blockDim.x) {
+  for (int idx = lane; idx < half * w; idx += 32) {
     const int i = idx / w, c = idx - i * w;
     double v;
     if (c < half) {
@@ -186,46 +188,50 @@ __global__ void __launch_bounds__(kModeThreads) disk_modes_kernel(const DiskArgs
     } else {
       v = (c - half == i) ? 1.0 : 0.0;
     }
-    S[i][c] = v;
+    S[i * ld + c] = v;
   }
-  __syncthreads();
+  __syncwarp();
   for (int col = 0; col < half; ++col) {
-    if (tid == 0) {
-      int p = col;
-      double best = fabs(S[col][col]);
-      for (int i = col + 1; i < half; ++i)
-        if (fabs(S[i][col]) > best) { best = fabs(S[i][col]); p = i; }
-      s_piv = p;
-      s_pv = S[p][col];
+    // pivot: the first row of largest |S[i][col]|, i >= col
+    double best = (lane >= col && lane < half) ? fabs(S[lane * ld + col]) : -1.0;
+    int bi = lane;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
     }
-    __syncthreads();
-    if (s_pv == 0.0) {  // uniform: singular mode matrix
-      if (tid == 0) atomicOr(&a.flags[0], 1);
+    const int p = bi;
+    const double pv = S[p * ld + col];
+    if (pv == 0.0) {  // uniform over the warp: singular mode matrix
+      if (lane == 0) atomicOr(&a.flags[0], 1);
       return;
     }
-    const int p = s_piv;
     if (p != col)
-      for (int c = tid; c < w; c += blockDim.x) {
-        const double t = S[col][c];
-        S[col][c] = S[p][c];
-        S[p][c] = t;
+      for (int c = lane; c < w; c += 32) {
+        const double t = S[col * ld + c];
+        S[col * ld + c] = S[p * ld + c];
+        S[p * ld + c] = t;
       }
-    __syncthreads();
-    const double pv = S[col][col];
-    if (tid < half) fac[tid] = S[tid][col];
-    __syncthreads();
-    for (int c = tid; c < w; c += blockDim.x) S[col][c] = S[col][c] / pv;
-    __syncthreads();
-    for (int idx = tid; idx < half * w; idx += blockDim.x) {
-      const int i = idx / w, c = idx - i * w;
-      if (i != col) S[i][c] = S[i][c] - fac[i] * S[col][c];
+    __syncwarp();
+    const double fac = (lane < half) ? S[lane * ld + col] : 0.0;  // column col, after the swap
+    __syncwarp();
+    // columns < col of the left block are already unit vectors: only the
+    // columns from col + 1 on change (column col itself is not read again)
+    const double inv = 1.0 / pv;
+    for (int c = col + 1 + lane; c < w; c += 32) S[col * ld + c] = S[col * ld + c] * inv;
+    __syncwarp();
+    for (int i = 0; i < half; ++i) {
+      const double f = __shfl_sync(0xffffffffu, fac, i);
+      if (i == col) continue;
+      for (int c = col + 1 + lane; c < w; c += 32) S[i * ld + c] = S[i * ld + c] - f * S[col * ld + c];
     }
-    __syncthreads();
+    __syncwarp();
   }
   double* out = a.minv + D.minv_off + static_cast<long long>(k) * half * half;
-  for (int idx = tid; idx < half * half; idx += blockDim.x) {
+  for (int idx = lane; idx < half * half; idx += 32) {
     const int i = idx / half, j = idx - i * half;
-    out[idx] = S[i][half + j];
+    out[idx] = S[i * ld + half + j];
   }
 }
 
@@ -234,14 +240,10 @@ struct SolveSmem {
   double *cosT, *sinT, *rhs, *z, *w, *C, *S, *C2, *S2, *red;
 };
 
-// out = L0^-1 in (in and out may alias): real DFT in the angle for every
-// radius, the inverse mode matrix per frequency, inverse DFT.  ring_only:
-// `in` is zero off the outer ring (radius 0), so only that radius is
-// transformed and only column 0 of each mode inverse is used.
-__device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, const SolveSmem& m, const double* in,
-                            double* out, bool ring_only) {
+// Real DFT in the angle of the first `radii` radii of `in`: C[k][j] =
+// sum_l in(l, j) cos(2 pi k l / N), S[k][j] the same with sin, k = 0 .. N/2.
+__device__ void forward_dft(const DiskDev& D, const SolveSmem& m, const double* in, int radii) {
   const int nc = D.nc, half = D.half, nm = nc / 2 + 1, tid = threadIdx.x, nt = blockDim.x;
-  const int radii = ring_only ? 1 : half;
   for (int idx = tid; idx < nm * radii; idx += nt) {
     const int k = idx / radii, j = idx - k * radii;
     double c = 0.0, s = 0.0;
@@ -257,6 +259,12 @@ __device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, c
     m.S[k * half + j] = s;
   }
   __syncthreads();
+}
+
+// The inverse mode matrix per frequency, using the first `radii` radii of
+// the transform (the others are zero): C2 = M_k^-1 C, S2 = M_k^-1 S.
+__device__ void mode_product(const DiskDev& D, const double* __restrict__ minv, const SolveSmem& m, int radii) {
+  const int nc = D.nc, half = D.half, nm = nc / 2 + 1, tid = threadIdx.x, nt = blockDim.x;
   for (int idx = tid; idx < nm * half; idx += nt) {
     const int k = idx / half, i = idx - k * half;
     const double* Mi = minv + (static_cast<long long>(k) * half + i) * half;
@@ -269,6 +277,11 @@ __device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, c
     m.S2[idx] = s;
   }
   __syncthreads();
+}
+
+// out(l, j) = inverse real DFT of (C2, S2).
+__device__ void inverse_dft(const DiskDev& D, const SolveSmem& m, double* out) {
+  const int nc = D.nc, half = D.half, tid = threadIdx.x, nt = blockDim.x;
   const double inv_n = 1.0 / nc;
   for (int idx = tid; idx < nc * half; idx += nt) {
     const int j = idx / nc, l = idx - j * nc;
@@ -284,6 +297,17 @@ __device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, c
     out[idx] = acc * inv_n;
   }
   __syncthreads();
+}
+
+// out = L0^-1 in (in and out may alias).  ring_only: `in` is zero off the
+// outer ring (radius 0), so only that radius is transformed and only column
+// 0 of each mode inverse is used.
+__device__ void apply_l0inv(const DiskDev& D, const double* __restrict__ minv, const SolveSmem& m, const double* in,
+                            double* out, bool ring_only) {
+  const int radii = ring_only ? 1 : D.half;
+  forward_dft(D, m, in, radii);
+  mode_product(D, minv, m, radii);
+  inverse_dft(D, m, out);
 }
 
 __global__ void __launch_bounds__(kSolveThreads) disk_solve_kernel(const DiskArgs a, int max_nc, int max_half) {
@@ -316,15 +340,48 @@ __global__ void __launch_bounds__(kSolveThreads) disk_solve_kernel(const DiskArg
     for (int q = tid; q < n; q += nt) {
       double v = 0.0;
       if (q < nc) {
+        // sum_{k=-nh}^{nh-1} cos(k del) = 1 + 2 sum_{k=1}^{nh-1} cos(k del) + cos(nh del),
+        // the cosines by rotation from one sincos
         const double del = (q * dt + D.theta0) - ti;
-        for (int k = -nh; k < nh; ++k) v += cos(k * del);
-        v = v / (2 * nh);
+        double s1, c1;
+        sincos(del, &s1, &c1);
+        double ck = 1.0, sk = 0.0, acc = 0.0;
+        for (int k = 1; k <= nh; ++k) {
+          const double cn = ck * c1 - sk * s1;
+          sk = sk * c1 + ck * s1;
+          ck = cn;
+          acc += (k < nh) ? 2.0 * ck : ck;
+        }
+        v = (1.0 + acc) / (2 * nh);
       }
       m.rhs[q] = v;
     }
   }
   __syncthreads();
   const double* minv = a.minv + D.minv_off;
+  if (!a.varying[d]) {
+    // constant c: the solution is kept as its spectrum.  B: (C2, S2) over
+    // all radii; a periphery right-hand side (zero off the outer ring): the
+    // ring's transform (C, S) alone, its mode products are folded into the
+    // interpolation (disk_interp_kernel)
+    double* so = a.z + D.z_off + static_cast<long long>(rho) * D.zstride;
+    const int nm = nc / 2 + 1;
+    if (rho == 0) {
+      forward_dft(D, m, m.rhs, half);
+      mode_product(D, minv, m, half);
+      for (int q = tid; q < nm * half; q += nt) {
+        so[q] = m.C2[q];
+        so[nm * half + q] = m.S2[q];
+      }
+    } else {
+      forward_dft(D, m, m.rhs, 1);
+      for (int k = tid; k < nm; k += nt) {
+        so[k] = m.C[k * half];
+        so[nm + k] = m.S[k * half];
+      }
+    }
+    return;
+  }
   apply_l0inv(D, minv, m, m.rhs, m.z, rho > 0);  // the cardinal right-hand sides live on the outer ring
   if (a.varying[d]) {
     const double cb = a.cbar[d];
@@ -351,7 +408,7 @@ __global__ void __launch_bounds__(kSolveThreads) disk_solve_kernel(const DiskArg
     }
     if (!done && tid == 0) atomicOr(&a.flags[1], 1);
   }
-  double* zo = a.z + D.z_off + static_cast<long long>(rho) * n;
+  double* zo = a.z + D.z_off + static_cast<long long>(rho) * D.zstride;
   for (int q = tid; q < n; q += nt) zo[q] = m.z[q];
 }
 
@@ -382,6 +439,63 @@ __global__ void disk_interp_kernel(const DiskArgs a, long long n_inner, int max_
   const double rp = sqrt(dx * dx + dy * dy) / D.radius;
   double tp = atan2(dy, dx);
   tp = (tp >= 0) ? tp : tp + 2.0 * M_PI;
+  const double* T = a.tab + D.tab_off;
+  double sw = 0.0;
+  for (int i = lane; i < m; i += 32) {
+    const double wi = T[tab_bw(half) + i] / (rp - T[tab_diam(half) + i]);
+    wv[i] = wi;
+    sw += wi;
+  }
+  sw = warp_sum(sw);
+  const double scale = (1.0 / nc) / sw;
+  const int np = D.n_periph;
+  __syncwarp();
+  if (!a.varying[d]) {
+    // Spectral form (constant c).  With z's transform (C2_k(j), S2_k(j)),
+    // sum_l z(l,j) F_l = sum_{k=0}^{N/2} e_k (C2_k(j) cos k phi + S2_k(j) sin k phi)
+    // (e_k = 2 for 0 < k < N/2, else 1; phi = theta_p - theta_0) and F'_l adds
+    // (-1)^k, so value = scale sum_{k,j} a_k(j) (C2 cos k phi + S2 sin k phi)
+    // with a_k(j) = e_k (w_{m-1-j} + (-1)^k w_j).  A periphery right-hand side
+    // has C2_k(j) = M_k^-1(j,0) C_k (its ring transform), so its value is
+    // sum_k b_k (C_k cos k phi + S_k sin k phi), b_k = scale sum_j a_k(j) M_k^-1(j,0).
+    const int nm = nh + 1;
+    const double phi = tp - D.theta0;
+    for (int k = lane; k < nm; k += 32) sincos(k * phi, &Fp[k], &Fv[k]);
+    __syncwarp();
+    const double* sb = a.z + D.z_off;
+    double acc = 0.0;
+    for (int q = lane; q < nm * half; q += 32) {
+      const int k = q / half, j = q - k * half;
+      const double e = (k == 0 || k == nh) ? 1.0 : 2.0;
+      const double al = e * (wv[m - 1 - j] + ((k & 1) ? -wv[j] : wv[j]));
+      acc += al * (sb[q] * Fv[k] + sb[nm * half + q] * Fp[k]);
+    }
+    acc = warp_sum(acc) * scale;
+    if (lane == 0) {
+      if (a.B) a.B[D.inner_off + p] = acc;
+      if (a.Bcsr) atomicAdd(&a.Bcsr[a.inner_row[node]], acc);
+    }
+    const double* minv = a.minv + D.minv_off;
+    for (int k = lane; k < nm; k += 32) {
+      const double e = (k == 0 || k == nh) ? 1.0 : 2.0;
+      double b = 0.0;
+      for (int j = 0; j < half; ++j)
+        b += (wv[m - 1 - j] + ((k & 1) ? -wv[j] : wv[j])) * minv[(static_cast<long long>(k) * half + j) * half];
+      b *= e * scale;
+      aco[k] = b * Fv[k];
+      aco[nm + k] = b * Fp[k];
+    }
+    __syncwarp();
+    for (int rho = 1 + lane; rho <= np; rho += 32) {
+      const double* sr = a.z + D.z_off + static_cast<long long>(rho) * D.zstride;
+      double v = 0.0;
+      for (int k = 0; k < nm; ++k) v += aco[k] * sr[k] + aco[nm + k] * sr[nm + k];
+      const long long g = D.g_off + p * np + (rho - 1);
+      if (a.G) a.G[g] = -v;
+      if (a.val) atomicAdd(&a.val[a.csr_pos[g]], -v);
+    }
+    return;
+  }
   const double dt = 2 * M_PI / nc;
   for (int l = lane; l < nc; l += 32) {
     double s1, c1;
@@ -398,24 +512,14 @@ __global__ void disk_interp_kernel(const DiskArgs a, long long n_inner, int max_
     Fv[l] = F;
     Fp[l] = G;
   }
-  const double* T = a.tab + D.tab_off;
-  double sw = 0.0;
-  for (int i = lane; i < m; i += 32) {
-    const double wi = T[tab_bw(half) + i] / (rp - T[tab_diam(half) + i]);
-    wv[i] = wi;
-    sw += wi;
-  }
-  sw = warp_sum(sw);
   __syncwarp();
   for (int q = lane; q < n; q += 32) {
     const int j = q / nc, l = q - j * nc;
     aco[q] = Fv[l] * wv[m - 1 - j] + Fp[l] * wv[j];
   }
   __syncwarp();
-  const double scale = (1.0 / nc) / sw;
-  const int np = D.n_periph;
   for (int rho = 0; rho <= np; ++rho) {
-    const double* zr = a.z + D.z_off + static_cast<long long>(rho) * n;
+    const double* zr = a.z + D.z_off + static_cast<long long>(rho) * D.zstride;
     double acc = 0.0;
     for (int q = lane; q < n; q += 32) acc += aco[q] * zr[q];
     acc = warp_sum(acc);
@@ -491,8 +595,10 @@ bool disk_prepare(const std::vector<DiskHost>& in, DiskBatch& out, std::string& 
     out.grid_total += 2 * n;
     D.minv_off = out.minv_total;
     out.minv_total += static_cast<long long>(D.nc / 2 + 1) * D.half * D.half;
+    // per right-hand side: grid values (varying c) or the spectrum (constant c)
+    D.zstride = std::max(n, 2LL * (D.nc / 2 + 1) * D.half);
     D.z_off = out.z_total;
-    out.z_total += (np + 1) * n;
+    out.z_total += (np + 1) * D.zstride;
     D.inner_off = inner;
     D.g_off = g;
     D.periph_off = periph;
@@ -528,7 +634,12 @@ cudaError_t disk_launch(int problem, const DiskArgs& a, const DiskBatch& b, cuda
     case 2: disk_coef_kernel<2><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
     default: disk_coef_kernel<3><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
   }
-  disk_modes_kernel<<<dim3(a.n_disks, b.max_modes), kModeThreads, 0, s>>>(a);
+  const size_t mode_smem = static_cast<size_t>(kModeWarps) * b.max_half * (2 * b.max_half + 1) * sizeof(double);
+  cudaError_t em = cudaFuncSetAttribute(disk_modes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(mode_smem));
+  if (em != cudaSuccess) return em;
+  disk_modes_kernel<<<dim3(a.n_disks, (b.max_modes + kModeWarps - 1) / kModeWarps), 32 * kModeWarps, mode_smem, s>>>(
+      a, b.max_half);
   const size_t max_n = static_cast<size_t>(b.max_nc) * b.max_half;
   const size_t max_nm = static_cast<size_t>(b.max_nc / 2 + 1) * b.max_half;
   const size_t solve_smem = (2 * b.max_nc + 3 * max_n + 4 * max_nm + 64) * sizeof(double);

@@ -53,7 +53,8 @@ struct DiskDev {
   long long mu_off;     // mu_k, k = 0 .. nc/2
   long long grid_off;   // c and -f at the grid points, 2 x nc*half
   long long minv_off;   // (nc/2 + 1) x half x half
-  long long z_off;      // (n_periph + 1) x nc*half solutions
+  long long z_off;      // (n_periph + 1) solutions of zstride doubles
+  long long zstride;    // max(nc*half, 2 (nc/2 + 1) half): grid values or spectrum
   long long inner_off;  // first interior node of the disk (in the batch)
   long long g_off;      // first G entry (n_inner x n_periph)
   long long periph_off; // first periphery angle
