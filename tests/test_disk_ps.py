@@ -214,3 +214,26 @@ def test_gpu_serial_driver_pipeline_solves_franke(gpu, fk):
     xy, _ = gpu.mesh_nodes(mesh)
     err = x - franke(xy[:, 0], xy[:, 1])
     assert np.sqrt(np.mean(err ** 2)) < 1e-2 and np.abs(err).max() < 5e-2, (np.sqrt(np.mean(err ** 2)), np.abs(err).max())
+
+
+@pytest.mark.gpu
+def test_gpu_ps_disk_periphery_off_grid(gpu, fk, orc):
+    """Constant c (spectral path) with periphery nodes that are not the grid
+    angles and fewer of them than grid angles (n_periph = 12, N_c = 16): the
+    cardinal right-hand sides are general ring data; against the oracle."""
+    rng = np.random.default_rng(8)
+    cx, cy, R, nc, nr, th0 = 0.45, 0.55, 0.25, 16, 11, 0.3
+    th = 0.05 + 2 * np.pi * np.arange(12) / 12 + 0.02 * rng.standard_normal(12)
+    rr = 0.9 * R * np.sqrt(rng.random(20))
+    aa = 2 * np.pi * rng.random(20)
+    xy = np.stack([cx + rr * np.cos(aa), cy + rr * np.sin(aa)], 1)
+    for problem, dom in ((fk.FRANKE, (0, 0, 1, 1)), (fk.MONEGROS, (-200, -200, 200, 200))):
+        c = (cx, cy, R) if problem == fk.FRANKE else (-72.0, -38.0, 5.0)
+        pts = xy if problem == fk.FRANKE else np.stack([c[0] + (xy[:, 0] - cx) * 20, c[1] + (xy[:, 1] - cy) * 20], 1)
+        b = gpu.register_bvp(problem, dom=dom)
+        (G, B), = gpu.solve_disks_ps(b, [dict(cx=c[0], cy=c[1], radius=c[2], theta0=th0, n_circle=nc, n_radial=nr,
+                                              periph_theta=th, inner_xy=pts)])
+        Go, Bo = orc.ps_disk(orc.bvp(problem, dom=dom), c[0], c[1], c[2], nc, nr, th0, th, pts)
+        tol = ps_tol(nc, nr)
+        assert np.abs(G - Go).max() <= tol * np.abs(Go).max(), problem
+        assert np.abs(B - Bo).max() <= tol * np.abs(Bo).max(), problem
