@@ -46,12 +46,15 @@ constexpr int W = 64;
 // warps per CTA, warp w owning the 16 rows 16 (w % 2).. and the 16 columns
 // 16 (w / 2).. of every 64-wide product; two warps share each SM
 // sub-partition to hide latencies.
-constexpr int kRows = 32;
+#ifndef FK_MLP_ROWS
+#define FK_MLP_ROWS 32
+#endif
+constexpr int kRows = FK_MLP_ROWS;
 constexpr int kThreads = 256;
 constexpr int kRowGroups = kRows / 16;
 constexpr int kWarpRows = kRows / kRowGroups;
 constexpr int kMT = kWarpRows / 16;  // m16 tiles per warp
-constexpr int kNT = 2;               // n8 tiles per warp (16 columns)
+constexpr int kNT = kRows / 16;      // n8 tiles per warp (8 warps = row groups x column groups)
 constexpr int kColsPerWarp = 8 * kNT;
 constexpr int kColGroups = W / kColsPerWarp;
 constexpr int kQuarters = kThreads / W;  // row groups of the per-column sums
