@@ -18,10 +18,13 @@
 
 namespace fk {
 
-// device buffer that grows and never shrinks
+// device buffer that grows and never shrinks; owns its allocation (not copyable)
 struct DBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
   cudaError_t ensure(size_t n) {
     if (n <= bytes) return cudaSuccess;
     if (p) cudaFree(p);
