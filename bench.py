@@ -325,6 +325,7 @@ def main():
                 "gpu_launches": 2 * args.steps,
                 "kernels_ms": {"paths": k_ms, "finalize_scatter": f_ms},
                 "mean_steps_per_path": steps_per_assembly,
+                "roofline_scatter": _scatter_roofline(info, f_ms, peaks, src),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                              "frac": achieved / fp32_peak, "traffic": traffic,
                              "peak_source": f"nominal FP32: 152 SMs x 128 lanes x 2 flop x {smax:.0f} MHz "
@@ -490,6 +491,25 @@ def _mean_steps(ctx, mesh, bvp, prec, paths):
     ctx.check(rc)
     ms = np.array([s.mean_steps for s in st])
     return float(ms.mean())
+
+
+def _scatter_roofline(info, f_ms, peaks, src):
+    """HBM roofline of the finalize/scatter kernel.  Algorithmic bytes per
+    launch: per item its FP64 stencil moments (nwin x k words of the patch's
+    windows), its 12 FP64 statistics, a read-modify-write of its G entries in
+    the CSR values (16 B each) and of its B (16 B); per patch the FP32 window
+    corrections E_W (nwin x k^2) read once."""
+    k = CFG["knn"]
+    m = info["max_stencil"]            # patch-boundary nodes = windows of a closed chain
+    per_item = m * k * 8 + 12 * 8 + m * 16 + 16
+    per_patch = m * k * k * 4
+    bytes_ = info["n_items"] * per_item + info["n_stencils"] * per_patch
+    achieved = bytes_ / (f_ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs", 6800.0)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": _read_profile_figures().get("finalize_dram_bytes_per_launch"), "algorithmic_bytes": bytes_,
+            "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({src})",
+            "note": "latency-bound: per-item FP64 reductions and CSR atomics (profiles/)"}
 
 
 def _read_profile_figures():
