@@ -45,8 +45,15 @@ extern "C" {
  *                      b = (y - 1/2, 1/2 - x), c = -(1 + x^2 + y^2),
  *                      u = Franke (1 + x y), f = -(L u)
  *  FK_PROBLEM_DISK     Franke rescaled to the disk (prob = cx, cy, R):
- *                      u(x) = Franke((x - c)/(2R) + 1/2), sigma = 1.41421356237 I */
-enum { FK_PROBLEM_FRANKE = 0, FK_PROBLEM_MONEGROS = 1, FK_PROBLEM_ANISO = 2, FK_PROBLEM_DISK = 3 };
+ *                      u(x) = Franke((x - c)/(2R) + 1/2), sigma = 1.41421356237 I
+ *  FK_PROBLEM_ROBIN    FK_PROBLEM_ANISO with reflecting rectangle sides: the
+ *                      reflecting step Paso_Reflejante (Solvers/FeynmanKacSolver.cpp:19-67)
+ *                      where Frontera::Absorbente is false (BVP/Frontera.hpp:23-36).
+ *                      prob[0] = side mask (1: x = x0, 2: y = y0, 4: x = x1, 8: y = y1),
+ *                      prob[1] = varphi (Y += varphi Y dL), prob[2] = rho (the
+ *                      reflecting step runs within rho of the side); psi =
+ *                      d_n u - varphi u (Z += psi Y dL), so u is the exact solution. */
+enum { FK_PROBLEM_FRANKE = 0, FK_PROBLEM_MONEGROS = 1, FK_PROBLEM_ANISO = 2, FK_PROBLEM_DISK = 3, FK_PROBLEM_ROBIN = 4 };
 /* Frontera distance functors: Dominios/Rectangulo.hpp:7-229 (x0,y0,x1,y1) and
  * Dominios/Circulo.hpp:7-22 (r,cx,cy). */
 enum { FK_SHAPE_RECT = 0, FK_SHAPE_CIRCLE = 1 };

@@ -23,8 +23,13 @@
 // CPU path.  Frontera::parametros are passed as they are: (x0, y0, x1, y1)
 // for rectangles, (r, cx, cy) for circles.  A subdomain Frontera whose
 // distance function is not registered is treated as "no subdomain" (point
-// solves stop at the domain boundary).  rho is accepted and unused: it only
-// enters the reference's reflecting step, which absorbing BVPs never take.
+// solves stop at the domain boundary).
+// Reflecting sides: on a rectangular domain, Frontera::Absorbente is
+// evaluated at the midpoint of each side (the device functors take one
+// boundary type per side); sides where it is false reflect, which needs a u
+// registered as FK_PROBLEM_ROBIN (prob[1] = varphi).  The side mask and the
+// call's rho (the width of the zone where the reflecting step runs) are then
+// passed in prob[0] and prob[2]; absorbing problems ignore rho.
 #ifndef SPAC_FK_GPU_HPP
 #define SPAC_FK_GPU_HPP
 #include <cmath>
@@ -33,6 +38,7 @@
 #include <stdexcept>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "spac_fk.h"
@@ -58,6 +64,33 @@ std::uintptr_t key_of(Fn f) {
   return reinterpret_cast<std::uintptr_t>(f);
 }
 
+// argument type of a boundary-type predicate (Frontera::pftipo)
+template <class T>
+struct predicate_arg;
+template <class R, class A>
+struct predicate_arg<R (*)(A)> {
+  using type = typename std::decay<A>::type;
+};
+
+// Reflecting sides of a rectangular domain (x0, y0, x1, y1): bit s set where
+// Frontera::Absorbente is false at the midpoint of side s (0: x = x0,
+// 1: y = y0, 2: x = x1, 3: y = y1; Frontera.hpp:23-36).
+template <class FronteraT>
+int reflecting_sides(const FronteraT& fr, const double d[4]) {
+  if (!fr.Absorbente) return 0;
+  using V = typename predicate_arg<decltype(fr.Absorbente)>::type;
+  const double mid[4][2] = {{d[0], 0.5 * (d[1] + d[3])}, {0.5 * (d[0] + d[2]), d[1]},
+                            {d[2], 0.5 * (d[1] + d[3])}, {0.5 * (d[0] + d[2]), d[3]}};
+  int mask = 0;
+  for (int s = 0; s < 4; ++s) {
+    V p;
+    p[0] = mid[s][0];
+    p[1] = mid[s][1];
+    if (!fr.Absorbente(p)) mask |= 1 << s;
+  }
+  return mask;
+}
+
 // Frontera -> (shape, parameters) through the distance registry.
 template <class FronteraT>
 bool shape_of(const FronteraT& fr, int* shape, double p[4], bool required) {
@@ -79,7 +112,7 @@ bool shape_of(const FronteraT& fr, int* shape, double p[4], bool required) {
 // (the exact-gradient control variate when it is the registered F_exact).
 // need_domain: the domain's distance function must be registered.
 template <class BVPT>
-fk_bvp_desc describe_bvp(const BVPT& P, bool need_domain) {
+fk_bvp_desc describe_bvp(const BVPT& P, bool need_domain, double rho = 0.0) {
   auto& reg = problem_registry();
   const auto f = reg.find(key_of(P.u.funcion));
   if (f == reg.end()) throw std::runtime_error("spac_fk_gpu: unregistered BVP (its u function)");
@@ -96,6 +129,13 @@ fk_bvp_desc describe_bvp(const BVPT& P, bool need_domain) {
     for (int i = 0; i < 4; ++i) d.dom[i] = (d.dom_shape == FK_SHAPE_CIRCLE) ? unit_circle[i] : unit_rect[i];
   }
   for (int i = 0; i < 4; ++i) d.prob[i] = b.prob[i];
+  const int mask = d.dom_shape == FK_SHAPE_RECT ? reflecting_sides(P.frontera_dominio, d.dom) : 0;
+  if (mask != 0 && b.problem != FK_PROBLEM_ROBIN)
+    throw std::runtime_error("spac_fk_gpu: reflecting domain sides need a problem registered as FK_PROBLEM_ROBIN");
+  if (b.problem == FK_PROBLEM_ROBIN) {
+    d.prob[0] = mask;
+    d.prob[2] = rho;
+  }
   return d;
 }
 
@@ -143,8 +183,7 @@ class FeynmanKacSolverGPU {
   template <class Vec2, class BVPT>
   void Solve_OMP_Analytic(const Vec2& X0, unsigned int numero_trayectorias, double discretizacion_temporal,
                           double rho, const BVPT& Problema) {
-    (void)rho;
-    const int bvp = bvp_id(Problema);
+    const int bvp = bvp_id(Problema, rho);
     int sub_shape = -1;
     double sub[4] = {0, 0, 0, 0};
     const bool has_sub = shape_of(Problema.frontera_subdominio, &sub_shape, sub, false);
@@ -161,8 +200,7 @@ class FeynmanKacSolverGPU {
   template <class NudoT, class BVPT, class InterfazT>
   void Solve_OMP_Analytic(NudoT& nudo, unsigned int numero_trayectorias, double discretizacion_temporal, double rho,
                           const BVPT& Problema, const InterfazT& interfaz) {
-    (void)rho;
-    const int bvp = bvp_id(Problema);
+    const int bvp = bvp_id(Problema, rho);
     const int n = static_cast<int>(interfaz.nudos_circunferencia.size());
     std::vector<double> theta(n);
     std::vector<int> gids(n);
@@ -206,8 +244,8 @@ class FeynmanKacSolverGPU {
   }
 
   template <class BVPT>
-  int bvp_id(const BVPT& P) {
-    const fk_bvp_desc d = spac_fk_gpu::describe_bvp(P, true);
+  int bvp_id(const BVPT& P, double rho) {
+    const fk_bvp_desc d = spac_fk_gpu::describe_bvp(P, true, rho);
     const auto key = std::make_tuple(d.problem, d.cv, d.dom_shape, d.dom[0], d.dom[1], d.dom[2], d.dom[3], d.prob[0],
                                      d.prob[1], d.prob[2], d.prob[3]);
     const auto it = bvps_.find(key);

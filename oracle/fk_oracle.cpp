@@ -9,6 +9,7 @@
 #include "fk_oracle.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -273,7 +274,7 @@ Coef coefficients(const orc_bvp* B, double x, double y) {
       M2 nt{-c.s.a00, -c.s.a10, -c.s.a01, -c.s.a11};
       c.F = mul(nt, gr);
     }
-  } else if (B->problem == ORC_PROBLEM_ANISO) {
+  } else if (B->problem == ORC_PROBLEM_ANISO || B->problem == ORC_PROBLEM_ROBIN) {
     Franke fr(x, y);
     double q = 1.0 + x * y;
     double F = fr.u(), Fx = fr.dudx(), Fy = fr.dudy(), Fxx = fr.d2udx2(), Fyy = fr.d2udy2();
@@ -321,7 +322,7 @@ Coef coefficients(const orc_bvp* B, double x, double y) {
 
 // sigma alone (the same expressions as in coefficients())
 M2 sigma_of(const orc_bvp* B, double x, double y) {
-  if (B->problem == ORC_PROBLEM_ANISO) {
+  if (B->problem == ORC_PROBLEM_ANISO || B->problem == ORC_PROBLEM_ROBIN) {
     double s = std::sqrt(2.0 * aniso_a(x, y));
     return M2{1.0 * s, 0.0 * s, 0.0 * s, 1.0 * s};
   }
@@ -347,11 +348,175 @@ int dentro(const orc_bvp* B, int sub_shape, const double* sub, V2 X, double sqrt
   return (d < kGobet * norm(tmul(N, s)) * sqrth) ? ORC_OUT_INSIDE : ORC_OUT_SUBDOMAIN;
 }
 
+// ---------------------------------------------------- reflecting sides -----
+// ORC_PROBLEM_ROBIN: psi = d_n u - varphi u at a boundary point with outward
+// normal n (u = Franke (1 + x y)), so u solves the Robin problem.
+double robin_psi(const orc_bvp* B, double x, double y, double nx, double ny) {
+  Franke fr(x, y);
+  double q = 1.0 + x * y;
+  double F = fr.u();
+  double ux = fr.dudx() * q + F * y, uy = fr.dudy() * q + F * x;
+  return nx * ux + ny * uy - B->prob[1] * (F * q);
+}
+
+// Whether the domain can ever win Dentro's comparison: not when the
+// subdomain lies strictly inside the rectangular domain (its distance is
+// then always the larger).  Reflection only happens where it can.
+bool dom_can_win(const orc_bvp* B, int sub_shape, const double* s) {
+  const double* d = B->dom;
+  if (B->dom_shape != ORC_SHAPE_RECT) return true;
+  if (sub_shape == ORC_SHAPE_CIRCLE)
+    return !(s[1] - s[0] > d[0] && s[1] + s[0] < d[2] && s[2] - s[0] > d[1] && s[2] + s[0] < d[3]);
+  return !(s[0] > d[0] && s[1] > d[1] && s[2] < d[2] && s[3] < d[3]);
+}
+
+// Dentro's nearest boundary at X, if it is a reflecting side of the domain
+// (0: x = x0, 1: y = y0, 2: x = x1, 3: y = y1; -1 otherwise), and the domain
+// distance.
+int robin_side(const orc_bvp* B, int sub_shape, const double* sub, int mask, V2 X, double* dist) {
+  V2 pa, na, ps, ns;
+  double da = shape_dist(B->dom_shape, B->dom, X, pa, na);
+  double d = shape_dist(sub_shape, sub, X, ps, ns);
+  *dist = da;
+  if (!(da >= d)) return -1;
+  int side = (na.x == -1.0) ? 0 : (na.y == -1.0) ? 1 : (na.x == 1.0) ? 2 : (na.y == 1.0) ? 3 : -1;
+  return (side >= 0 && ((mask >> side) & 1)) ? side : -1;
+}
+
+// One path: Simulacion_OMP loop body (FeynmanKacSolver.cpp:161-194) with
+// Paso_Absorbente (:7-18), and for ORC_PROBLEM_ROBIN the reflecting step
+// Paso_Reflejante (:19-67) near reflecting sides.  The reference's reflecting
+// step reads two uninitialised values (the proposal's projection Nprop in
+// its loop test, :46, and dist_k on a path's first step, :158), draws
+// omega ~ Exp(1) where its comment states mean 2h (:33) and clamps an inside
+// distance to zero (:39); it is restated as the scheme it implements,
+// Lepingle's reflected Euler step: on every reflecting side within rho of
+// the current point, the push-back is the exact maximum of the Brownian
+// bridge of the normal displacement, 1/2 (uc + sqrt(uc^2 + 2 s^2 h E)),
+// E ~ Exp(1), started from the point's distance to the side (the normals
+// are coordinate axes and sigma = s I, so corner pushes are independent).
+// A reflecting side crossed all the same puts the path back on it with the
+// overshoot as local time (:49-58); psi is taken at the side's point nearest
+// the new position.  The Exp(1) variate of side q is word q of Philox counter
+// (2^31 | k, path, item, stream).
+int simulate_robin(Session& S, const orc_bvp* B, int sub_shape, const double* sub, double x0, double y0,
+                   double h, uint32_t item, uint32_t path, int max_steps, orc_exit* out) {
+  if (S.mode != ORC_RNG_PHILOX) return -2;
+  double sqrth = std::sqrt(h);
+  V2 X{x0, y0}, proj{0, 0}, N{0, 0};
+  double Y = 1, Z = 0, xi = 0, t = 0;
+  const double* d = B->dom;
+  const int mask = dom_can_win(B, sub_shape, sub) ? (static_cast<int>(B->prob[0]) & 15) : 0;
+  const double rphi = B->prob[1], rho = B->prob[2];
+  dentro(B, sub_shape, sub, X, sqrth, proj, N);
+  int status = ORC_OUT_INSIDE, k = 0;
+  const uint32_t key[2] = {static_cast<uint32_t>(S.seed), static_cast<uint32_t>(S.seed >> 32)};
+  do {
+    Coef c = coefficients(B, X.x, X.y);
+    double dW[2];
+    increment(S, item, path, k, sqrth, dW);
+    V2 inc{dW[0], dW[1]};
+    const double s = c.s.a00;  // sigma = s I
+    double xn = X.x + (c.b.x * h + s * dW[0]), yn = X.y + (c.b.y * h + s * dW[1]);
+    double lt[4] = {0.0, 0.0, 0.0, 0.0}, ploc = 0.0, vloc = 0.0;
+    if (mask) {
+      uint32_t r[4] = {0, 0, 0, 0};
+      bool drawn = false;
+      for (int q = 0; q < 4; ++q) {
+        if (!((mask >> q) & 1)) continue;
+        double dq = q == 0 ? d[0] - X.x : (q == 1 ? d[1] - X.y : (q == 2 ? X.x - d[2] : X.y - d[3]));
+        if (!(dq > -rho)) continue;
+        if (!drawn) {
+          uint32_t ctr[4] = {0x80000000u | static_cast<uint32_t>(k), path, item, S.stream};
+          philox(ctr, key, r);
+          drawn = true;
+        }
+        double E = -std::log((static_cast<double>(r[q]) + 0.5) * kInv32);
+        double nx = q == 0 ? -1.0 : (q == 2 ? 1.0 : 0.0);
+        double ny = q == 1 ? -1.0 : (q == 3 ? 1.0 : 0.0);
+        double uc = s * (nx * dW[0] + ny * dW[1]) + (nx * c.b.x + ny * c.b.y) * h;
+        double nu = 0.5 * (uc + std::sqrt(uc * uc + 2.0 * s * s * h * E));
+        double L = std::max(0.0, nu + std::min(dq, 0.0));
+        xn -= L * nx;
+        yn -= L * ny;
+        lt[q] = L;
+      }
+      for (int q = 0; q < 4; ++q) {
+        if (!((mask >> q) & 1)) continue;
+        double o = q == 0 ? d[0] - xn : (q == 1 ? d[1] - yn : (q == 2 ? xn - d[2] : yn - d[3]));
+        if (o > 0.0) {
+          if (q == 0) xn = d[0]; else if (q == 1) yn = d[1]; else if (q == 2) xn = d[2]; else yn = d[3];
+          lt[q] += o;
+        }
+      }
+      for (int q = 0; q < 4; ++q) {
+        if (lt[q] > 0.0) {
+          double px = q == 0 ? d[0] : (q == 2 ? d[2] : std::min(std::max(xn, d[0]), d[2]));
+          double py = q == 1 ? d[1] : (q == 3 ? d[3] : std::min(std::max(yn, d[1]), d[3]));
+          double nx = q == 0 ? -1.0 : (q == 2 ? 1.0 : 0.0);
+          double ny = q == 1 ? -1.0 : (q == 3 ? 1.0 : 0.0);
+          ploc += robin_psi(B, px, py, nx, ny) * lt[q];
+          vloc += rphi * lt[q];
+        }
+      }
+    }
+    Z += c.f * Y * h + ploc * Y;
+    xi += Y * dot(c.F, inc);
+    Y += c.c * Y * h + vloc * Y;
+    X.x = xn;
+    X.y = yn;
+    t += h;
+    ++k;
+    status = dentro(B, sub_shape, sub, X, sqrth, proj, N);
+    double dd;
+    if (mask && robin_side(B, sub_shape, sub, mask, X, &dd) >= 0) {
+      // the nearest boundary reflects: no stop there (dentro / reflejada,
+      // :82-84), but a stop within the Gobet band of the nearer of the
+      // subdomain and the absorbing sides
+      double da = -FLT_MAX;
+      int qa = -1;
+      for (int q = 0; q < 4; ++q) {
+        if ((mask >> q) & 1) continue;
+        double dq = q == 0 ? d[0] - X.x : (q == 1 ? d[1] - X.y : (q == 2 ? X.x - d[2] : X.y - d[3]));
+        if (dq > da) { da = dq; qa = q; }
+      }
+      int cand = ORC_OUT_DOMAIN;
+      V2 pc{0, 0};
+      if (qa >= 0) {
+        pc.x = qa == 0 ? d[0] : (qa == 2 ? d[2] : std::min(std::max(X.x, d[0]), d[2]));
+        pc.y = qa == 1 ? d[1] : (qa == 3 ? d[3] : std::min(std::max(X.y, d[1]), d[3]));
+      } else {
+        da = -FLT_MAX;
+      }
+      if (sub != B->dom) {
+        V2 ps, ns;
+        double ds = shape_dist(sub_shape, sub, X, ps, ns);
+        if (!(da >= ds)) { da = ds; pc = ps; cand = ORC_OUT_SUBDOMAIN; }
+      }
+      // the threshold of the reflecting side's test (sigma where Dentro takes it)
+      M2 sg = (dd < 0.0) ? sigma_of(B, X.x, X.y) : sigma_of(B, proj.x, proj.y);
+      const double thr = kGobet * norm(tmul(N, sg)) * sqrth;
+      status = ORC_OUT_INSIDE;
+      if (!(da < thr)) { status = cand; proj = pc; }
+    }
+  } while (status == ORC_OUT_INSIDE && k < max_steps);
+  out->x = proj.x;
+  out->y = proj.y;
+  out->Y = Y;
+  out->Z = Z;
+  out->xi = xi;
+  out->t = t;
+  out->outcome = status;
+  out->steps = k;
+  return status == ORC_OUT_INSIDE ? -1 : 0;
+}
+
 // One path: Simulacion_OMP loop body (FeynmanKacSolver.cpp:161-194) with
 // Paso_Absorbente (:7-18).  psi, varphi and mu are the reference's zero
 // defaults; their terms are kept so the floating-point order is the same.
 int simulate(Session& S, const orc_bvp* B, int sub_shape, const double* sub, double x0, double y0,
              double h, uint32_t item, uint32_t path, int max_steps, orc_exit* out) {
+  if (B->problem == ORC_PROBLEM_ROBIN) return simulate_robin(S, B, sub_shape, sub, x0, y0, h, item, path, max_steps, out);
   double sqrth = std::sqrt(h);
   V2 X{x0, y0}, proj{0, 0}, N{0, 0};
   double Y = 1, Z = 0, xi = 0, t = 0, ji_t = 0;

@@ -21,7 +21,10 @@ extern "C" {
 
 enum { ORC_RNG_PHILOX = 0, ORC_RNG_SEQUENTIAL = 1 };
 enum { ORC_SHAPE_RECT = 0, ORC_SHAPE_CIRCLE = 1 };
-enum { ORC_PROBLEM_FRANKE = 0, ORC_PROBLEM_MONEGROS = 1, ORC_PROBLEM_ANISO = 2, ORC_PROBLEM_DISK = 3 };
+/* ORC_PROBLEM_ROBIN: ANISO with reflecting rectangle sides, prob = (side
+ * mask 1: x = x0, 2: y = y0, 4: x = x1, 8: y = y1; varphi; rho; -) */
+enum { ORC_PROBLEM_FRANKE = 0, ORC_PROBLEM_MONEGROS = 1, ORC_PROBLEM_ANISO = 2, ORC_PROBLEM_DISK = 3,
+       ORC_PROBLEM_ROBIN = 4 };
 enum { ORC_OUT_INSIDE = 0, ORC_OUT_DOMAIN = 1, ORC_OUT_SUBDOMAIN = 2 };
 
 typedef struct {

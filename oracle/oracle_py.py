@@ -119,6 +119,7 @@ def philox(ctr, key):
     return list(o)
 
 
+ROBIN = 4  # ORC_PROBLEM_ROBIN: prob = (side mask, varphi, rho, 0)
 STAT_NAMES = ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL", "RNGC")
 
 

@@ -526,7 +526,7 @@ int fk_last_timing(const fk_ctx* ctx, double out[3]) {
 
 int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* d, int* id) {
   if (!ctx || !d || !id) return fail(ctx, FK_ERR_ARG, "null argument");
-  if (d->problem < 0 || d->problem > 3) return fail(ctx, FK_ERR_REGISTRY, "unknown problem functor");
+  if (d->problem < 0 || d->problem > 4) return fail(ctx, FK_ERR_REGISTRY, "unknown problem functor");
   if (d->cv < FK_CV_NONE || d->cv > FK_CV_MLP) return fail(ctx, FK_ERR_ARG, "unknown control-variate mode");
   const int need_shape = (d->problem == FK_PROBLEM_DISK) ? FK_SHAPE_CIRCLE : FK_SHAPE_RECT;
   if (d->dom_shape != need_shape) return fail(ctx, FK_ERR_ARG, "domain shape does not match the problem functor");
@@ -537,6 +537,11 @@ int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* d, int* id) {
   if (d->dom_shape == FK_SHAPE_RECT && !(d->dom[2] > d->dom[0] && d->dom[3] > d->dom[1]))
     return fail(ctx, FK_ERR_ARG, "empty rectangle domain");
   if (d->dom_shape == FK_SHAPE_CIRCLE && !(d->dom[0] > 0)) return fail(ctx, FK_ERR_ARG, "non-positive radius");
+  if (d->problem == FK_PROBLEM_ROBIN) {
+    const double m = d->prob[0];
+    if (!(m >= 0 && m <= 15 && m == std::floor(m))) return fail(ctx, FK_ERR_ARG, "reflecting side mask must be 0..15");
+    if (!(d->prob[2] >= 0)) return fail(ctx, FK_ERR_ARG, "rho must be >= 0");
+  }
   fk::BvpDev b;
   std::memset(&b, 0, sizeof(b));
   b.problem = d->problem;

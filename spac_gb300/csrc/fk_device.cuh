@@ -52,6 +52,14 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, fl
   z1 = rad * s;
 }
 
+// Exp(1) variate from one 32-bit word: -log(u), u = (word + 1/2) 2^-32.
+__device__ __forceinline__ double exp1_draw(uint32_t w, double) {
+  return -log((static_cast<double>(w) + 0.5) * 2.3283064365386962890625e-10);
+}
+__device__ __forceinline__ float exp1_draw(uint32_t w, float) {
+  return -__logf((static_cast<float>(w) + 0.5f) * 2.3283064365386962890625e-10f);
+}
+
 // ------------------------------------------------------------ geometry -------
 template <typename R>
 struct Bnd {
@@ -332,5 +340,43 @@ struct Problem<3> {
     return FrankeEval<R>((x - R(b.prob[0])) * inv + R(0.5), (y - R(b.prob[1])) * inv + R(0.5)).u();
   }
 };
+
+// FK_PROBLEM_ROBIN: the anisotropic problem on a rectangle whose sides in the
+// mask prob[0] (1: x = x0, 2: y = y0, 4: x = x1, 8: y = y1) reflect instead of
+// absorbing (Frontera::Absorbente false there, Frontera.hpp:23-36), with the
+// Robin coefficients of Paso_Reflejante (FeynmanKacSolver.cpp:19-67):
+// varphi = prob[1] (Y += varphi Y dL) and psi = d_n u - varphi u (Z += psi Y dL),
+// so that u stays the exact solution.  prob[2] = rho: the reflecting step is
+// taken while the path is within rho of its reflecting side.
+template <>
+struct Problem<4> : Problem<2> {
+  template <typename R>
+  __device__ static R psi(const BvpDev& b, R x, R y, R nx, R ny) {
+    FrankeEval<R> F(x, y);
+    const R q = R(1) + x * y;
+    const R Fv = F.u();
+    const R ux = F.ux() * q + Fv * y, uy = F.uy() * q + Fv * x;
+    return nx * ux + ny * uy - R(b.prob[1]) * (Fv * q);
+  }
+};
+
+// Problems with reflecting sides (the Paso_Reflejante branch of the step).
+template <int PROB>
+struct RobinOf {
+  static constexpr bool value = false;
+};
+template <>
+struct RobinOf<4> {
+  static constexpr bool value = true;
+};
+
+// Side of a rectangle that Dentro's nearest boundary point lies on (0: x = x0,
+// 1: y = y0, 2: x = x1, 3: y = y1), if it is in the reflecting mask; -1 for
+// absorbing sides and for corners (diagonal normals).
+template <typename R>
+__device__ __forceinline__ int robin_side(const Bnd<R>& w, int mask) {
+  const int s = (w.nx == R(-1)) ? 0 : (w.ny == R(-1)) ? 1 : (w.nx == R(1)) ? 2 : (w.ny == R(1)) ? 3 : -1;
+  return (s >= 0 && ((mask >> s) & 1)) ? s : -1;
+}
 
 }  // namespace fk

@@ -631,7 +631,7 @@ cudaError_t disk_launch(int problem, const DiskArgs& a, const DiskBatch& b, cuda
   switch (problem) {
     case 0: disk_coef_kernel<0><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
     case 1: disk_coef_kernel<1><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
-    case 2: disk_coef_kernel<2><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
+    case 2: case 4: disk_coef_kernel<2><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;  // ROBIN: ANISO's c, f
     default: disk_coef_kernel<3><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
   }
   const size_t mode_smem = static_cast<size_t>(kModeWarps) * b.max_half * (2 * b.max_half + 1) * sizeof(double);

@@ -280,7 +280,7 @@ cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s) 
   const dim3 grid(a.n_items), block(kFinalizeThreads);
   switch (problem) {
     case 1: finalize_kernel<1><<<grid, block, 0, s>>>(a); break;
-    case 2: finalize_kernel<2><<<grid, block, 0, s>>>(a); break;
+    case 2: case 4: finalize_kernel<2><<<grid, block, 0, s>>>(a); break;  // ROBIN: the ANISO u
     case 3: finalize_kernel<3><<<grid, block, 0, s>>>(a); break;
     default: finalize_kernel<0><<<grid, block, 0, s>>>(a); break;
   }

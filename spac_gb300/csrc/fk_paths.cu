@@ -366,6 +366,15 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         dom_can_win = !(s0 > d0 && s1 > d1 && s2 < d2 && s3 < d3);
     }
     const R st0 = Problem<PROB>::template state<R>(bvp, x0, y0);  // sigma state at the start point
+    // Reflecting sides (FK_PROBLEM_ROBIN), only where the domain can win
+    // Dentro's comparison.
+    int rmask = 0;
+    R rho = R(0), rphi = R(0);
+    if constexpr (RobinOf<PROB>::value) {
+      rmask = dom_can_win ? (static_cast<int>(bvp.prob[0]) & 15) : 0;
+      rphi = R(bvp.prob[1]);
+      rho = R(bvp.prob[2]);
+    }
     const uint32_t item = static_cast<uint32_t>(ch.item);
     // learned control variate: grad u_hat table of this item's region
     const float2* ctab = nullptr;
@@ -523,11 +532,78 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         R z0, z1;
         box_muller(wa, wb, z0, z1);
         const R dWx = sqrth * z0, dWy = sqrth * z1;
-        Z += co.f * Y * h;
-        if (cv) xi += Y * (co.Fx * dWx + co.Fy * dWy);
-        Y += co.c * Y * h;
-        x += co.bx * h + co.s * dWx;
-        y += co.by * h + co.s * dWy;
+        if constexpr (RobinOf<PROB>::value) {
+          // ---- Paso_Reflejante (FeynmanKacSolver.cpp:19-67) on reflecting sides
+          R xn = x + (co.bx * h + co.s * dWx), yn = y + (co.by * h + co.s * dWy);
+          R lt[4] = {R(0), R(0), R(0), R(0)};  // local time pushed back through each side
+          R ploc = R(0), vloc = R(0);
+          if (rmask) {
+            // Lepingle's step on every reflecting side within rho of the
+            // current point: the push-back through the side is the maximum
+            // over the step of the Brownian bridge of the normal
+            // displacement, drawn exactly from an Exp(1) variate (mean 2h of
+            // the reference's omega, :33-36) and started from the distance
+            // to the side.  The sides' normals are the coordinate axes and
+            // sigma is s I, so in a corner the two pushes are independent.
+            uint4 re = make_uint4(0u, 0u, 0u, 0u);
+            bool drawn = false;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              if (!((rmask >> q) & 1)) continue;
+              const R dq = q == 0 ? d0 - x : (q == 1 ? d1 - y : (q == 2 ? x - d2 : y - d3));
+              if (!(dq > -rho)) continue;
+              if (!drawn) {
+                re = philox10(make_uint4(0x80000000u | static_cast<uint32_t>(k), ch.p0 + pl, item, a.stream), a.key0,
+                              a.key1);
+                drawn = true;
+              }
+              const R E = exp1_draw(q == 0 ? re.x : (q == 1 ? re.y : (q == 2 ? re.z : re.w)), R(0));
+              const R nx = q == 0 ? R(-1) : (q == 2 ? R(1) : R(0));
+              const R ny = q == 1 ? R(-1) : (q == 3 ? R(1) : R(0));
+              const R uc = co.s * (nx * dWx + ny * dWy) + (nx * co.bx + ny * co.by) * h;
+              const R nu = R(0.5) * (uc + sqrt(uc * uc + R(2) * co.s * co.s * h * E));
+              const R L = fmax(R(0), nu + fmin(dq, R(0)));
+              xn -= L * nx;
+              yn -= L * ny;
+              lt[q] = L;
+            }
+            // a reflecting side crossed in the step: back onto it, the
+            // overshoot added to its local time (:49-58)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              if (!((rmask >> q) & 1)) continue;
+              const R o = q == 0 ? d0 - xn : (q == 1 ? d1 - yn : (q == 2 ? xn - d2 : yn - d3));
+              if (o > R(0)) {
+                if (q == 0) xn = d0; else if (q == 1) yn = d1; else if (q == 2) xn = d2; else yn = d3;
+                lt[q] += o;
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const R l = lt[q];
+              if (l > R(0)) {
+                // psi at the side's point nearest the new position
+                const R px = q == 0 ? d0 : (q == 2 ? d2 : fmin(fmax(xn, d0), d2));
+                const R py = q == 1 ? d1 : (q == 3 ? d3 : fmin(fmax(yn, d1), d3));
+                const R nx = q == 0 ? R(-1) : (q == 2 ? R(1) : R(0));
+                const R ny = q == 1 ? R(-1) : (q == 3 ? R(1) : R(0));
+                ploc += Problem<PROB>::psi(bvp, px, py, nx, ny) * l;
+                vloc += rphi * l;
+              }
+            }
+          }
+          Z += co.f * Y * h + ploc * Y;
+          if (cv) xi += Y * (co.Fx * dWx + co.Fy * dWy);
+          Y += co.c * Y * h + vloc * Y;
+          x = xn;
+          y = yn;
+        } else {
+          Z += co.f * Y * h;
+          if (cv) xi += Y * (co.Fx * dWx + co.Fy * dWy);
+          Y += co.c * Y * h;
+          x += co.bx * h + co.s * dWx;
+          y += co.by * h + co.s * dWy;
+        }
         ++k;
         // ---- exit rule (Dentro, FeynmanKacSolver.cpp:68-106)
         Bnd<R> w;
@@ -551,6 +627,35 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         const R thr = R(kGobet) * sqrt(nsx * nsx + nsy * nsy) * sqrth;
         capped = k >= a.max_steps;
         exits = !(w.d < thr) || capped;
+        if constexpr (RobinOf<PROB>::value) {
+          if (rmask && dom_wins && robin_side<R>(w, rmask) >= 0) {
+            // The nearest boundary is a reflecting side: no stop there
+            // (dentro / reflejada, :82-84).  The path still stops within the
+            // Gobet band of the subdomain or of an absorbing side, the
+            // nearer of them (the reference tests only the nearest boundary,
+            // which lets paths near a mixed corner cross the absorbing side).
+            R da = R(-FLT_MAX);
+            int qa = -1;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              if ((rmask >> q) & 1) continue;
+              const R dq = q == 0 ? d0 - x : (q == 1 ? d1 - y : (q == 2 ? x - d2 : y - d3));
+              if (dq > da) { da = dq; qa = q; }
+            }
+            if (qa >= 0) {
+              w.d = da;
+              w.ex = qa == 0 ? d0 : (qa == 2 ? d2 : fmin(fmax(x, d0), d2));
+              w.ey = qa == 1 ? d1 : (qa == 3 ? d3 : fmin(fmax(y, d1), d3));
+            } else {
+              w.d = R(-FLT_MAX);
+            }
+            if (has_sub) {
+              const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
+              if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
+            }
+            exits = !(w.d < thr) || capped;
+          }
+        }
         ex = w.ex;
         ey = w.ey;
       }
@@ -642,6 +747,7 @@ const void* paths_fn_r(int problem, int st) {
     case 1: return paths_fn<R, 1, WM>(st);
     case 2: return paths_fn<R, 2, WM>(st);
     case 3: return paths_fn<R, 3, WM>(st);
+    case 4: return paths_fn<R, 4, WM>(st);
     default: return paths_fn<R, 0, WM>(st);
   }
 }

@@ -14,7 +14,9 @@ from . import lib_path
 FK_OK = 0
 FK_ERR_ARG, FK_ERR_CUDA, FK_ERR_REGISTRY, FK_ERR_STEP_CAP = -1, -2, -3, -4
 FK_ERR_NOT_FOUND, FK_ERR_NO_DEVICE, FK_ERR_CAPACITY = -5, -6, -7
-FRANKE, MONEGROS, ANISO, DISK = 0, 1, 2, 3
+FRANKE, MONEGROS, ANISO, DISK, ROBIN = 0, 1, 2, 3, 4
+# reflecting sides of FK_PROBLEM_ROBIN (prob[0] is their sum)
+SIDE_X0, SIDE_Y0, SIDE_X1, SIDE_Y1 = 1, 2, 4, 8
 RECT, CIRCLE = 0, 1
 CV_NONE, CV_EXACT, CV_MLP = 0, 1, 2
 FP64, FP32 = 0, 1
@@ -223,7 +225,23 @@ class Context:
         d = BvpDesc(problem, cv, dom_shape, (C.c_double * 4)(*dom), (C.c_double * 4)(*prob), mlp_id)
         i = C.c_int()
         self.check(self.L.fk_register_bvp(self.h, C.byref(d), C.byref(i)))
+        if not hasattr(self, "_descs"):
+            self._descs = {}
+        self._descs[i.value] = dict(problem=problem, cv=cv, dom=tuple(dom), dom_shape=dom_shape, prob=tuple(prob),
+                                    mlp_id=mlp_id)
         return i.value
+
+    def bvp_with_rho(self, bvp, rho):
+        """The registered BVP with the reflecting-zone width rho (FK_PROBLEM_ROBIN
+        keeps it in prob[2]); other problems ignore rho."""
+        d = getattr(self, "_descs", {}).get(bvp)
+        if d is None or d["problem"] != ROBIN or d["prob"][2] == rho:
+            return bvp
+        key = ("rho", bvp, float(rho))
+        if key not in self._descs:
+            prob = (d["prob"][0], d["prob"][1], float(rho), d["prob"][3])
+            self._descs[key] = self.register_bvp(d["problem"], d["cv"], d["dom"], d["dom_shape"], prob, d["mlp_id"])
+        return self._descs[key]
 
     # -- point solves
     def solve_points(self, bvp, xy, paths, h, precision=FP64, sub_shape=None, sub_params=None, allow=()):
@@ -404,8 +422,8 @@ class FeynmanKacSolverGPU:
 
     Solve_OMP_Analytic(X0, N, h, rho, bvp) fills phi, phiphi, phi_VR,
     phiphi_VR, xi, xixi, xiphi, APL, RNGC (FeynmanKacSolver.cpp:335-342);
-    rho (reflecting boundaries) is accepted and unused, as every boundary of
-    the supported problems is absorbing.
+    rho is the width of the zone near a reflecting side where the reflecting
+    step runs (FK_PROBLEM_ROBIN); absorbing problems ignore it.
     """
 
     def __init__(self, ctx, precision=FP64):
@@ -416,6 +434,7 @@ class FeynmanKacSolverGPU:
             setattr(self, k, 0.0)
 
     def Solve_OMP_Analytic(self, X0, N, h, rho, bvp):
+        bvp = self.ctx.bvp_with_rho(bvp, rho)
         st = self.ctx.solve_points(bvp, np.asarray(X0, dtype=np.float64).reshape(1, 2), N, h, self.precision)
         self.N = N
         for k in ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL", "RNGC"):

@@ -4,10 +4,12 @@
 // Usage: drop_in_main <arc file> <seed>
 // Arc file: cx cy radius c2 interior n / n lines "theta gid" / n*n iPsi
 // (column-major) / item count / per item "x y frontera gid".
+// drop_in_main --robin <seed>: one point solve with a reflecting domain side.
 // drop_in_main --disk <disk file> drives PseudoespectralCirculoSolverGPU the
 // way main_test_serial.cpp:67-75 drives PseudoespectralCirculoSolver.
 // Disk file: cx cy radius N_circunferencia N_radio theta_0 / n_periph lines
 // "theta gid" / n_inner / n_inner lines "x y gid".
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
@@ -50,7 +52,38 @@ static int disk_main(const char* path) {
   return 0;
 }
 
+// Solve_OMP_Analytic(X0, ...) on a BVP whose domain side x = 0 reflects
+// (Frontera::Absorbente false there), registered as FK_PROBLEM_ROBIN with
+// varphi = -0.5, rho = 0.1.
+static double aniso_u(Vector2d) { return 0.0; }
+static bool absorbing_except_left(Vector2d p) { return !(std::fabs(p[0]) < 1e-8); }
+static int robin_main(unsigned long long seed) {
+  const double prob[4] = {0.0, -0.5, 0.0, 0.0};
+  FeynmanKacSolverGPU::Register_Problem(&aniso_u, FK_PROBLEM_ROBIN, nullptr, prob);
+  FeynmanKacSolverGPU::Register_Distance(&rectangulo, FK_SHAPE_RECT);
+  FeynmanKacSolverGPU solver(0, seed);
+  BVP bvp;
+  bvp.u.funcion = &aniso_u;
+  bvp.frontera_dominio.Distancia = &rectangulo;
+  bvp.frontera_dominio.parametros = {0.0, 0.0, 1.0, 1.0};
+  bvp.frontera_dominio.Absorbente = &absorbing_except_left;
+  Vector2d X0;
+  X0[0] = 0.02;
+  X0[1] = 0.4;
+  solver.Solve_OMP_Analytic(X0, 2000, 1e-3, 0.1, bvp);
+  std::printf("robin %.17g %.17g %.17g %.17g\n", solver.phi, solver.phiphi, solver.APL, solver.RNGC);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 3 && std::string(argv[1]) == "--robin") {
+    try {
+      return robin_main(std::strtoull(argv[2], nullptr, 10));
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 3;
+    }
+  }
   if (argc == 3 && std::string(argv[1]) == "--disk") {
     try {
       return disk_main(argv[2]);

@@ -25,11 +25,13 @@ struct MatrixXd {  // column-major, like Eigen's default
 typedef double (*pfescalar)(Vector2d);
 typedef Vector2d (*pfvectorial)(Vector2d);
 typedef double (*pfdistancia)(std::vector<double>, Vector2d, Vector2d&, Vector2d&);
+typedef bool (*pftipo)(Vector2d);
 
 struct Coeficiente_Escalar { pfescalar funcion = nullptr; };
 struct Coeficiente_Vectorial { pfvectorial funcion = nullptr; };
 struct Frontera {
   pfdistancia Distancia = nullptr;
+  pftipo Absorbente = nullptr, Neumann = nullptr;
   std::vector<double> parametros;
 };
 struct BVP {

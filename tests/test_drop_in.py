@@ -166,3 +166,21 @@ def test_disk_drop_in_matches_c_abi(fk):
         got = dict((int(p.split(":")[0]), float(p.split(":")[1])) for p in parts[3:])
         assert sorted(got) == [int(g) for g in gids]
         assert [got[int(g)] for g in gids] == list(G[k])
+
+
+@pytest.mark.gpu
+def test_robin_drop_in_matches_c_abi(fk):
+    """Frontera::Absorbente false on x = 0 and the call's rho reach the
+    device as FK_PROBLEM_ROBIN's side mask and prob[2]: the drop-in's point
+    solve equals the C ABI's on the same seed and stream."""
+    seed = 5151
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = _driver(tmp)
+        out = subprocess.run([exe, "--robin", str(seed)], capture_output=True, text=True, check=True)
+    v = [float(t) for t in out.stdout.split()[1:]]
+    ctx = fk.Context(0, seed)
+    b = ctx.register_bvp(fk.ROBIN, prob=(1, -0.5, 0.1, 0))
+    st = ctx.solve_points(b, [(0.02, 0.4)], 2000, 1e-3, fk.FP64)
+    for name, got in zip(("phi", "phiphi", "APL", "RNGC"), v):
+        assert np.isclose(got, st[name][0], rtol=1e-12, atol=1e-14), name
+    ctx.close()
