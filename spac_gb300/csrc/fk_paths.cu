@@ -655,6 +655,9 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
             }
             exits = !(w.d < thr) || capped;
           }
+          // a path that goes on from a point on (or, by rounding, just past)
+          // a reflecting side steps with sigma at that point
+          if (!exits && !inside) st = Problem<PROB>::template state<R>(bvp, x, y);
         }
         ex = w.ex;
         ey = w.ey;
