@@ -489,9 +489,10 @@ int simulate_robin(Session& S, const orc_bvp* B, int sub_shape, const double* su
         da = -FLT_MAX;
       }
       if (sub != B->dom) {
+        // a subdomain boundary on the reflecting side (a tie the domain wins) is no candidate
         V2 ps, ns;
         double ds = shape_dist(sub_shape, sub, X, ps, ns);
-        if (!(da >= ds)) { da = ds; pc = ps; cand = ORC_OUT_SUBDOMAIN; }
+        if (ds < dd && !(da >= ds)) { da = ds; pc = ps; cand = ORC_OUT_SUBDOMAIN; }
       }
       // the threshold of the reflecting side's test (sigma where Dentro takes it)
       M2 sg = (dd < 0.0) ? sigma_of(B, X.x, X.y) : sigma_of(B, proj.x, proj.y);

@@ -634,6 +634,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
             // Gobet band of the subdomain or of an absorbing side, the
             // nearer of them (the reference tests only the nearest boundary,
             // which lets paths near a mixed corner cross the absorbing side).
+            const R dref = w.d;  // the reflecting side's distance
             R da = R(-FLT_MAX);
             int qa = -1;
 #pragma unroll
@@ -650,8 +651,10 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
               w.d = R(-FLT_MAX);
             }
             if (has_sub) {
+              // (a subdomain boundary that coincides with the reflecting side,
+              // a tie that the domain wins, is not a candidate)
               const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
-              if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
+              if (sb.d < dref && !(w.d >= sb.d)) { w = sb; dom_wins = false; }
             }
             exits = !(w.d < thr) || capped;
           }
