@@ -413,6 +413,13 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
     f.patch_e32 = S->d_e32.as<float>();
     f.patch_emax = S->d_emax.as<float>();
     f.split_ok = precision == FK_FP32 ? 1 : 0;
+    int kcommon = -1;
+    for (const fk::PatchDev& P : S->patches) {
+      f.fin_words = std::max(f.fin_words, P.nwin * P.k);
+      f.fin_m = std::max(f.fin_m, P.m);
+      kcommon = (kcommon < 0 || kcommon == P.k) ? P.k : 0;
+    }
+    f.fin_k = std::max(kcommon, 0);
   }
   f.stats = a.stats;
   f.acc = a.acc;

@@ -60,6 +60,20 @@ __device__ __forceinline__ float exp1_draw(uint32_t w, float) {
   return -__logf((static_cast<float>(w) + 0.5f) * 2.3283064365386962890625e-10f);
 }
 
+// FP32 -> FP64 by bit manipulation on the integer pipes (the F2F conversion
+// runs on the FP64 pipe, a 64th of the FP32 rate on this part).  Exact for
+// normal numbers and infinities; subnormal inputs (below 1.2e-38, far under
+// any stencil weight that is added) become zero.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u) return (u & 0x80000000u) ? -0.0 : 0.0;
+  const unsigned e64 = (e == 0xffu) ? 0x7ffu : e + 896u;
+  const unsigned hi = (u & 0x80000000u) | (e64 << 20) | ((u & 0x7fffffu) >> 3);
+  const unsigned lo = (u & 0x7u) << 29;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+
 // ------------------------------------------------------------ geometry -------
 template <typename R>
 struct Bnd {

@@ -127,6 +127,9 @@ struct FinalizeArgs {
   const int* row;           // item -> row (for B scatter)
   double* B;                // may be null
   int* flags;               // may be null: [0] |= an item had capped paths, [1] |= an item lost paths
+  // patch stencils: the largest nwin * k, m and the common k over the
+  // launch's patches (fin_words = 0: the generic per-item path)
+  int fin_words, fin_m, fin_k;
 };
 
 // host launchers (fk_paths.cu)

@@ -22,43 +22,48 @@ constexpr int kFinalizeThreads = 512;
 // fk_stats layout (16 doubles): phi, phiphi, phi_VR, phiphi_VR, xi, xixi,
 // xiphi, APL, RNGC, B, n_paths, n_domain_exits, n_capped, xi_mean,
 // xi_sq_mean, mean_steps.
+// Per-item statistics, B and the result flags (thread 0 of the item's CTA).
 template <int PROB>
-__global__ void finalize_kernel(const FinalizeArgs a) {
-  const int item = blockIdx.x;
-  if (item >= a.n_items) return;
-  const ItemDev it = a.items[item];
+__device__ __forceinline__ void finalize_item_head(const FinalizeArgs& a, int item, const ItemDev& it, bool live,
+                                                   double N) {
   const BvpDev bvp = a.bvp[it.bvp];
-  const double N = static_cast<double>(it.paths);
   const double* S = a.stats + static_cast<long long>(item) * kNumStats;
   double Bv;
-  // an item given no paths contributes nothing (G = 0, B = 0)
-  const bool live = !it.frontera && it.paths > 0;
   if (it.frontera) {
     Bv = Problem<PROB>::u(bvp, it.x, it.y);  // Solve_OMP_Analytic :346-347
   } else {
     Bv = live ? S[7] / N : 0.0;
   }
-  if (threadIdx.x == 0) {
-    if (a.item_stats) {
-      double* o = a.item_stats + static_cast<long long>(item) * 16;
-      if (!live) {
-        for (int j = 0; j < 16; ++j) o[j] = 0.0;
-        o[9] = Bv;
-      } else {
-        // slot 2 holds sum(xi + xi^2); the reference adds it twice (xi/xixi aliasing)
-        o[0] = S[0] / N; o[1] = S[1] / N; o[2] = S[3] / N; o[3] = S[4] / N;
-        o[4] = (S[2] + S[2]) / N; o[5] = (S[2] + S[2]) / N; o[6] = S[5] / N;
-        o[7] = it.h * S[6] / N; o[8] = 4.0 * S[6]; o[9] = Bv; o[10] = S[kStatPaths]; o[11] = S[8]; o[12] = S[9];
-        o[13] = (S[2] - S[10]) / N; o[14] = S[10] / N; o[15] = S[6] / N;
-      }
-    }
-    if (a.item_B) a.item_B[item] = Bv;
-    if (a.B) atomicAdd(&a.B[a.row[item]], Bv);
-    if (a.flags && live) {
-      if (S[kStatCap] > 0.0) atomicOr(&a.flags[0], 1);
-      if (S[kStatPaths] != N) atomicOr(&a.flags[1], 1);  // every requested path must have completed
+  if (a.item_stats) {
+    double* o = a.item_stats + static_cast<long long>(item) * 16;
+    if (!live) {
+      for (int j = 0; j < 16; ++j) o[j] = 0.0;
+      o[9] = Bv;
+    } else {
+      // slot 2 holds sum(xi + xi^2); the reference adds it twice (xi/xixi aliasing)
+      o[0] = S[0] / N; o[1] = S[1] / N; o[2] = S[3] / N; o[3] = S[4] / N;
+      o[4] = (S[2] + S[2]) / N; o[5] = (S[2] + S[2]) / N; o[6] = S[5] / N;
+      o[7] = it.h * S[6] / N; o[8] = 4.0 * S[6]; o[9] = Bv; o[10] = S[kStatPaths]; o[11] = S[8]; o[12] = S[9];
+      o[13] = (S[2] - S[10]) / N; o[14] = S[10] / N; o[15] = S[6] / N;
     }
   }
+  if (a.item_B) a.item_B[item] = Bv;
+  if (a.B) atomicAdd(&a.B[a.row[item]], Bv);
+  if (a.flags && live) {
+    if (S[kStatCap] > 0.0) atomicOr(&a.flags[0], 1);
+    if (S[kStatPaths] != N) atomicOr(&a.flags[1], 1);  // every requested path must have completed
+  }
+}
+
+template <int PROB>
+__global__ void finalize_kernel(const FinalizeArgs a) {
+  const int item = blockIdx.x;
+  if (item >= a.n_items) return;
+  const ItemDev it = a.items[item];
+  const double N = static_cast<double>(it.paths);
+  // an item given no paths contributes nothing (G = 0, B = 0)
+  const bool live = !it.frontera && it.paths > 0;
+  if (threadIdx.x == 0) finalize_item_head<PROB>(a, item, it, live, N);
   if (a.stencil_kind == 0 || it.stencil < 0) return;
   const double* acc = a.acc + it.acc_off;
   const long long goff = a.g_off ? a.g_off[item] : 0;
@@ -146,6 +151,146 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
       }
     }
   }
+}
+
+// ------------------------------------------------- patch-stencil finalize --
+// Items of a square-patch mesh, one CTA per item, everything of the item in
+// shared memory:
+//  1. its nwin x k FP64 moments t_W (one coalesced sweep) and CSR positions;
+//  2. the windows some exit chose (a nonzero moment);
+//  3. v_W = E_W t_W (FP32 assemblies with A_W^-1 = I + E_W, max |E| small)
+//     or A_W^-1 t_W (FP64): one warp per window and lane per row, so a
+//     warp's loads of one column of the window's matrix are k consecutive
+//     words; a warp keeps two windows' loads in flight;
+//  4. G entry gi: -(sum over the windows covering it, in a fixed order) / N,
+//     written to item_G and added to its CSR position.
+// The matrices (12.7 MB for the 8x8 mesh) stay in L2; each item's moments
+// are read from DRAM once.
+constexpr int kPatchThreads = 256;
+
+template <typename T, int K>
+__device__ __forceinline__ void window_products(const T* __restrict__ Mw0, const T* __restrict__ Mw1,
+                                                const T* t0, const T* t1, int k, int r, T& s0, T& s1) {
+  // s = sum_b M(r, b) t(b), M column-major; K > 0: k == K at compile time
+  const int kk = K > 0 ? K : k;
+  s0 = T(0);
+  s1 = T(0);
+  if (K > 0) {
+    T m0[K > 0 ? K : 1], m1[K > 0 ? K : 1];
+#pragma unroll
+    for (int b = 0; b < (K > 0 ? K : 1); ++b) {
+      m0[b] = __ldg(Mw0 + r + b * kk);
+      m1[b] = Mw1 ? __ldg(Mw1 + r + b * kk) : T(0);
+    }
+#pragma unroll
+    for (int b = 0; b < (K > 0 ? K : 1); ++b) {
+      s0 = fma(m0[b], t0[b], s0);
+      if (Mw1) s1 = fma(m1[b], t1[b], s1);
+    }
+  } else {
+    for (int b = 0; b < kk; ++b) {
+      s0 = fma(__ldg(Mw0 + r + b * kk), t0[b], s0);
+      if (Mw1) s1 = fma(__ldg(Mw1 + r + b * kk), t1[b], s1);
+    }
+  }
+}
+
+template <typename T, int K>
+__device__ __forceinline__ void patch_window_pass(const T* __restrict__ M, const T* tw, const unsigned char* vis,
+                                                  int nwin, int k, T* v) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int W0 = warp; W0 < nwin; W0 += 2 * nw) {
+    const int W1 = W0 + nw;
+    const bool a0 = vis[W0] != 0, a1 = W1 < nwin && vis[W1] != 0;
+    if (!a0 && !a1) continue;
+    const int w0 = a0 ? W0 : W1;  // the first live window of the pair
+    const T* M0 = M + static_cast<long long>(w0) * k * k;
+    const T* M1 = (a0 && a1) ? M + static_cast<long long>(W1) * k * k : nullptr;
+    for (int r = lane; r < k; r += 32) {
+      T s0, s1;
+      window_products<T, K>(M0, M1, tw + w0 * k, tw + W1 * k, k, r, s0, s1);
+      v[w0 * k + r] = s0;
+      if (M1) v[W1 * k + r] = s1;
+    }
+  }
+}
+
+template <int PROB, int K>
+__global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const FinalizeArgs a) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  const int item = blockIdx.x;
+  if (item >= a.n_items) return;
+  const ItemDev it = a.items[item];
+  const double N = static_cast<double>(it.paths);
+  const bool live = !it.frontera && it.paths > 0;
+  if (threadIdx.x == 0) finalize_item_head<PROB>(a, item, it, live, N);
+  if (it.stencil < 0) return;
+  const PatchDev P = a.patches[it.stencil];
+  const int m = P.m, k = P.k, nwin = P.nwin, words = nwin * k;
+  const long long goff = a.g_off ? a.g_off[item] : 0;
+  if (!live) {
+    if (a.item_G)
+      for (int gi = threadIdx.x; gi < m; gi += blockDim.x) a.item_G[goff + gi] = 0.0;
+    return;
+  }
+  // moments (FP64), results (FP64, or FP32 in the first half), moments in
+  // FP32 for the split products (converted once: F2F runs on the FP64 pipe)
+  double* tw = reinterpret_cast<double*>(fsm);
+  double* v64 = tw + a.fin_words;
+  float* v32 = reinterpret_cast<float*>(v64);
+  float* t32 = reinterpret_cast<float*>(v64 + a.fin_words);
+  int* cidx = reinterpret_cast<int*>(t32 + a.fin_words);
+  unsigned char* vis = reinterpret_cast<unsigned char*>(cidx + a.fin_m);
+  const double* acc = a.acc + it.acc_off;
+  const bool split = a.split_ok && a.patch_e32 && a.patch_emax[it.stencil] < kSplitMaxE;
+  for (int i = threadIdx.x; i < words; i += blockDim.x) {
+    const double t = acc[i];
+    tw[i] = t;
+    if (split) t32[i] = static_cast<float>(t);
+  }
+  if (a.csr_val)
+    for (int j = threadIdx.x; j < m; j += blockDim.x) cidx[j] = a.csr_idx[goff + j];
+  __syncthreads();
+  for (int W = threadIdx.x; W < nwin; W += blockDim.x) {
+    // nonzero test on the bits (+-0 are zero), off the FP64 pipe
+    unsigned long long any = 0ull;
+    for (int b = 0; b < k; ++b) any |= static_cast<unsigned long long>(__double_as_longlong(tw[W * k + b])) << 1;
+    vis[W] = any != 0ull ? 1 : 0;
+  }
+  __syncthreads();
+  if (split)
+    patch_window_pass<float, K>(a.patch_e32 + P.ainv_off, t32, vis, nwin, k, v32);
+  else
+    patch_window_pass<double, K>(a.patch_ainv + P.ainv_off, tw, vis, nwin, k, v64);
+  __syncthreads();
+  for (int gi = threadIdx.x; gi < m; gi += blockDim.x) {
+    double g = 0.0;
+    auto add = [&](int W, int t) {
+      if (!vis[W]) return;
+      g += split ? tw[W * k + t] + f32_to_f64(v32[W * k + t]) : v64[W * k + t];
+    };
+    if (P.closed) {
+      for (int t = 0; t < k; ++t) {
+        int W = gi - t;
+        if (W < 0) W += m;
+        add(W, t);
+      }
+    } else {
+      const int wlo = max(0, gi - k + 1), whi = min(gi, m - k);
+      for (int W = wlo; W <= whi; ++W) add(W, gi - W);
+    }
+    g = -g / N;
+    if (a.item_G) a.item_G[goff + gi] = g;
+    if (a.csr_val) a.csr_val[cidx[gi]] += g;
+  }
+}
+
+// Shared memory of finalize_patch_kernel (0: the item-per-CTA generic path).
+size_t finalize_patch_smem(const FinalizeArgs& a) {
+  if (a.stencil_kind != 2 || a.fin_words <= 0) return 0;
+  const size_t b = static_cast<size_t>(a.fin_words) * (2 * sizeof(double) + sizeof(float)) +
+                   static_cast<size_t>(a.fin_m) * sizeof(int) + static_cast<size_t>(a.fin_m);
+  return b <= 160 * 1024 ? (b + 15) / 16 * 16 : 0;
 }
 
 // ---------------------------------------------------- FP64 matrix builders --
@@ -275,8 +420,31 @@ __global__ void inverse_kernel(const double* A, double* inv, const int* ns, cons
 }
 
 // --------------------------------------------------------------- launchers --
+template <int PROB, int K>
+cudaError_t launch_patch_finalize(const FinalizeArgs& a, size_t smem, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(finalize_patch_kernel<PROB, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  finalize_patch_kernel<PROB, K><<<a.n_items, kPatchThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int PROB>
+cudaError_t launch_patch_finalize_k(const FinalizeArgs& a, size_t smem, cudaStream_t s) {
+  return a.fin_k == 20 ? launch_patch_finalize<PROB, 20>(a, smem, s) : launch_patch_finalize<PROB, 0>(a, smem, s);
+}
+
 cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s) {
   if (a.n_items <= 0) return cudaSuccess;
+  const size_t psmem = finalize_patch_smem(a);
+  if (psmem > 0) {
+    switch (problem) {
+      case 1: return launch_patch_finalize_k<1>(a, psmem, s);
+      case 2: case 4: return launch_patch_finalize_k<2>(a, psmem, s);
+      case 3: return launch_patch_finalize_k<3>(a, psmem, s);
+      default: return launch_patch_finalize_k<0>(a, psmem, s);
+    }
+  }
   const dim3 grid(a.n_items), block(kFinalizeThreads);
   switch (problem) {
     case 1: finalize_kernel<1><<<grid, block, 0, s>>>(a); break;
