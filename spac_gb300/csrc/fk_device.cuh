@@ -74,6 +74,23 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
+// FP64 -> FP32 on the integer pipes, rounded toward zero (|error| < 1 ulp of
+// the result): for operands of small corrections only.  Magnitudes below the
+// FP32 normal range become zero, above it infinity; NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32_rz(double d) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(d));
+  const unsigned hi = static_cast<unsigned>(u >> 32), lo = static_cast<unsigned>(u);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = static_cast<int>((hi >> 20) & 0x7ffu);
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  unsigned r;
+  if (e == 0x7ff) r = sign | 0x7f800000u | (mant ? 0x400000u : 0u);
+  else if (e - 896 <= 0) r = sign;
+  else if (e - 896 >= 255) r = sign | 0x7f800000u;
+  else r = sign | (static_cast<unsigned>(e - 896) << 23) | mant;
+  return __uint_as_float(r);
+}
+
 // ------------------------------------------------------------ geometry -------
 template <typename R>
 struct Bnd {

@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
   for (int i = threadIdx.x; i < words; i += blockDim.x) {
     const double t = acc[i];
     tw[i] = t;
-    if (split) t32[i] = static_cast<float>(t);
+    if (split) t32[i] = f64_to_f32_rz(t);  // (the F2F instruction runs on the FP64 pipe)
   }
   if (a.csr_val)
     for (int j = threadIdx.x; j < m; j += blockDim.x) cidx[j] = a.csr_idx[goff + j];
@@ -263,11 +263,20 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
   else
     patch_window_pass<double, K>(a.patch_ainv + P.ainv_off, tw, vis, nwin, k, v64);
   __syncthreads();
+  // the identity part in FP64, the correction E_W t_W summed in FP32 (it is
+  // below 1e-2 of the identity part), one FP64 division per item
+  const double ninv = -1.0 / N;
   for (int gi = threadIdx.x; gi < m; gi += blockDim.x) {
     double g = 0.0;
+    float corr = 0.f;
     auto add = [&](int W, int t) {
       if (!vis[W]) return;
-      g += split ? tw[W * k + t] + f32_to_f64(v32[W * k + t]) : v64[W * k + t];
+      if (split) {
+        g += tw[W * k + t];
+        corr += v32[W * k + t];
+      } else {
+        g += v64[W * k + t];
+      }
     };
     if (P.closed) {
       for (int t = 0; t < k; ++t) {
@@ -279,7 +288,7 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
       const int wlo = max(0, gi - k + 1), whi = min(gi, m - k);
       for (int W = wlo; W <= whi; ++W) add(W, gi - W);
     }
-    g = -g / N;
+    g = (g + f32_to_f64(corr)) * ninv;
     if (a.item_G) a.item_G[goff + gi] = g;
     if (a.csr_val) a.csr_val[cidx[gi]] += g;
   }
