@@ -38,6 +38,37 @@ struct DBuf {
   ~DBuf() { if (p) cudaFree(p); }
 };
 
+// Page-locked host staging (per-call uploads and result reads; every API call
+// drains its stream before it returns, so a staging buffer is free again at
+// the next call).
+struct HBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  HBuf() = default;
+  HBuf(const HBuf&) = delete;
+  HBuf& operator=(const HBuf&) = delete;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  ~HBuf() { if (p) cudaFreeHost(p); }
+};
+
+template <typename T>
+static cudaError_t upload_pinned(DBuf& b, HBuf& h, const std::vector<T>& v, cudaStream_t s) {
+  const size_t n = v.size() * sizeof(T);
+  cudaError_t e = b.ensure(std::max<size_t>(n, 16));
+  if (e != cudaSuccess || v.empty()) return e;
+  if ((e = h.ensure(n)) != cudaSuccess) return e;
+  std::memcpy(h.p, v.data(), n);
+  return cudaMemcpyAsync(b.p, h.p, n, cudaMemcpyHostToDevice, s);
+}
+
 template <typename T>
 static cudaError_t upload(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
   cudaError_t e = b.ensure(std::max<size_t>(v.size() * sizeof(T), 16));
@@ -107,6 +138,7 @@ struct fk_ctx {
   fk::DBuf w_items, w_chunks, w_stats, w_acc, w_queue, w_gout, w_bout, w_sout, w_val, w_B, w_goff, w_row, w_tmp;
   fk::DBuf w_dgrid, w_dcbar, w_dvar, w_dminv, w_dz, w_dG, w_dB, w_dflags;
   fk::DiskBufs w_disk;
+  fk::HBuf h_items, h_chunks, h_goff, h_stats;  // pinned staging of the per-call transfers
 };
 
 namespace {
@@ -356,8 +388,8 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   // longest chunks first (uneven path counts, as in batched solves)
   std::stable_sort(chunks.begin(), chunks.end(),
                    [](const fk::ChunkDev& a, const fk::ChunkDev& b) { return (a.p1 - a.p0) > (b.p1 - b.p0); });
-  FK_CUDA(fk::upload(ctx->w_items, it, s));
-  FK_CUDA(fk::upload(ctx->w_chunks, chunks, s));
+  FK_CUDA(fk::upload_pinned(ctx->w_items, ctx->h_items, it, s));
+  FK_CUDA(fk::upload_pinned(ctx->w_chunks, ctx->h_chunks, chunks, s));
   FK_CUDA(ctx->w_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
   FK_CUDA(cudaMemsetAsync(ctx->w_stats.p, 0, static_cast<size_t>(n) * fk::kNumStats * sizeof(double), s));
   FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
@@ -400,7 +432,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
   FK_CUDA(ctx->w_gout.ensure(std::max<size_t>(g_total * sizeof(double), 16)));
   FK_CUDA(ctx->w_bout.ensure(std::max<size_t>(n * sizeof(double), 16)));
   FK_CUDA(ctx->w_sout.ensure(std::max<size_t>(static_cast<size_t>(n) * 16 * sizeof(double), 16)));
-  if (g_off) FK_CUDA(fk::upload(ctx->w_goff, *g_off, s));
+  if (g_off) FK_CUDA(fk::upload_pinned(ctx->w_goff, ctx->h_goff, *g_off, s));
   fk::FinalizeArgs f;
   std::memset(&f, 0, sizeof(f));
   f.bvp = a.bvp;
@@ -572,6 +604,18 @@ static void stats_to_struct(const double* s, fk_stats* o) {
   o->n_capped = s[12]; o->xi_mean = s[13]; o->xi_sq_mean = s[14]; o->mean_steps = s[15];
 }
 
+// Per-item statistics (device, fk_stats layout) into out[n] through the
+// pinned staging buffer; drains the context stream.
+static int read_stats(fk_ctx* ctx, const double* d_stats, int n, fk_stats* out) {
+  const size_t bytes = static_cast<size_t>(n) * 16 * sizeof(double);
+  FK_CUDA(ctx->h_stats.ensure(std::max<size_t>(bytes, 16)));
+  FK_CUDA(cudaMemcpyAsync(ctx->h_stats.p, d_stats, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  FK_CUDA(cudaStreamSynchronize(ctx->stream));
+  const double* st = static_cast<const double*>(ctx->h_stats.p);
+  for (int i = 0; i < n; ++i) stats_to_struct(st + static_cast<size_t>(i) * 16, &out[i]);
+  return FK_OK;
+}
+
 int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsigned* paths, const double* h,
                     const int* sub_shape, const double* sub_params, int precision, fk_stats* out) {
   if (!ctx) return FK_ERR_ARG;
@@ -595,9 +639,7 @@ int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsi
   RunOut ro;
   rc = run_items(ctx, bvp_id, precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro);
   if (rc) return rc;
-  std::vector<double> st(static_cast<size_t>(n) * 16);
-  FK_CUDA(cudaMemcpy(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &out[i]);
+  if ((rc = read_stats(ctx, ro.item_stats, n, out))) return rc;
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
   return FK_OK;
 }
@@ -636,9 +678,7 @@ int fk_solve_points_multi(fk_ctx* ctx, int n, const int* bvp_ids, const double* 
   RunOut ro;
   rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro, true);
   if (rc) return rc;
-  std::vector<double> st(static_cast<size_t>(n) * 16);
-  FK_CUDA(cudaMemcpy(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &out[i]);
+  if ((rc = read_stats(ctx, ro.item_stats, n, out))) return rc;
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
   return FK_OK;
 }
@@ -755,10 +795,7 @@ int fk_solve_nodes_arc(fk_ctx* ctx, int bvp_id, int n, const fk_node_item* items
   FK_CUDA(copy_out(G, ro.item_G, gt * sizeof(double), ctx->stream));
   FK_CUDA(copy_out(B, ro.item_B, n * sizeof(double), ctx->stream));
   if (stats) {
-    std::vector<double> st(static_cast<size_t>(n) * 16);
-    FK_CUDA(cudaMemcpyAsync(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    FK_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &stats[i]);
+    if ((rc = read_stats(ctx, ro.item_stats, n, stats))) return rc;
   }
   FK_CUDA(cudaStreamSynchronize(ctx->stream));
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
@@ -1079,10 +1116,7 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   FK_CUDA(copy_out(item_G, ro.item_G, M->g_total * sizeof(double), s));
   FK_CUDA(copy_out(item_B, ro.item_B, n * sizeof(double), s));
   if (item_stats) {
-    std::vector<double> st(static_cast<size_t>(n) * 16);
-    FK_CUDA(cudaMemcpyAsync(st.data(), ro.item_stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-    FK_CUDA(cudaStreamSynchronize(s));
-    for (int i = 0; i < n; ++i) stats_to_struct(&st[static_cast<size_t>(i) * 16], &item_stats[i]);
+    if ((rc = read_stats(ctx, ro.item_stats, n, item_stats))) return rc;
   }
   FK_CUDA(cudaStreamSynchronize(s));
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
