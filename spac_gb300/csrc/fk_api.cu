@@ -139,6 +139,8 @@ struct fk_ctx {
   fk::DBuf w_dgrid, w_dcbar, w_dvar, w_dminv, w_dz, w_dG, w_dB, w_dflags;
   fk::DiskBufs w_disk;
   fk::HBuf h_items, h_chunks, h_goff, h_stats;  // pinned staging of the per-call transfers
+  std::vector<fk::ItemDev> tmp_items;            // host scratch kept across calls
+  std::vector<fk::ChunkDev> tmp_chunks;
 };
 
 namespace {
@@ -313,18 +315,17 @@ struct RunOut {
   bool capped = false;
 };
 
-int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::ItemDev>& items, fk::StencilSet* S,
+int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& it, fk::StencilSet* S,
               const std::vector<long long>* g_off, long long g_total, const int* d_csr_idx, double* d_csr_val,
               const int* d_row, double* d_B, RunOut& out, bool multi_bvp = false) {
   // multi_bvp: items carry their own BVP index (same functor and control mode
   // as bvp_id); otherwise every item uses bvp_id
   cudaStream_t s = ctx->stream;
-  const int n = static_cast<int>(items.size());
+  const int n = static_cast<int>(it.size());
   const int kind = S ? S->kind : 0;
   const fk::BvpDev& bvp = ctx->bvps[bvp_id];
   if (precision != FK_FP64 && precision != FK_FP32) return fail(ctx, FK_ERR_ARG, "precision must be FK_FP64 or FK_FP32");
-  // per-item stencil accumulator offsets
-  std::vector<fk::ItemDev> it = items;
+  // per-item stencil accumulator offsets (set in the caller's item vector)
   long long acc_total = 0;
   int acc_words = 0;
   // learned control variate: one network region per stencil, or region 0
@@ -374,7 +375,8 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
     chunk = total_paths / (4LL * grid);
     chunk = std::max<long long>(block, std::min<long long>(chunk, 32768));
   }
-  std::vector<fk::ChunkDev> chunks;
+  std::vector<fk::ChunkDev>& chunks = ctx->tmp_chunks;  // (reused: no page faults per call)
+  chunks.clear();
   for (int i = 0; i < n; ++i) {
     if (it[i].frontera || it[i].paths == 0) continue;
     const long long np = it[i].paths;
@@ -386,8 +388,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, const std::vector<fk::Item
     }
   }
   // longest chunks first (uneven path counts, as in batched solves)
-  std::stable_sort(chunks.begin(), chunks.end(),
-                   [](const fk::ChunkDev& a, const fk::ChunkDev& b) { return (a.p1 - a.p0) > (b.p1 - b.p0); });
+  bool uneven = false;
+  for (size_t c = 1; c < chunks.size() && !uneven; ++c)
+    uneven = (chunks[c].p1 - chunks[c].p0) != (chunks[0].p1 - chunks[0].p0);
+  if (uneven)
+    std::stable_sort(chunks.begin(), chunks.end(),
+                     [](const fk::ChunkDev& a, const fk::ChunkDev& b) { return (a.p1 - a.p0) > (b.p1 - b.p0); });
   FK_CUDA(fk::upload_pinned(ctx->w_items, ctx->h_items, it, s));
   FK_CUDA(fk::upload_pinned(ctx->w_chunks, ctx->h_chunks, chunks, s));
   FK_CUDA(ctx->w_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
@@ -624,7 +630,8 @@ int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsi
   if (rc) return rc;
   if (n == 0) return FK_OK;
   if ((rc = need_device(ctx))) return rc;
-  std::vector<fk::ItemDev> items(n);
+  std::vector<fk::ItemDev>& items = ctx->tmp_items;
+  items.resize(n);
   for (int i = 0; i < n; ++i) {
     fk::ItemDev& it = items[i];
     std::memset(&it, 0, sizeof(it));
@@ -773,7 +780,8 @@ int fk_solve_nodes_arc(fk_ctx* ctx, int bvp_id, int n, const fk_node_item* items
   if (n == 0) return FK_OK;
   if ((rc = need_device(ctx))) return rc;
   fk::StencilSet& S = ctx->arcs;
-  std::vector<fk::ItemDev> it(n);
+  std::vector<fk::ItemDev>& it = ctx->tmp_items;
+  it.resize(n);
   std::vector<long long> goff(n);
   long long gt = 0;
   for (int i = 0; i < n; ++i) {
@@ -1085,7 +1093,8 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   if ((rc = upload_mesh(ctx, M))) return rc;
   const fk::HostMesh& hm = M->host;
   const int n = static_cast<int>(hm.items.size());
-  std::vector<fk::ItemDev> it(n);
+  std::vector<fk::ItemDev>& it = ctx->tmp_items;
+  it.resize(n);
   for (int i = 0; i < n; ++i) {
     const fk::MeshItem& q = hm.items[i];
     fk::ItemDev& d = it[i];
