@@ -715,8 +715,14 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
       if (ST != 0) {
         double* gacc = a.acc + itg.acc_off;
         for (int i = lane; i < a.acc_words; i += 32) {
-          const double t = static_cast<double>(sacc[i]);
-          if (t != 0.0) atomicAdd(&gacc[i], t);
+          if constexpr (std::is_same<SAcc, float>::value) {
+            // FP32 chunk partials: widened on the integer pipes (F2F runs on the FP64 pipe)
+            const float t = sacc[i];
+            if (t != 0.f) atomicAdd(&gacc[i], f32_to_f64(t));
+          } else {
+            const double t = static_cast<double>(sacc[i]);
+            if (t != 0.0) atomicAdd(&gacc[i], t);
+          }
         }
       }
       __syncwarp();
