@@ -395,7 +395,7 @@ def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
     return res
 
 
-def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=32, pilot_paths=250, pilot_h=1e-3, train_steps=800,
+def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=600, pilot_h=1e-3, train_steps=800,
                    table=128, lr=3e-2, batch=4096, fit_output=True):
     """Time to `target` RMS node error on the assembly, plain FK vs the learned
     control variate (both FP32 stepping, same h).
