@@ -221,9 +221,14 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
   const int item = blockIdx.x;
   if (item >= a.n_items) return;
   const ItemDev it = a.items[item];
-  const double N = static_cast<double>(it.paths);
   const bool live = !it.frontera && it.paths > 0;
-  if (threadIdx.x == 0) finalize_item_head<PROB>(a, item, it, live, N);
+  // -1/N once per item (the FP64 pipe is the scarce one), broadcast through shared memory
+  __shared__ double s_ninv;
+  if (threadIdx.x == 0) {
+    const double N = static_cast<double>(it.paths);
+    finalize_item_head<PROB>(a, item, it, live, N);
+    s_ninv = live ? -1.0 / N : 0.0;
+  }
   if (it.stencil < 0) return;
   const PatchDev P = a.patches[it.stencil];
   const int m = P.m, k = P.k, nwin = P.nwin, words = nwin * k;
@@ -264,8 +269,8 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
     patch_window_pass<double, K>(a.patch_ainv + P.ainv_off, tw, vis, nwin, k, v64);
   __syncthreads();
   // the identity part in FP64, the correction E_W t_W summed in FP32 (it is
-  // below 1e-2 of the identity part), one FP64 division per item
-  const double ninv = -1.0 / N;
+  // below 1e-2 of the identity part)
+  const double ninv = s_ninv;
   for (int gi = threadIdx.x; gi < m; gi += blockDim.x) {
     double g = 0.0;
     float corr = 0.f;
