@@ -509,7 +509,7 @@ def _scatter_roofline(info, f_ms, peaks, src):
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": _read_profile_figures().get("finalize_dram_bytes_per_launch"), "algorithmic_bytes": bytes_,
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({src})",
-            "note": "latency-bound: per-item FP64 reductions and CSR atomics (profiles/)"}
+            "note": "latency-bound: CTA-wide phases per item (moments staged, window products, CSR scatter); profiles/"}
 
 
 def _read_profile_figures():
