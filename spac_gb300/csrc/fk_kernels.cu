@@ -77,7 +77,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
         g = -g / N;
       }
       if (a.item_G) a.item_G[goff + j] = g;
-      if (a.csr_val && live) a.csr_val[a.csr_idx[goff + j]] += g;
+      if (a.csr_val && live) atomicAdd(&a.csr_val[a.csr_idx[goff + j]], g);  // rows of several items may share columns
     }
   } else {
     const PatchDev P = a.patches[it.stencil];
@@ -147,7 +147,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
       if (gi < m && part == 0) {
         if (live) g = -(g + static_cast<double>(corr)) / N;
         if (a.item_G) a.item_G[goff + gi] = g;
-        if (a.csr_val && live) a.csr_val[a.csr_idx[goff + gi]] += g;
+        if (a.csr_val && live) atomicAdd(&a.csr_val[a.csr_idx[goff + gi]], g);
       }
     }
   }
@@ -295,7 +295,9 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
     }
     g = (g + f32_to_f64(corr)) * ninv;
     if (a.item_G) a.item_G[goff + gi] = g;
-    if (a.csr_val) a.csr_val[cidx[gi]] += g;
+    // a row with several items (a node inside several patches) may meet a
+    // column twice: the additions are atomic
+    if (a.csr_val) atomicAdd(&a.csr_val[cidx[gi]], g);
   }
 }
 
