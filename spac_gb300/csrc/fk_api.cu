@@ -426,6 +426,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
     a.cv_tab = M.d_table;
     a.cv_rect = M.d_rect;
     a.cv_grid = M.table_grid;
+    a.cv_tex = M.d_tex;
   }
   a.stencil_kind = kind;
   a.acc_words = acc_words;

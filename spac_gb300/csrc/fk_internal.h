@@ -95,6 +95,7 @@ struct LaunchArgs {
   const float2* cv_tab;    // [regions][grid][grid] grad u_hat
   const double* cv_rect;   // 4 per region
   int cv_grid;
+  unsigned long long cv_tex;  // the table as a filtered texture (FP32 stepping), or 0
   int stencil_kind;        // 0 none, 1 arc, 2 patch
   int acc_words;           // shared accumulator length (elements) per CTA
   int smem_nodes;          // patch nodes / arc angles staged in shared memory (max over stencils)

@@ -31,6 +31,7 @@
 namespace fk {
 
 Mlp::~Mlp() {
+  if (d_tex) cudaDestroyTextureObject(static_cast<cudaTextureObject_t>(d_tex));
   for (void* p : {static_cast<void*>(d_master), d_bf16, static_cast<void*>(d_m), static_cast<void*>(d_v),
                   static_cast<void*>(d_norm), static_cast<void*>(d_partial), static_cast<void*>(d_loss),
                   static_cast<void*>(d_rect), static_cast<void*>(d_table), static_cast<void*>(d_samples),
@@ -1173,6 +1174,8 @@ int mlp_fit_output(Mlp& M, int n, const double* xy, const double* target, const 
 int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err) {
   if (G < 2 || G > 2048) { err = "table grid must be 2..2048"; return FK_ERR_ARG; }
   const long long npts = static_cast<long long>(M.n_regions) * G * G;
+  if (M.d_tex) cudaDestroyTextureObject(static_cast<cudaTextureObject_t>(M.d_tex));
+  M.d_tex = 0;
   if (M.d_table) cudaFree(M.d_table);
   M.d_table = nullptr;
   float2* d_pts = nullptr;
@@ -1199,6 +1202,39 @@ int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err) {
   cudaFree(d_eval);
   if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
   M.table_grid = G;
+  // The texture unit interpolates the FP32 lookups (bilinear with 8-bit
+  // fractional weights: the control term stays a martingale whatever grad
+  // u_hat it uses, and the weights' rounding is far below the network's fit
+  // error).  Pitch-linear 2-D texture: G x (regions G) float2.
+  int dev = 0, pitch_align = 0, tex_align = 0, max_w = 0, max_h = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&pitch_align, cudaDevAttrTexturePitchAlignment, dev);
+  cudaDeviceGetAttribute(&tex_align, cudaDevAttrTextureAlignment, dev);
+  cudaDeviceGetAttribute(&max_w, cudaDevAttrMaxTexture2DLinearWidth, dev);
+  cudaDeviceGetAttribute(&max_h, cudaDevAttrMaxTexture2DLinearHeight, dev);
+  const size_t pitch = static_cast<size_t>(G) * sizeof(float2);
+  const long long height = static_cast<long long>(M.n_regions) * G;
+  if (pitch_align > 0 && tex_align > 0 && pitch % pitch_align == 0 &&
+      reinterpret_cast<uintptr_t>(M.d_table) % tex_align == 0 && G <= max_w && height <= max_h) {
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypePitch2D;
+    rd.res.pitch2D.devPtr = M.d_table;
+    rd.res.pitch2D.desc = cudaCreateChannelDesc<float2>();
+    rd.res.pitch2D.width = G;
+    rd.res.pitch2D.height = static_cast<size_t>(height);
+    rd.res.pitch2D.pitchInBytes = pitch;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = cudaAddressModeClamp;
+    td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    cudaTextureObject_t t = 0;
+    if (cudaCreateTextureObject(&t, &rd, &td, nullptr) == cudaSuccess) M.d_tex = t;
+    else cudaGetLastError();
+  }
   return FK_OK;
 }
 

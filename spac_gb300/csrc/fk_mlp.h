@@ -26,6 +26,9 @@ struct Mlp {
   int* d_sample_off = nullptr;      // inside the d_samples allocation
   float2* d_table = nullptr;        // grad u_hat on a G x G grid per region
   int table_grid = 0;
+  // the same table as a linearly filtered texture (regions stacked in y),
+  // for FP32 stepping; 0 where the table's shape does not allow one
+  unsigned long long d_tex = 0;
   long long adam_t = 0;
   int trainer = 0;                  // fk_mlp_set_trainer: 0 auto, 1 grid-persistent, 2 per-step graph
   Mlp() = default;

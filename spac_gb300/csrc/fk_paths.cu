@@ -365,9 +365,11 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
     // learned control variate: grad u_hat table of this item's region
     const float2* ctab = nullptr;
     R cx0 = R(0), cy0 = R(0), csx = R(0), csy = R(0);
+    float tex_y0 = 0.f;  // the region's first texel row of the filtered table
     const int G = a.cv_grid;
     if (cv_table) {
       const int r = itg.cv_region;
+      tex_y0 = static_cast<float>(r * G) + 0.5f;
       const double* rc = a.cv_rect + 4 * r;
       ctab = a.cv_tab + static_cast<long long>(r) * G * G;
       cx0 = R(rc[0]);
@@ -498,12 +500,20 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
           R u = (x - cx0) * csx, v = (y - cy0) * csy;
           u = fmin(fmax(u, R(0)), R(G - 1) - R(1e-3));
           v = fmin(fmax(v, R(0)), R(G - 1) - R(1e-3));
-          const int i = static_cast<int>(u), j = static_cast<int>(v);
-          const R fu = u - R(i), fv = v - R(j);
-          const float2* T = ctab + j * G + i;
-          const float2 t00 = __ldg(T), t10 = __ldg(T + 1), t01 = __ldg(T + G), t11 = __ldg(T + G + 1);
-          const R gx = (R(1) - fv) * ((R(1) - fu) * R(t00.x) + fu * R(t10.x)) + fv * ((R(1) - fu) * R(t01.x) + fu * R(t11.x));
-          const R gy = (R(1) - fv) * ((R(1) - fu) * R(t00.y) + fu * R(t10.y)) + fv * ((R(1) - fu) * R(t01.y) + fu * R(t11.y));
+          R gx, gy;
+          if (std::is_same<R, float>::value && a.cv_tex) {
+            // the texture unit's bilinear filter (texel centres at i + 1/2)
+            const float2 g = tex2D<float2>(a.cv_tex, static_cast<float>(u) + 0.5f, static_cast<float>(v) + tex_y0);
+            gx = R(g.x);
+            gy = R(g.y);
+          } else {
+            const int i = static_cast<int>(u), j = static_cast<int>(v);
+            const R fu = u - R(i), fv = v - R(j);
+            const float2* T = ctab + j * G + i;
+            const float2 t00 = __ldg(T), t10 = __ldg(T + 1), t01 = __ldg(T + G), t11 = __ldg(T + G + 1);
+            gx = (R(1) - fv) * ((R(1) - fu) * R(t00.x) + fu * R(t10.x)) + fv * ((R(1) - fu) * R(t01.x) + fu * R(t11.x));
+            gy = (R(1) - fv) * ((R(1) - fu) * R(t00.y) + fu * R(t10.y)) + fv * ((R(1) - fu) * R(t01.y) + fu * R(t11.y));
+          }
           co.Fx = -co.s * gx;
           co.Fy = -co.s * gy;
         }
