@@ -436,7 +436,7 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=60
     # learned control variate: pilot from boundary data only
     t0 = time.perf_counter()
     g = (np.arange(pilot_grid) + 0.5) / pilot_grid
-    pxy = np.array([(x, y) for x in g for y in g])
+    pxy = np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2)  # x outer, y inner
     # the pilot only has to approximate u (any u_hat keeps the estimator
     # unbiased), so it runs at the coarse step pilot_h
     pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec)
