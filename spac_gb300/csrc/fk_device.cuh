@@ -36,16 +36,26 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& z0, d
   z0 = rad * c;
   z1 = rad * s;
 }
-// FP32 stepping uses the SFU forms (ex2/lg2.approx): relative error ~1e-6,
-// far below the Monte Carlo error of any node estimate.
+// FP32 stepping uses the SFU forms (ex2/lg2.approx, sqrt.approx and an
+// approximate division): relative errors ~1e-6 at most, far below the Monte
+// Carlo error of any node estimate.  FP64 stepping keeps the correctly
+// rounded forms (it follows the oracle's paths).
 __device__ __forceinline__ float fexp(float v) { return __expf(v); }
 __device__ __forceinline__ double fexp(double v) { return exp(v); }
+__device__ __forceinline__ float fsqrt(float v) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+__device__ __forceinline__ double fsqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
 
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
   const float inv32 = 2.3283064365386962890625e-10f;
   const float u1 = (static_cast<float>(a) + 0.5f) * inv32;  // rounds into (0, 1]
   const float u2 = (static_cast<float>(b) + 0.5f) * inv32;
-  const float rad = sqrtf(-2.0f * __logf(u1));
+  const float rad = fsqrt(-2.0f * __logf(u1));
   float s, c;
   __sincosf(6.28318530717958647692f * u2, &s, &c);
   z0 = rad * c;
@@ -104,10 +114,10 @@ template <typename R>
 __device__ __forceinline__ Bnd<R> circle_dist(R x, R y, R r0, R cx, R cy) {
   Bnd<R> b;
   R nx = x - cx, ny = y - cy;
-  R r = sqrt(nx * nx + ny * ny);
+  R r = fsqrt(nx * nx + ny * ny);
   r = r > R(5e-4) ? r : R(5e-4);
-  nx = nx / r;
-  ny = ny / r;
+  nx = fdiv(nx, r);
+  ny = fdiv(ny, r);
   b.nx = nx;
   b.ny = ny;
   b.ex = nx * r0 + cx;
@@ -142,7 +152,7 @@ __device__ __forceinline__ Bnd<R> rect_dist(R x, R y, R x0, R y0, R x1, R y1) {
     b.ey = by;
     b.nx = sx * kDiag;
     b.ny = sy * kDiag;
-    b.d = sqrt(ox * ox + oy * oy);
+    b.d = fsqrt(ox * ox + oy * oy);
     return b;
   } else {
     side_x = dx > hx;
@@ -234,7 +244,7 @@ struct MonegrosEval {
   __device__ __forceinline__ MonegrosEval(R x, R y) {
     const R k1 = R(1.0), k2 = R(0.01), k3 = R(0.02), k4 = R(0.12), k5 = R(0.05), k6 = R(0.05), k7 = R(-0.12),
             sf = R(0.333);
-    const R rho = sqrt(k1 + k2 * x * x + k3 * y * y);
+    const R rho = fsqrt(k1 + k2 * x * x + k3 * y * y);
     R sr, cr;
     sr = sin(rho);
     cr = cos(rho);
@@ -320,7 +330,7 @@ struct Problem<2> {
   template <typename R>
   __device__ static R state(const BvpDev&, R x, R y) { return coef_a(x, y); }
   template <typename R>
-  __device__ static R sigma_of(R a) { return sqrt(R(2) * a); }
+  __device__ static R sigma_of(R a) { return fsqrt(R(2) * a); }
   template <typename R>
   __device__ static void step(const BvpDev&, R x, R y, R a, bool cv, StepCoef<R>& o) {
     FrankeEval<R> F(x, y);
@@ -329,7 +339,7 @@ struct Problem<2> {
     const R u = Fv * q;
     const R ux = Fx * q + Fv * y, uy = Fy * q + Fv * x;
     const R lap = (F.uxx() + F.uyy()) * q + R(2) * (Fx * y + Fy * x);
-    o.s = sqrt(R(2) * a);
+    o.s = fsqrt(R(2) * a);
     o.c = -(R(1) + x * x + y * y);
     o.bx = y - R(0.5);
     o.by = R(0.5) - x;

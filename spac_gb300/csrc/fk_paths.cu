@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
               const R nx = q == 0 ? R(-1) : (q == 2 ? R(1) : R(0));
               const R ny = q == 1 ? R(-1) : (q == 3 ? R(1) : R(0));
               const R uc = co.s * (nx * dWx + ny * dWy) + (nx * co.bx + ny * co.by) * h;
-              const R nu = R(0.5) * (uc + sqrt(uc * uc + R(2) * co.s * co.s * h * E));
+              const R nu = R(0.5) * (uc + fsqrt(uc * uc + R(2) * co.s * co.s * h * E));
               const R L = fmax(R(0), nu + fmin(dq, R(0)));
               xn -= L * nx;
               yn -= L * ny;
@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
         if (inside) st = stq;
         const R sg = Problem<PROB>::template sigma_of<R>(stq);
         const R nsx = w.nx * sg, nsy = w.ny * sg;
-        const R thr = R(kGobet) * sqrt(nsx * nsx + nsy * nsy) * sqrth;
+        const R thr = R(kGobet) * fsqrt(nsx * nsx + nsy * nsy) * sqrth;
         capped = k >= a.max_steps;
         exits = !(w.d < thr) || capped;
         if constexpr (RobinOf<PROB>::value) {
