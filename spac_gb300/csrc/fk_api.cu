@@ -398,13 +398,19 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   FK_CUDA(fk::upload_pinned(ctx->w_chunks, ctx->h_chunks, chunks, s));
   FK_CUDA(ctx->w_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
   FK_CUDA(cudaMemsetAsync(ctx->w_stats.p, 0, static_cast<size_t>(n) * fk::kNumStats * sizeof(double), s));
+  // slot mode with every item in one chunk: the chunks store their moments,
+  // so the accumulators need no zeroing
+  bool whole_items = !warp_mode;
+  for (const fk::ChunkDev& c : chunks)
+    if (c.p0 != 0 || c.p1 != it[c.item].paths) { whole_items = false; break; }
   FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
-  if (acc_total > 0) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
+  if (acc_total > 0 && !whole_items) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
   FK_CUDA(ctx->w_queue.ensure(16));
   FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));  // queue, error word, result flags
 
   fk::LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
+  a.acc_zeroed = whole_items ? 0 : 1;
   a.bvp = ctx->d_bvps.as<fk::BvpDev>();
   a.items = ctx->w_items.as<fk::ItemDev>();
   a.chunks = ctx->w_chunks.as<fk::ChunkDev>();

@@ -78,6 +78,8 @@ __host__ __device__ inline size_t paths_slot_bytes(int precision, int stencil_ki
 }
 
 struct LaunchArgs {
+  int acc_zeroed;  // 1: the moment accumulators were zeroed (chunks add atomically);
+                   // 0: every chunk is a whole item (slot mode), its flush stores them
   const BvpDev* bvp;
   const ItemDev* items;
   const ChunkDev* chunks;

@@ -128,6 +128,7 @@ extern "C" int fk_solve_points_noalloc(const fk_bvp_desc* d, unsigned long long 
 
   LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
+  a.acc_zeroed = 1;  // (point solves: no stencil moments)
   a.bvp = d_bvp;
   a.items = d_items;
   a.chunks = d_chunks;

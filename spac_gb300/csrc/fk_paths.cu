@@ -724,14 +724,24 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) p
       __threadfence_block();
       if (ST != 0) {
         double* gacc = a.acc + itg.acc_off;
-        for (int i = lane; i < a.acc_words; i += 32) {
-          if constexpr (std::is_same<SAcc, float>::value) {
-            // FP32 chunk partials: widened on the integer pipes (F2F runs on the FP64 pipe)
-            const float t = sacc[i];
-            if (t != 0.f) atomicAdd(&gacc[i], f32_to_f64(t));
-          } else {
-            const double t = static_cast<double>(sacc[i]);
-            if (t != 0.0) atomicAdd(&gacc[i], t);
+        if (!a.acc_zeroed) {
+          // the chunk is the whole item: its moments are stored, zeros included
+          // (no memset of the accumulators and no atomics)
+          const int words = (ST == 2) ? (sp.closed ? sp.m : sp.m - sp.k + 1) * sp.k : sarc.n;
+          for (int i = lane; i < words; i += 32) {
+            if constexpr (std::is_same<SAcc, float>::value) gacc[i] = f32_to_f64(sacc[i]);
+            else gacc[i] = static_cast<double>(sacc[i]);
+          }
+        } else {
+          for (int i = lane; i < a.acc_words; i += 32) {
+            if constexpr (std::is_same<SAcc, float>::value) {
+              // FP32 chunk partials: widened on the integer pipes (F2F runs on the FP64 pipe)
+              const float t = sacc[i];
+              if (t != 0.f) atomicAdd(&gacc[i], f32_to_f64(t));
+            } else {
+              const double t = static_cast<double>(sacc[i]);
+              if (t != 0.0) atomicAdd(&gacc[i], t);
+            }
           }
         }
       }
