@@ -129,6 +129,49 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
   const int g = lane >> 2, t4 = lane & 3;
   const float* P = a.params + static_cast<long long>(region) * NPARAM;
   const __nv_bfloat16* WB = a.wbf + static_cast<long long>(region) * BF_PER_REGION;
+  int n_tiles, row0;
+  if (a.mode == MODE_GRADX) {
+    n_tiles = 1;
+    row0 = (cta + region * grid_x) * kRows;
+  } else {
+    n_tiles = a.rows_per_cta / kRows;
+    row0 = cta * a.rows_per_cta;
+  }
+  // row r of a tile's samples (GRADX: points; TRAIN: Philox-drawn samples;
+  // LOSSGRAD: consecutive samples)
+  auto fetch = [&](int tile, int r, float& x, float& y, float& tg, int& valid) {
+    x = 0.f; y = 0.f; tg = 0.f; valid = 0;
+    if (a.mode == MODE_GRADX) {
+      const int pi = row0 + r;
+      if (pi < a.n_points) {
+        const float2 p = a.points[pi];
+        x = p.x; y = p.y; valid = 1;
+      }
+    } else {
+      const int lo = a.sample_off[region], cnt = a.sample_off[region + 1] - lo;
+      const int gr = row0 + tile * kRows + r;  // row of the region's batch
+      if (cnt > 0) {
+        int si;
+        if (a.mode == MODE_TRAIN) {
+          const uint4 rr = philox10(make_uint4(a.step, static_cast<uint32_t>(gr), static_cast<uint32_t>(region), 0x6d6c70u),
+                                    a.seed0, a.seed1);
+          si = lo + static_cast<int>(rr.x % static_cast<uint32_t>(cnt));
+          valid = 1;
+        } else {
+          si = lo + gr;
+          valid = gr < cnt;
+          if (!valid) si = lo;
+        }
+        const float4 s = a.samples[si];
+        x = s.x; y = s.y; tg = s.z;
+      }
+    }
+  };
+  // the first tile's sample loads go out before the weight loads, so the
+  // two L2 round trips overlap
+  float px = 0.f, py = 0.f, ptg = 0.f;
+  int pvalid = 0;
+  if (tid < kRows) fetch(0, tid, px, py, ptg, pvalid);
   // weights into shared memory, 8 bf16 (16 bytes) per load
   for (int e8 = tid; e8 < W * W / 8; e8 += kThreads) {
     const int r = (e8 * 8) / W, c = (e8 * 8) % W;
@@ -162,47 +205,15 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
     for (int q = 0; q < 4; ++q) cW2[0][j][q] = cW3[0][j][q] = 0.f;
   float gW4 = 0.f, gB3 = 0.f, gB2 = 0.f, gB1 = 0.f, gW10 = 0.f, gW11 = 0.f, gB4 = 0.f, lsum = 0.f;
 
-  int n_tiles, row0;
-  if (a.mode == MODE_GRADX) {
-    n_tiles = 1;
-    row0 = (cta + region * grid_x) * kRows;
-  } else {
-    n_tiles = a.rows_per_cta / kRows;
-    row0 = cta * a.rows_per_cta;
-  }
   __syncthreads();
 
   for (int tile = 0; tile < n_tiles; ++tile) {
     // ---- samples: row tid of this tile
     if (tid < kRows) {
       const int r = tid;
-      float x = 0.f, y = 0.f, tg = 0.f;
-      int valid = 0;
-      if (a.mode == MODE_GRADX) {
-        const int pi = row0 + r;
-        if (pi < a.n_points) {
-          const float2 p = a.points[pi];
-          x = p.x; y = p.y; valid = 1;
-        }
-      } else {
-        const int lo = a.sample_off[region], cnt = a.sample_off[region + 1] - lo;
-        const int gr = row0 + tile * kRows + r;  // row of the region's batch
-        if (cnt > 0) {
-          int si;
-          if (a.mode == MODE_TRAIN) {
-            const uint4 rr = philox10(make_uint4(a.step, static_cast<uint32_t>(gr), static_cast<uint32_t>(region), 0x6d6c70u),
-                                      a.seed0, a.seed1);
-            si = lo + static_cast<int>(rr.x % static_cast<uint32_t>(cnt));
-            valid = 1;
-          } else {
-            si = lo + gr;
-            valid = gr < cnt;
-            if (!valid) si = lo;
-          }
-          const float4 s = a.samples[si];
-          x = s.x; y = s.y; tg = s.z;
-        }
-      }
+      float x = px, y = py, tg = ptg;
+      int valid = pvalid;
+      if (tile > 0) fetch(tile, r, x, y, tg, valid);
       const float z0 = (x - nm.x) * nm.z, z1 = (y - nm.y) * nm.w;
       S.z[r][0] = z0; S.z[r][1] = z1; S.tgt[r] = tg; S.valid[r] = valid;
     }
