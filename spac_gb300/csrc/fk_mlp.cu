@@ -553,15 +553,25 @@ __device__ __forceinline__ unsigned long long mlp_global_ns() {
   return t;
 }
 
+// Arrival with release semantics (the CTA's writes, gathered by the block
+// barrier, become visible before the count), wait with acquire loads.
+__device__ __forceinline__ void bar_arrive_release(unsigned* bar) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
+}
+__device__ __forceinline__ unsigned bar_load_acquire(const unsigned* bar) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+  return v;
+}
+
 __device__ bool grid_barrier(unsigned* bar, unsigned target, int* err) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    __threadfence();
-    atomicAdd(bar, 1u);
+    bar_arrive_release(bar);
     const unsigned long long t0 = mlp_global_ns();
-    while (*reinterpret_cast<volatile unsigned*>(bar) < target) {
+    while (bar_load_acquire(bar) < target) {
       if (*reinterpret_cast<volatile int*>(err) != 0) { ok = 0; break; }
       if (mlp_global_ns() - t0 > kBarrierNs) {
         atomicExch(err, 1);
@@ -570,7 +580,6 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* err) {
       }
       __nanosleep(32);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
