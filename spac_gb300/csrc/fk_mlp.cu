@@ -99,6 +99,8 @@ struct PassArgs {
   float inv_batch;              // 1 / rows per region that contribute to the loss
   float* partial;               // [R][C][NPARAM]
   float* loss;                  // [R][C]
+  float* loss_add;              // if set: the CTA's loss times loss_add_scale is added here instead
+  float loss_add_scale;
   // GRADX
   int n_points;
   const float2* points;
@@ -440,7 +442,8 @@ __device__ void mlp_pass_body(const PassArgs& a, int region, int cta, int grid_x
   if (tid == 0) {
     float l = red[0];
     for (int w = 1; w < kThreads / 32; ++w) l += red[w];
-    a.loss[region * a.ctas_per_region + cta] = l;
+    if (a.loss_add) atomicAdd(a.loss_add, l * a.loss_add_scale);  // off the training step's critical path
+    else a.loss[region * a.ctas_per_region + cta] = l;
   }
 }
 
@@ -596,8 +599,10 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs 
   const long long e0 = bid * per, e1 = min(total, e0 + per);
   PassArgs a = t.a;
   unsigned target = 0;
+  a.loss_add_scale = t.loss_scale;
   for (int s = 0; s < t.steps; ++s) {
     a.step = static_cast<uint32_t>(t.t0 + s);
+    a.loss_add = t.hist + s;  // (zeroed before the launch)
     mlp_pass_body(a, blockIdx.y, blockIdx.x, gridDim.x, smem_raw);
     target += nb;
     if (!grid_barrier(t.bar, target, t.err)) return;
@@ -644,15 +649,6 @@ __global__ void __launch_bounds__(kThreads, 1) mlp_train_kernel(const TrainArgs 
                         bc1, bc2);
       }
       __syncthreads();
-    }
-    if (bid == 0 && threadIdx.x < 32) {
-      // loss of the step: one warp, loads first, then a shuffle tree
-      const int nl = t.a.n_regions * ctas;
-      float sl = 0.f;
-      for (int i = threadIdx.x; i < nl; i += 32) sl += __ldcg(a.loss + i);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o);
-      if (threadIdx.x == 0) t.hist[s] = sl * t.loss_scale;
     }
     target += nb;
     if (!grid_barrier(t.bar, target, t.err)) return;
@@ -996,6 +992,7 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
     t.sched = M.d_sched;
     e = cudaMemcpyAsync(M.d_sched, sched.data(), sched.size() * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(M.d_sync, 0, 2 * sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(M.d_hist, 0, std::max(steps, 1) * sizeof(float), s);
     void* args[] = {&t};
     if (e == cudaSuccess)
       e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel), dim3(ctas, M.n_regions),
