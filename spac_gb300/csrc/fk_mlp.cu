@@ -35,7 +35,7 @@ Mlp::~Mlp() {
   for (void* p : {static_cast<void*>(d_master), d_bf16, static_cast<void*>(d_m), static_cast<void*>(d_v),
                   static_cast<void*>(d_norm), static_cast<void*>(d_partial), static_cast<void*>(d_loss),
                   static_cast<void*>(d_rect), static_cast<void*>(d_table), static_cast<void*>(d_samples),
-                  static_cast<void*>(d_hist), static_cast<void*>(d_sync), static_cast<void*>(d_sched)})
+                  static_cast<void*>(d_hist), static_cast<void*>(d_sync), static_cast<void*>(d_sched), d_fit})
     if (p) cudaFree(p);
 }
 
@@ -857,6 +857,19 @@ int mlp_set_params(Mlp& M, const float* host) {
 }
 
 // Uploads (x, y, target) samples grouped by region.
+// Grow-only device buffer: reallocated only when `need` exceeds its capacity.
+template <typename T>
+static cudaError_t grow(T*& p, size_t& cap, size_t need) {
+  if (need <= cap && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  void* q = nullptr;
+  const cudaError_t e = cudaMalloc(&q, need);
+  if (e == cudaSuccess) { p = static_cast<T*>(q); cap = need; }
+  return e;
+}
+
 static int upload_samples(Mlp& M, int n, const double* xy, const double* target, const int* region,
                           std::vector<int>& off, std::string& err) {
   std::vector<std::vector<float4>> by(M.n_regions);
@@ -873,10 +886,8 @@ static int upload_samples(Mlp& M, int n, const double* xy, const double* target,
     flat.insert(flat.end(), by[r].begin(), by[r].end());
   }
   off[M.n_regions] = static_cast<int>(flat.size());
-  if (M.d_samples) cudaFree(M.d_samples);
-  M.d_samples = nullptr;
-  if (cudaMalloc(&M.d_samples, std::max<size_t>(flat.size(), 1) * sizeof(float4) + (M.n_regions + 1) * sizeof(int)) !=
-      cudaSuccess) {
+  if (grow(M.d_samples, M.cap_samples,
+           std::max<size_t>(flat.size(), 1) * sizeof(float4) + (M.n_regions + 1) * sizeof(int)) != cudaSuccess) {
     err = "mlp: sample allocation failed";
     return FK_ERR_CUDA;
   }
@@ -924,12 +935,9 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
   }
   const int ctas = batch / rows_per_cta;
   const size_t np = static_cast<size_t>(M.n_regions) * NPARAM;
-  if (M.d_partial) cudaFree(M.d_partial);
-  if (M.d_loss) cudaFree(M.d_loss);
-  if (M.d_hist) cudaFree(M.d_hist);
-  if (cudaMalloc(&M.d_partial, np * ctas * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&M.d_loss, static_cast<size_t>(M.n_regions) * ctas * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&M.d_hist, std::max(steps, 1) * sizeof(float)) != cudaSuccess) {
+  if (grow(M.d_partial, M.cap_partial, np * ctas * sizeof(float)) != cudaSuccess ||
+      grow(M.d_loss, M.cap_loss, static_cast<size_t>(M.n_regions) * ctas * sizeof(float)) != cudaSuccess ||
+      grow(M.d_hist, M.cap_hist, std::max(steps, 1) * sizeof(float)) != cudaSuccess) {
     err = "mlp: training buffers";
     return FK_ERR_CUDA;
   }
@@ -983,9 +991,7 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
       sched[3 * st + 1] = static_cast<float>(1.0 - std::pow(0.9, tt));
       sched[3 * st + 2] = static_cast<float>(1.0 - std::pow(0.999, tt));
     }
-    if (M.d_sched) cudaFree(M.d_sched);
-    M.d_sched = nullptr;
-    if (cudaMalloc(&M.d_sched, sched.size() * sizeof(float)) != cudaSuccess) {
+    if (grow(M.d_sched, M.cap_sched, sched.size() * sizeof(float)) != cudaSuccess) {
       err = "mlp: training buffers";
       return FK_ERR_CUDA;
     }
@@ -1141,16 +1147,27 @@ int mlp_fit_output(Mlp& M, int n, const double* xy, const double* target, const 
       }
     const int m = static_cast<int>(pts.size());
     if (m == 0) continue;
-    float2* d_pts = nullptr;
-    float *d_feat = nullptr, *d_tgt = nullptr;
-    double* d_gram = nullptr;
-    int* d_flag = nullptr;
-    cudaError_t e = cudaMalloc(&d_pts, m * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMalloc(&d_feat, static_cast<size_t>(m) * W * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&d_tgt, m * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&d_gram, (W + 1) * kGramCols * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&d_flag, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_pts, pts.data(), m * sizeof(float2), cudaMemcpyHostToDevice, s);
+    // one scratch block, kept in the Mlp: Gram (FP64) | flag | points | features | targets
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t b_gram = up((W + 1) * kGramCols * sizeof(double)), b_flag = up(sizeof(int));
+    const size_t b_pts = up(m * sizeof(float2)), b_feat = up(static_cast<size_t>(m) * W * sizeof(float));
+    const size_t need = b_gram + b_flag + b_pts + b_feat + up(m * sizeof(float));
+    cudaError_t e = cudaSuccess;
+    if (need > M.fit_bytes) {
+      if (M.d_fit) cudaFree(M.d_fit);
+      M.d_fit = nullptr;
+      M.fit_bytes = 0;
+      e = cudaMalloc(&M.d_fit, need);
+      if (e == cudaSuccess) M.fit_bytes = need;
+    }
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+    unsigned char* base = static_cast<unsigned char*>(M.d_fit);
+    double* d_gram = reinterpret_cast<double*>(base);
+    int* d_flag = reinterpret_cast<int*>(base + b_gram);
+    float2* d_pts = reinterpret_cast<float2*>(base + b_gram + b_flag);
+    float* d_feat = reinterpret_cast<float*>(base + b_gram + b_flag + b_pts);
+    float* d_tgt = reinterpret_cast<float*>(base + b_gram + b_flag + b_pts + b_feat);
+    e = cudaMemcpyAsync(d_pts, pts.data(), m * sizeof(float2), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_tgt, tg.data(), m * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_gram, 0, (W + 1) * kGramCols * sizeof(double), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), s);
@@ -1177,11 +1194,6 @@ int mlp_fit_output(Mlp& M, int n, const double* xy, const double* target, const 
     int flag = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(d_pts);
-    cudaFree(d_feat);
-    cudaFree(d_tgt);
-    cudaFree(d_gram);
-    cudaFree(d_flag);
     if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
     if (flag) { err = "mlp fit: the feature Gram matrix is not positive definite (raise the ridge)"; return FK_ERR_NUMERIC; }
   }

@@ -29,6 +29,11 @@ struct Mlp {
   // the same table as a linearly filtered texture (regions stacked in y),
   // for FP32 stepping; 0 where the table's shape does not allow one
   unsigned long long d_tex = 0;
+  void* d_fit = nullptr;            // output-layer refit scratch (kept across calls)
+  size_t fit_bytes = 0;
+  // capacities (bytes) of the training buffers, which only grow: a training
+  // call allocates nothing once they are large enough
+  size_t cap_samples = 0, cap_partial = 0, cap_loss = 0, cap_hist = 0, cap_sched = 0;
   long long adam_t = 0;
   int trainer = 0;                  // fk_mlp_set_trainer: 0 auto, 1 grid-persistent, 2 per-step graph
   Mlp() = default;
