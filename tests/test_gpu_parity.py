@@ -180,7 +180,7 @@ def _oracle_assembly(orc, gpu, mesh, problem, cv, N, h, stream, kind):
         if kind == "patch":
             a, bb = divmod(int(st[i]), int(round(np.sqrt(info["n_stencils"]))))
             rect = _patch_rect(gpu, mesh, st[i])
-            G, Bv, _, _ = s.node_solve_knn(ob, x, y, rect, nxy[gids], 6, gpu._eps, N, h, item=i)
+            G, Bv, _, _ = s.node_solve_knn(ob, x, y, rect, nxy[gids], getattr(gpu, "_k", 6), gpu._eps, N, h, item=i)
         items_G.append(G)
         items_B.append(Bv)
         cols = np.ascontiguousarray(gids, dtype=np.int32)
@@ -199,9 +199,13 @@ def _patch_rect(gpu, mesh, s):
 # eps * spacing = 3 puts the opposite side of a patch beyond the weight cutoff,
 # so the kernel walks each window outward from the exit and stops early;
 # eps * spacing = 1 scans whole windows.
+# k = 20 runs the finalize kernel's compile-time stencil size, k = 6 its
+# general path.
+@pytest.mark.parametrize("k,nps", [(6, 9), (20, 15)])
 @pytest.mark.parametrize("eps_sp", [1.0, 3.0])
-def test_square_patch_assembly_matches_oracle(gpu, orc, fk, launch, eps_sp):
-    n_sub, nps, e, k = 3, 9, 0.25, 6
+def test_square_patch_assembly_matches_oracle(gpu, orc, fk, launch, eps_sp, k, nps):
+    n_sub, e = 3, 0.25
+    gpu._k = k
     mesh = gpu.mesh_square_patches((0, 0, 1, 1), n_sub, nps, e, eps_sp, k)
     info = gpu.mesh_info(mesh)
     H = 1.0 / n_sub
