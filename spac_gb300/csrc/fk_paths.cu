@@ -265,8 +265,12 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
 // accumulators with global atomics; no warp ever waits for another, so an
 // item's longest path delays only its own warp.  Otherwise the CTA's warps
 // share the chunk slots described above.
+#ifndef FK_PATHS_MIN_BLOCKS_FP32
+#define FK_PATHS_MIN_BLOCKS_FP32 3
+#endif
 template <typename R, int PROB, int ST, bool WM>
-__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 3) paths_kernel(const LaunchArgs a) {
+__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : FK_PATHS_MIN_BLOCKS_FP32)
+    paths_kernel(const LaunchArgs a) {
   using SAcc = typename std::conditional<WM, double, typename SAccType<R, ST>::type>::type;
   using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
   constexpr int kPrec = std::is_same<R, double>::value ? 0 : 1;
