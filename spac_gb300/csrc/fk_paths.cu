@@ -265,14 +265,20 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
 // accumulators with global atomics; no warp ever waits for another, so an
 // item's longest path delays only its own warp.  Otherwise the CTA's warps
 // share the chunk slots described above.
-// FP32 stepping is issue-bound: 4 CTAs of 256 per SM (64 registers, with
-// ~150 B of spills) run the 8x8 assembly 2.9 % faster than 3 CTAs at 80
-// registers without spills.
+// FP32 stepping is issue-bound.  In slot mode 4 CTAs of 256 per SM (64
+// registers, ~150 B of spills) run the 8x8 assembly 2.9 % faster than 3 CTAs
+// at 80 registers without spills; warp mode (global moment atomics, few
+// paths per item) measured slower at 4 and keeps 3.
 #ifndef FK_PATHS_MIN_BLOCKS_FP32
 #define FK_PATHS_MIN_BLOCKS_FP32 4
 #endif
+#ifndef FK_PATHS_MIN_BLOCKS_FP32_WARP
+#define FK_PATHS_MIN_BLOCKS_FP32_WARP 3
+#endif
 template <typename R, int PROB, int ST, bool WM>
-__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : FK_PATHS_MIN_BLOCKS_FP32)
+__global__ void __launch_bounds__(256, std::is_same<R, double>::value
+                                           ? 2
+                                           : (WM ? FK_PATHS_MIN_BLOCKS_FP32_WARP : FK_PATHS_MIN_BLOCKS_FP32))
     paths_kernel(const LaunchArgs a) {
   using SAcc = typename std::conditional<WM, double, typename SAccType<R, ST>::type>::type;
   using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
