@@ -265,21 +265,14 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
 // accumulators with global atomics; no warp ever waits for another, so an
 // item's longest path delays only its own warp.  Otherwise the CTA's warps
 // share the chunk slots described above.
-// FP32 stepping is issue-bound.  In slot mode 4 CTAs of 256 per SM (64
-// registers, ~150 B of spills) run the 8x8 assembly 2.9 % faster than 3 CTAs
-// at 80 registers without spills; warp mode (global moment atomics, few
-// paths per item) measured slower at 4 and keeps 3.
-#ifndef FK_PATHS_MIN_BLOCKS_FP32
-#define FK_PATHS_MIN_BLOCKS_FP32 4
-#endif
-#ifndef FK_PATHS_MIN_BLOCKS_FP32_WARP
-#define FK_PATHS_MIN_BLOCKS_FP32_WARP 3
-#endif
-template <typename R, int PROB, int ST, bool WM>
-__global__ void __launch_bounds__(256, std::is_same<R, double>::value
-                                           ? 2
-                                           : (WM ? FK_PATHS_MIN_BLOCKS_FP32_WARP : FK_PATHS_MIN_BLOCKS_FP32))
-    paths_kernel(const LaunchArgs a) {
+// MB: minimum CTAs of 256 per SM the registers are sized for.  FP64: 2.
+// FP32: 3 (80 registers, no spills), and for patch-stencil slot mode also a
+// 4-CTA build (64 registers, ~150 B of spills), used where shared memory
+// admits 4 CTAs: it runs the 8x8 assembly 2.9 % faster, while point solves,
+// warp mode and the larger patches of the 32x32 mesh measured slower at 64
+// registers.
+template <typename R, int PROB, int ST, bool WM, int MB>
+__global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
   using SAcc = typename std::conditional<WM, double, typename SAccType<R, ST>::type>::type;
   using Acc = typename std::conditional<std::is_same<R, double>::value, AccD, AccK>::type;
   constexpr int kPrec = std::is_same<R, double>::value ? 0 : 1;
@@ -765,26 +758,44 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value
 }
 
 template <typename R, int PROB, bool WM>
-const void* paths_fn(int st) {
+const void* paths_fn(int st, bool four) {
+  constexpr int MB = std::is_same<R, double>::value ? 2 : 3;
   switch (st) {
-    case 1: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 1, WM>);
-    case 2: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2, WM>);
-    default: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 0, WM>);
+    case 1: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 1, WM, MB>);
+    case 2:
+      if constexpr (std::is_same<R, float>::value && !WM)
+        if (four) return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2, WM, 4>);
+      return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 2, WM, MB>);
+    default: return reinterpret_cast<const void*>(&paths_kernel<R, PROB, 0, WM, MB>);
   }
 }
 template <typename R, bool WM>
-const void* paths_fn_r(int problem, int st) {
+const void* paths_fn_r(int problem, int st, bool four) {
   switch (problem) {
-    case 1: return paths_fn<R, 1, WM>(st);
-    case 2: return paths_fn<R, 2, WM>(st);
-    case 3: return paths_fn<R, 3, WM>(st);
-    case 4: return paths_fn<R, 4, WM>(st);
-    default: return paths_fn<R, 0, WM>(st);
+    case 1: return paths_fn<R, 1, WM>(st, four);
+    case 2: return paths_fn<R, 2, WM>(st, four);
+    case 3: return paths_fn<R, 3, WM>(st, four);
+    case 4: return paths_fn<R, 4, WM>(st, four);
+    default: return paths_fn<R, 0, WM>(st, four);
   }
 }
-const void* select_paths(int problem, int precision, int st, bool warp_mode) {
-  if (warp_mode) return precision == 1 ? paths_fn_r<float, true>(problem, st) : paths_fn_r<double, true>(problem, st);
-  return precision == 1 ? paths_fn_r<float, false>(problem, st) : paths_fn_r<double, false>(problem, st);
+const void* select_paths_v(int problem, int precision, int st, bool warp_mode, bool four) {
+  if (warp_mode)
+    return precision == 1 ? paths_fn_r<float, true>(problem, st, false) : paths_fn_r<double, true>(problem, st, false);
+  return precision == 1 ? paths_fn_r<float, false>(problem, st, four) : paths_fn_r<double, false>(problem, st, false);
+}
+// The variant a launch uses: the 4-CTA build for FP32 patch-stencil slot
+// mode when 4 of its CTAs fit on an SM with this shared memory and block.
+const void* select_paths(int problem, int precision, int st, bool warp_mode, int block, size_t smem) {
+  if (precision == 1 && st == 2 && !warp_mode && block == 256) {
+    const void* f4 = select_paths_v(problem, precision, st, warp_mode, true);
+    int n = 0;
+    if (cudaFuncSetAttribute(f4, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f4, block, smem) == cudaSuccess && n >= 4)
+      return f4;
+    cudaGetLastError();
+  }
+  return select_paths_v(problem, precision, st, warp_mode, false);
 }
 
 }  // namespace
@@ -797,7 +808,7 @@ size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block, size_t smem,
                          cudaStream_t s, bool warp_mode) {
   if (block < 32 || block > 256 || block % 32 != 0) return cudaErrorInvalidValue;
-  const void* fn = select_paths(problem, precision, a.stencil_kind, warp_mode);
+  const void* fn = select_paths(problem, precision, a.stencil_kind, warp_mode, block, smem);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<LaunchArgs*>(&a)};
@@ -805,7 +816,7 @@ cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int gr
 }
 
 int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int, int block, size_t smem, bool warp_mode) {
-  const void* fn = select_paths(problem, precision, stencil_kind, warp_mode);
+  const void* fn = select_paths(problem, precision, stencil_kind, warp_mode, block, smem);
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem) != cudaSuccess) return 1;
