@@ -68,6 +68,38 @@ def point_solves(ctx, paths=10000, h=1e-3, precisions=(fk.FP64, fk.FP32)):
     return out
 
 
+def aniso_u(x, y):
+    return franke(x, y) * (1 + x * y)
+
+
+def robin(ctx, paths=4000, h=1e-4, n=24, mask=1 + 8, varphi=-0.5, rho=0.05):
+    """Reflecting sides (FK_PROBLEM_ROBIN, Paso_Reflejante): point solves on an
+    n x n grid of the unit square whose sides x = 0 and y = 1 reflect (Robin,
+    varphi) and whose other sides absorb; FP32 stepping with the exact-gradient
+    control variate (error against the exact u) and plain (throughput next to
+    the all-absorbing problem on the same points)."""
+    g = (np.arange(n) + 0.5) / n
+    xy = np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2)
+    u = aniso_u(xy[:, 0], xy[:, 1])
+    out = {"points": len(xy), "paths": paths, "h": h, "mask": mask, "varphi": varphi, "rho": rho}
+    b_abs = ctx.register_bvp(fk.ANISO)
+    b_rob = ctx.register_bvp(fk.ROBIN, prob=(mask, varphi, rho, 0))
+    b_cv = ctx.register_bvp(fk.ROBIN, cv=fk.CV_EXACT, prob=(mask, varphi, rho, 0))
+    for name, b in (("absorbing", b_abs), ("robin", b_rob), ("robin_exact_cv", b_cv)):
+        ctx.solve_points(b, xy[:8], 64, h, fk.FP32)  # warm-up
+        st, t = _sync_time(lambda: ctx.solve_points(b, xy, paths, h, fk.FP32))
+        key = "phi_VR" if name == "robin_exact_cv" else "phi"
+        var = np.maximum(st["phiphi_VR" if key == "phi_VR" else "phiphi"] - st[key] ** 2, 0)
+        se = np.sqrt(var / paths)
+        err = st[key] - u
+        out[name] = {"seconds": t, "kernel_ms": ctx.last_timing()[0], "paths_per_s": len(xy) * paths / t,
+                     "mean_steps": float(st["mean_steps"].mean()), "mean_se": float(se.mean())}
+        if name != "absorbing":
+            out[name].update(rms_error=float(np.sqrt(np.mean(err ** 2))), max_abs_error=float(np.abs(err).max()),
+                             bias_rms_est=float(np.sqrt(max(np.mean(err ** 2) - np.mean(se ** 2), 0.0))))
+    return out
+
+
 def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp64_fraction=0.05):
     rng = np.random.default_rng(seed)
     R = rng.uniform(0.25, 1.0, n_bvp)
@@ -257,7 +289,7 @@ def serial_driver(ctx, paths=1000, h=1e-5, n_radial=43, precision=fk.FP64, repea
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows", "serial_driver"])
+    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows", "serial_driver", "robin"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=2026)
     a = ap.parse_args()
@@ -270,6 +302,8 @@ def main():
         r = disk_rows(ctx, n_disks=max(1, int(900 * a.scale)))
     elif a.workload == "serial_driver":
         r = serial_driver(ctx, paths=max(16, int(1000 * a.scale)))
+    elif a.workload == "robin":
+        r = robin(ctx, paths=max(64, int(4000 * a.scale)))
     else:
         r = large(ctx, n_sub=max(2, int(round(32 * a.scale))), nodes_per_side=63 if a.scale >= 1 else 31)
     print(json.dumps({"workload": a.workload, **r}))
