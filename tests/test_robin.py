@@ -223,3 +223,21 @@ def test_gpu_assembly_with_a_reflecting_side_follows_the_oracle(gpu, orc, fk):
         assert np.allclose(r["item_G"][offs[i]:offs[i + 1]], G, atol=1e-9), i
         checked += 1
     assert checked >= 4
+
+
+@pytest.mark.gpu
+def test_gpu_fp32_assembly_with_reflecting_sides_pairs_with_fp64(gpu, fk):
+    """FP32 stepping (slot mode, the patch kernel's 4-CTA build where it fits)
+    on a mesh with reflecting sides x = 0 and y = 0, paired with FP64 on the
+    same stream: item B within half a standard error, G entries close."""
+    mesh = gpu.mesh_square_patches((0, 0, 1, 1), 3, 15, 0.25, 3.0, 20)
+    b = gpu.register_bvp(fk.ROBIN, prob=(1 + 2, -0.5, 0.05, 0))
+    N = 4000
+    gpu.set_stream(360)
+    r64 = gpu.assemble(mesh, b, N, 5e-4, fk.FP64)
+    gpu.set_stream(360)
+    r32 = gpu.assemble(mesh, b, N, 5e-4, fk.FP32)
+    se = np.sqrt(np.maximum(r64["item_stats"]["phiphi"] - r64["item_stats"]["phi"] ** 2, 1e-30) / N)
+    assert np.all(np.abs(r32["item_B"] - r64["item_B"]) < 0.5 * se + 1e-6)
+    assert np.allclose(r32["item_G"], r64["item_G"], atol=0.02)
+    assert r64["item_stats"]["n_capped"].sum() == 0
