@@ -105,80 +105,219 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- CPU side ----
-def _cpu_worker(args):
-    """Oracle node solves for a slice of items (one process per host core)."""
+# The CPU legs (cpu_baseline, --impl reference) never load the product
+# library: the layout comes from the oracle's numpy restatement of the mesh.
+def _cpu_items(eps_spacing=None):
+    """Items of the workload for the oracle: (item, x, y, patch rect, patch
+    chain coordinates), the Gaussian shape eps, and the item count."""
     import oracle_py as orc
-    items, nodes_xy, seed, N, h, k, eps = args
-    s = orc.Session(orc.RNG_PHILOX, seed=seed, stream=1)
-    b = orc.bvp(orc.__dict__.get("PROBLEM_ANISO", 2))
+    m = orc.square_patch_mesh(CFG["domain"], CFG["n_sub"], CFG["nodes_per_side"], CFG["enlarge"])
+    eps = (CFG["eps_spacing"] if eps_spacing is None else eps_spacing) / m["spacing"]
+    items = [(i, float(m["nodes"][g, 0]), float(m["nodes"][g, 1]), m["patches"][s]["rect"],
+              np.ascontiguousarray(m["patches"][s]["chain"])) for i, (g, s) in enumerate(m["items"])]
+    return items, eps
+
+
+def _cpu_worker(args):
+    """Oracle node solves (Gaussian k-nearest stencil) of a slice of items; one
+    process per host core."""
+    import oracle_py as orc
+    items, seed, stream, N, h, k, eps = args
+    s = orc.Session(orc.RNG_PHILOX, seed=seed, stream=stream)
+    b = orc.bvp(2)  # ORC_PROBLEM_ANISO
     t0 = time.perf_counter()
     npaths = 0
-    for (i, x, y, rect, gidx) in items:
-        s.node_solve_knn(b, x, y, rect, nodes_xy[gidx], k, eps, N, h, item=i)
+    for (i, x, y, rect, chain) in items:
+        s.node_solve_knn(b, x, y, rect, chain, k, eps, N, h, item=i)
         npaths += N
     return npaths, time.perf_counter() - t0
 
 
-def cpu_baseline(host_mesh, cores, budget_s=12.0):
-    """Times the CPU oracle port on a bounded sample of the same workload."""
+class CpuSample:
+    """A fixed, seeded sample of the workload's items, solved by the oracle
+    (FP64, 2,000 paths per item) on a pool of spawned processes, one per host
+    core; `run()` times one pass over the sample (wall clock)."""
+
+    N = 2000
+
+    def __init__(self, cores, budget_s):
+        self.items, self.eps = _cpu_items()
+        rng = np.random.default_rng(5)
+        # calibrate on one item (in this process), then size the sample so that
+        # one pass takes about budget_s on `cores` processes
+        n_cal, t_cal = _cpu_worker(([self.items[int(rng.integers(len(self.items)))]], 9, 1, self.N, CFG["h"],
+                                    CFG["knn"], self.eps))
+        per_core = max(1, int(budget_s * n_cal / max(t_cal, 1e-6) / self.N))
+        picks = rng.choice(len(self.items), size=min(len(self.items), per_core * cores), replace=False)
+        self.picks = picks
+        self.slices = [[self.items[int(i)] for i in picks[c::cores]] for c in range(cores)]
+        self.slices = [sl for sl in self.slices if sl]
+        self.pool = mp.get_context("spawn").Pool(len(self.slices))
+        self.pool.map(_cpu_worker, [(sl[:1], 9, 1, 16, CFG["h"], CFG["knn"], self.eps) for sl in self.slices])
+
+    @property
+    def cores(self):
+        return len(self.slices)
+
+    def describe(self, wall):
+        return (f"{len(self.picks)} of {len(self.items)} items x {self.N} paths per step (oracle FP64, "
+                f"one process per core, {wall:.2f} s wall per step)")
+
+    def run(self, stream=1):
+        t0 = time.perf_counter()
+        res = self.pool.map(_cpu_worker, [(sl, 9, stream, self.N, CFG["h"], CFG["knn"], self.eps)
+                                          for sl in self.slices])
+        wall = time.perf_counter() - t0
+        return sum(r[0] for r in res), wall
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+# The other configs' workloads, restated with numpy from their descriptions
+# (the GPU side builds them in spac_gb300.workloads with the same seeds).
+def _config1_points():
+    g = np.arange(1, 33) / 33.0
+    return np.array([(x, y) for x in g for y in g])
+
+
+def _config3_points(seed=2026, n_bvp=16, nodes=1 << 14):
+    """The 16 uneven disks: radius, centre, paths and h per node (the same
+    draws, in the same order, as spac_gb300.workloads.uneven)."""
+    rng = np.random.default_rng(seed)
+    R = rng.uniform(0.25, 1.0, n_bvp)
+    centers = np.stack([2.5 * np.arange(n_bvp), np.zeros(n_bvp)], axis=1)
+    per = nodes // n_bvp
+    xy, disk = [], []
+    for k in range(n_bvp):
+        r = R[k] * np.sqrt(rng.uniform(0, 1, per))
+        th = rng.uniform(0, 2 * np.pi, per)
+        xy.append(np.stack([centers[k, 0] + r * np.cos(th), centers[k, 1] + r * np.sin(th)], axis=1))
+        disk += [k] * per
+    xy = np.concatenate(xy)
+    disk = np.array(disk)
+    paths = np.maximum(1, np.round(np.exp(rng.uniform(np.log(1e3), np.log(1e5), len(xy))))).astype(np.int64)
+    h = rng.choice([1e-3, 5e-4], len(xy))
+    return xy, disk, R, centers, paths, h
+
+
+def _cpu_job(args):
+    """Oracle solves of one slice of a config's sample: point solves (configs 1
+    and 3) or Gaussian-stencil node solves (config 5).  Returns (paths, nodes,
+    seconds)."""
+    import oracle_py as orc
+    kind, jobs = args
+    s = orc.Session(orc.RNG_PHILOX, seed=9, stream=1)
+    t0 = time.perf_counter()
+    npaths = 0
+    for j in jobs:
+        if kind == "points":
+            i, problem, dom, dshape, prob, x, y, N, h = j
+            s.point_solve(orc.bvp(problem, dom=dom, dom_shape=dshape, prob=prob), x, y, N, h, item=i)
+        else:
+            i, x, y, rect, chain, k, eps, N, h = j
+            s.node_solve_knn(orc.bvp(0), x, y, rect, chain, k, eps, N, h, item=i)
+        npaths += N
+    return npaths, len(jobs), time.perf_counter() - t0
+
+
+def cpu_configs(cores, budget_s=4.0):
+    """The CPU oracle (FP64, the reference's arithmetic, pinned to its own
+    sources) on bounded seeded samples of configs 1, 3 and 5, one spawned
+    process per host core: paths/s and node solves/s beside the GPU's."""
     import oracle_py as orc
     orc.build(ref=False)
-    ctx, mesh = host_mesh
-    info = ctx.mesh_info(mesh)
-    row, ixy, st, fr = ctx.mesh_items(mesh)
-    nxy, _ = ctx.mesh_nodes(mesh)
-    n_sub, e = CFG["n_sub"], CFG["enlarge"]
-    H = 1.0 / n_sub
-    eps = CFG["eps_spacing"] / info["spacing"]
-    gid = {s: ctx.mesh_stencil_nodes(mesh, s) for s in range(info["n_stencils"])}
+    rng = np.random.default_rng(11)
+    samples = {}
+    p1 = _config1_points()
+    samples["config1"] = ("points", [(i, 0, (0, 0, 1, 1), orc.RECT, (0, 0, 0, 0), x, y, 10000, 1e-3)
+                                     for i, (x, y) in enumerate(p1)], "32x32 nodes x 1e4 paths, h=1e-3, Franke")
+    xy, disk, R, cen, paths, h = _config3_points()
+    jobs = [(i, 3, (R[disk[i]], cen[disk[i], 0], cen[disk[i], 1], 0), orc.CIRCLE,
+             (cen[disk[i], 0], cen[disk[i], 1], R[disk[i]], 0), xy[i, 0], xy[i, 1], int(paths[i]), h[i])
+            for i in range(len(xy))]
+    samples["config3"] = ("points", jobs, "16 uneven disks, 2^14 nodes, paths log-uniform 1e3..1e5, h in {1e-3, 5e-4}")
+    m = orc.square_patch_mesh((0, 0, 1, 1), 32, 63, 0.25)
+    eps = 3.0 / m["spacing"]
 
-    def item(i):
-        a, b = divmod(int(st[i]), n_sub)
-        return (i, ixy[i, 0], ixy[i, 1], ((a - e) * H, (b - e) * H, (a + 1 + e) * H, (b + 1 + e) * H), gid[int(st[i])])
+    class Items5:  # the config-5 items as jobs, built on access (409k chain copies would not fit)
+        def __len__(self):
+            return len(m["items"])
 
-    # calibrate on one item, then size the sample to the time budget
-    rng = np.random.default_rng(5)
-    N = 2000
-    n_cal, t_cal = _cpu_worker(([item(int(rng.integers(info["n_items"])))], nxy, 9, N, CFG["h"], CFG["knn"], eps))
-    rate1 = n_cal / max(t_cal, 1e-6)
-    per_core = max(1, int(budget_s * rate1 / N / 1.5))
-    picks = rng.choice(info["n_items"], size=min(info["n_items"], per_core * cores), replace=False)
-    slices = [[item(int(i)) for i in picks[c::cores]] for c in range(cores)]
-    args = [(sl, nxy, 9, N, CFG["h"], CFG["knn"], eps) for sl in slices if sl]
-    t0 = time.perf_counter()
-    with mp.get_context("spawn").Pool(len(args)) as pool:
-        res = pool.map(_cpu_worker, args)
-    wall = time.perf_counter() - t0
-    npaths = sum(r[0] for r in res)
-    return {"value": npaths / wall, "unit": "paths/s", "cores": len(args), "kind": "port",
-            "sample": f"{len(picks)} of {info['n_items']} items x {N} paths (oracle FP64, one process per core, "
-                      f"{wall:.1f} s wall)"}
+        def __getitem__(self, i):
+            g, st = m["items"][i]
+            return (i, float(m["nodes"][g, 0]), float(m["nodes"][g, 1]), m["patches"][st]["rect"],
+                    np.ascontiguousarray(m["patches"][st]["chain"]), 20, eps, 1000, 2.5e-4)
+
+    samples["config5"] = ("knn", Items5(), "32x32 square-patch items x 1000 paths, h=2.5e-4, Gaussian 20-NN stencil")
+    out = {}
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for name, (kind, jobs, desc) in samples.items():
+            # calibrate on a few jobs, then take a seeded sample worth budget_s on `cores` processes
+            probe = [jobs[int(i)] for i in rng.choice(len(jobs), size=min(4, len(jobs)), replace=False)]
+            n_cal, k_cal, t_cal = _cpu_job((kind, probe))
+            per_job = t_cal / max(k_cal, 1)
+            n_take = int(min(len(jobs), max(cores, budget_s * cores / max(per_job, 1e-6))))
+            pick = rng.choice(len(jobs), size=n_take, replace=False)
+            sl = [(kind, [jobs[int(i)] for i in pick[c::cores]]) for c in range(cores)]
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_job, [x for x in sl if x[1]])
+            wall = time.perf_counter() - t0
+            npaths, nodes = sum(r[0] for r in res), sum(r[1] for r in res)
+            out[name] = {"paths_per_s": npaths / wall, "node_solves_per_s": nodes / wall, "cores": cores,
+                         "kind": "port", "sample": f"{nodes} of {len(jobs)} nodes ({desc}); oracle FP64, "
+                                                   f"{wall:.2f} s wall"}
+    return out
+
+
+def cpu_baseline(cores, budget_s=12.0):
+    """The CPU oracle port timed on a bounded sample of the same workload."""
+    import oracle_py as orc
+    orc.build(ref=False)
+    cs = CpuSample(cores, budget_s)
+    try:
+        npaths, wall = cs.run()
+    finally:
+        cs.close()
+    return {"value": npaths / wall, "unit": "paths/s", "cores": cs.cores, "kind": "port",
+            "sample": cs.describe(wall)}
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's FK node solve
+    (pinned bit for bit to the reference's own sources) on all host cores.
+    Each step is one pass over a fixed sample of the workload's items; W
+    untimed passes, then K timed ones."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    from spac_gb300 import fk
+    import oracle_py as orc
+    orc.build(ref=False)
     cores = os.cpu_count() or 1
-    hctx = fk.Context(device=-1)
-    mesh = hctx.mesh_square_patches(CFG["domain"], CFG["n_sub"], CFG["nodes_per_side"], CFG["enlarge"],
-                                    CFG["eps_spacing"], CFG["knn"])
-    vals = []
-    base = None
-    for k in range(args.steps):
-        base = cpu_baseline((hctx, mesh), cores, budget_s=8.0)
-        vals.append(base["value"])
-    v = float(np.mean(vals))
-    info = hctx.mesh_info(mesh)
-    total_paths = info["n_items"] * CFG["paths_per_item"]
+    cs = CpuSample(cores, budget_s=2.0)
+    try:
+        for w in range(args.warmup):
+            cs.run(stream=100 + w)
+        walls, paths = [], 0
+        for k in range(args.steps):
+            n, wall = cs.run(stream=1 + k)
+            walls.append(wall)
+            paths += n
+    finally:
+        cs.close()
+    t_step = float(np.mean(walls))
+    v = paths / float(np.sum(walls))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "paths/s", "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * total_paths / v, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(CFG, precision="fp64", note="CPU oracle port of the reference FK node solve "
-                           "(the reference itself has no square-patch/Gaussian stencil; its sources need Eigen "
-                           "and Boost, absent on the GPU host)"),
-            "cpu_baseline": dict(base, value=v),
+            "config": dict(CFG, precision="fp64", paths_per_item=cs.N, items_per_step=len(cs.picks),
+                           sample=cs.describe(t_step),
+                           note="CPU oracle port of the reference FK node solve (the reference itself has no "
+                                "square-patch/Gaussian stencil; its sources need Eigen and Boost, absent on the GPU "
+                                "host); mesh from the oracle's own layout code"),
+            "cpu_baseline": {"value": v, "unit": "paths/s", "cores": cs.cores, "kind": "port",
+                             "sample": cs.describe(t_step)},
             "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -213,6 +352,7 @@ def main():
     ap.add_argument("--paths", type=int, default=CFG["paths_per_item"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-metric", action="store_true", help="skip the time-to-1e-3 comparison")
+    ap.add_argument("--no-configs", action="store_true", help="skip configs 1, 3 and 5 (GPU and CPU)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -223,14 +363,13 @@ def main():
     CFG["paths_per_item"] = args.paths
 
     # CPU baseline first (spawned pool, before any GPU call), rank 0 at N=1 only
-    from spac_gb300 import fk
-    base = None
+    base = cpu_cfg = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        hctx = fk.Context(device=-1)
-        hmesh = hctx.mesh_square_patches(CFG["domain"], CFG["n_sub"], CFG["nodes_per_side"], CFG["enlarge"],
-                                         CFG["eps_spacing"], CFG["knn"])
-        base = cpu_baseline((hctx, hmesh), os.cpu_count() or 1)
+        base = cpu_baseline(os.cpu_count() or 1)
+        if not args.no_configs:
+            cpu_cfg = cpu_configs(os.cpu_count() or 1)
 
+    from spac_gb300 import fk
     import torch
     dist = None
     if world > 1:
@@ -251,9 +390,24 @@ def main():
     ext = torch.cuda.ExternalStream(ctx.cuda_stream())
     dptr = lambda t: fk.C.cast(t.data_ptr(), fk._dp)
 
-    def step_device():
-        rc = ctx.L.fk_assemble(ctx.h, mesh, bvp, paths, None, CFG["h"], prec, dptr(val), dptr(Bd), None, None, None)
+    def step_device(precision=prec):
+        rc = ctx.L.fk_assemble(ctx.h, mesh, bvp, paths, None, CFG["h"], precision, dptr(val), dptr(Bd), None, None,
+                               None)
         ctx.check(rc)
+
+    def timed_device(n, precision=prec):
+        times, kern = [], []
+        for _ in range(n):
+            with torch.cuda.stream(ext):
+                flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            step_device(precision)
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            kern.append(ctx.last_timing())
+        return times, kern
 
     for _ in range(args.warmup):
         step_device()
@@ -262,18 +416,8 @@ def main():
         dist.barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    times, kern = [], []
     torch.cuda.synchronize()
-    for _ in range(args.steps):
-        with torch.cuda.stream(ext):
-            flush.fill_(1.0)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(ext)
-        step_device()
-        e1.record(ext)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-        kern.append(ctx.last_timing())
+    times, kern = timed_device(args.steps)
     torch.cuda.synchronize()
     clocks = sampler.stop()
     t_step = float(np.sum(times)) / args.steps  # ms
@@ -301,19 +445,28 @@ def main():
     item_bytes = info["n_items"] * (96 + 12)
     d2h = 8 * (info["nnz"] + info["n_rows"]) + 16
 
+    # the same assembly with FP64 stepping (the reference's arithmetic): the
+    # precision-matched GPU figure beside the CPU oracle's FP64 one
+    step_device(fk.FP64)
+    t64, _ = timed_device(2, fk.FP64)
+    fp64 = {"value": total_paths / (float(np.mean(t64)) / 1000.0), "unit": "paths/s", "ms_per_step": float(np.mean(t64)),
+            "note": "same assembly, FP64 stepping and FP64 stencil products, device buffers"}
+
     # roofline of the dominant kernel (the path kernel): algorithmic flops / its event time
     k_ms = float(np.mean([k[0] for k in kern]))
     f_ms = float(np.mean([k[1] for k in kern]))
-    steps_per_assembly = _mean_steps(ctx, mesh, bvp, prec, paths)
+    steps_per_assembly, visited = _mean_steps(ctx, mesh, bvp, prec, paths)
     flops = total_paths * steps_per_assembly * FLOPS_PER_STEP
     peaks, src = _peaks()
     smax = peaks.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12  # TFLOP/s, nominal at the maximum SM clock
     achieved = flops / (k_ms / 1000.0) / 1e12
     traffic = _read_traffic()
-    ttt = None
+    ttt = cfgs = None
     if rank == 0 and not args.no_metric:
-        ttt = time_to_target_all(ctx, mesh)
+        ttt = time_to_target_all(ctx)
+    if rank == 0 and not args.no_configs:
+        cfgs = other_configs(ctx, cpu_cfg)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -323,26 +476,51 @@ def main():
                 "e2e": {"value": world * total_paths / e2e_step, "unit": "paths/s", "h2d_bytes_per_step": item_bytes,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": 2 * args.steps,
+                "node_solves_per_s": world * info["n_items"] / (t_step / 1000.0),
+                "fp64_stepping": fp64,
                 "kernels_ms": {"paths": k_ms, "finalize_scatter": f_ms},
                 "mean_steps_per_path": steps_per_assembly,
-                "roofline_scatter": _scatter_roofline(info, f_ms, peaks, src),
+                "roofline_scatter": _scatter_roofline(info, f_ms, peaks, src, visited),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                              "frac": achieved / fp32_peak, "traffic": traffic,
                              "peak_source": f"nominal FP32: 152 SMs x 128 lanes x 2 flop x {smax:.0f} MHz "
                                             f"(sm_max_mhz of MEASURED_PEAKS.json, {src}); no FP32 figure is measured",
                              "flops_per_step": FLOPS_PER_STEP,
+                             "traffic_source": "ncu dram bytes of one launch, committed capture",
                              # the path kernel is bound by instruction issue: ncu pipe figures of the
-                             # committed capture (profiles/paths_kernel_8x8_assembly.md)
+                             # committed capture of this kernel on this workload
                              "ncu_pipes": {k[len("paths_kernel_"):]: v for k, v in _read_profile_figures().items()
                                            if k.startswith("paths_kernel_") and not k.endswith("per_launch")}},
                 "clocks": clocks,
                 "time_to_1e-3": ttt,
+                "configs": cfgs,
                 "cpu_baseline": base}
         print(json.dumps(line))
     ctx.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def other_configs(ctx, cpu=None):
+    """Configs 1, 3 and 5 on the GPU (spac_gb300.workloads), each beside the
+    CPU oracle's figure on a sample of the same workload when it was timed."""
+    from spac_gb300 import workloads as wl
+    out = {}
+    c1 = wl.point_solves(ctx)
+    out["config1"] = {"gpu": c1}
+    c3 = wl.uneven(ctx)
+    ctx.set_launch(0, 0)  # (the autotuner keeps its launch shape in the context)
+    out["config3"] = {"gpu": c3}
+    c5 = wl.large(ctx)
+    out["config5"] = {"gpu": c5}
+    if cpu:
+        for k in out:
+            out[k]["cpu"] = cpu.get(k)
+        out["config1"]["gpu_over_cpu_paths_per_s_fp64"] = c1["fp64"]["paths_per_s"] / cpu["config1"]["paths_per_s"]
+        out["config3"]["gpu_over_cpu_paths_per_s"] = c3["fp32"]["paths_per_s"] / cpu["config3"]["paths_per_s"]
+        out["config5"]["gpu_over_cpu_paths_per_s"] = c5["paths_per_s"] / cpu["config5"]["paths_per_s"]
+    return out
 
 
 def _franke_np(x, y):
@@ -368,13 +546,14 @@ def _pinned(n):
     return _PINNED[n]
 
 
-def _assemble_stats(ctx, mesh, bvp, paths, prec, h, kernels=None):
-    """One fk_assemble call into pinned host buffers (CSR values and B);
-    returns (seconds, per-item stats).  `kernels`, if a list, receives the
-    path and finalize kernel times (ms)."""
+def _assemble_host(ctx, mesh, bvp, paths, prec, h, kernels=None, stats=False):
+    """One fk_assemble call into pinned host buffers (CSR values and B, as a
+    caller of the C ABI keeps them); returns (seconds, val, B, per-item
+    stats or None).  `kernels`, if a list, receives the path and finalize
+    kernel times (ms)."""
     from spac_gb300 import fk
     info = ctx.mesh_info(mesh)
-    st = (fk.Stats * info["n_items"])()
+    st = (fk.Stats * info["n_items"])() if stats else None
     val = _pinned(info["nnz"])
     B = _pinned(info["n_rows"])
     t0 = time.perf_counter()
@@ -383,55 +562,150 @@ def _assemble_stats(ctx, mesh, bvp, paths, prec, h, kernels=None):
     dt = time.perf_counter() - t0
     if kernels is not None:
         kernels.extend(ctx.last_timing()[:2])
-    return dt, fk.stats_array(st)
+    return dt, val.copy(), B.copy(), fk.stats_array(st) if stats else None
 
 
-def time_to_target_all(ctx, mesh, target=1e-3, hs=(5e-4, 1e-4, 5e-5)):
-    """time_to_target at the configured h and at smaller steps (the bias floor
-    of the configured h can exceed the target)."""
-    res = {}
-    for h in hs:
-        res["h=%g" % h] = time_to_target(ctx, mesh, target=target, h=h)
+class AssembledSystem:
+    """The assembled 8x8 system G u = B of one mesh and the exact solution at
+    its nodes: the error measures of the time-to-1e-3 metric.
+
+    row residual  e_r = (sum_j val_rj u(x_j) - B_r) / diag_r, with u the exact
+                  solution: the average, over the row's items, of the item's
+                  FK estimate of u(x_r) given the exact values at its stencil
+                  nodes, minus u(x_r) (the reference's own check G u_exact ~ B,
+                  Mesh/Interfaz.cpp:252-262, divided by the diagonal).  It
+                  includes the exit stencil's interpolation error.
+    GMRES error   the host GMRES solution of the assembled system minus u at
+                  the nodes (the system the reference solves,
+                  Solvers/SistemaLinealSolverGMRES.hpp:157-597)."""
+
+    def __init__(self, ctx, mesh):
+        self.ctx, self.mesh = ctx, mesh
+        self.rp, self.col, v0 = ctx.mesh_csr(mesh)
+        xy, _ = ctx.mesh_nodes(mesh)
+        self.u = _u_aniso(xy)
+        n = len(self.rp) - 1
+        self.diag = v0[self.rp[:-1] + np.array([np.searchsorted(self.col[self.rp[i]:self.rp[i + 1]], i)
+                                                 for i in range(n)])]
+        self.row, ixy, _, _ = ctx.mesh_items(mesh)
+        self.u_items = _u_aniso(ixy)
+
+    def residual(self, val, B):
+        Au = np.add.reduceat(val * self.u[self.col], self.rp[:-1])
+        return (Au - B) / self.diag
+
+    def gmres_rms(self, val, B):
+        from spac_gb300 import fk
+        x, it, res, rc = fk.gmres(self.rp, self.col, val, B, tol=1e-10, max_iter=3000, restart=60)
+        return {"rms": float(np.sqrt(np.mean((x - self.u) ** 2))), "max": float(np.abs(x - self.u).max()),
+                "iterations": it, "rel_resid": res, "converged": rc == 0}
+
+    def calibrate(self, bvp, h, n_cal, streams=(9001, 9002)):
+        """Two independent assemblies at n_cal paths per item: their residual
+        difference gives the per-path variance of the row residual (bias
+        cancels), their mean the bias.  Returns (bias^2, variance per path,
+        the exact-exit item variance of the first run)."""
+        from spac_gb300 import fk
+        es, st0 = [], None
+        saved = self.ctx.get_stream()
+        for s in streams:
+            self.ctx.set_stream(s)
+            _, val, B, st = _assemble_host(self.ctx, self.mesh, bvp, n_cal, fk.FP32, h, stats=st0 is None)
+            es.append(self.residual(val, B))
+            st0 = st if st0 is None else st0
+        self.ctx.set_stream(saved)
+        var_path = float(np.mean((es[0] - es[1]) ** 2) / 2.0 * n_cal)
+        bias2 = max(float(np.mean(((es[0] + es[1]) / 2) ** 2)) - var_path / (2 * n_cal), 0.0)
+        return bias2, var_path, st0
+
+
+def _rms(e):
+    return float(np.sqrt(np.mean(e ** 2)))
+
+
+def weight_sum_defect(eps_spacing, k=20):
+    """Sum of the Gaussian k-nearest weights w = A^-1 phi(x) at points of a
+    straight chain of equispaced nodes (the inside of a patch side): 1 at a
+    node, less in between (Gaussian RBF interpolation does not reproduce
+    constants).  The probe points sit at fractions 0, 1/4 and 1/2 of a spacing
+    from a node in the middle of the window."""
+    x = np.arange(k, dtype=np.float64)
+    A = np.exp(-(eps_spacing * (x[:, None] - x[None, :])) ** 2)
+    out = {}
+    for name, f in (("at_node", 0.0), ("quarter", 0.25), ("midpoint", 0.5)):
+        t = k // 2 - 1 + f
+        phi = np.exp(-(eps_spacing * (t - x)) ** 2)
+        out[name] = float(np.linalg.solve(A, phi).sum())
+    return out
+
+
+def time_to_target_all(ctx, target=1e-3):
+    """The metric on the assembled system at the configured stencil shape
+    (eps = 3/spacing) and at eps = 1/spacing, at the configured h and at
+    smaller steps (the O(h) bias floor of h = 5e-4 exceeds the target)."""
+    res = {"error_measure": "RMS over rows of the row residual (sum_j val_rj u(x_j) - B_r) / diag_r with the exact u",
+           "weight_sum": {"eps_spacing=3": weight_sum_defect(3.0), "eps_spacing=1": weight_sum_defect(1.0)}}
+    for eps_sp in (3.0, 1.0):
+        mesh = ctx.mesh_square_patches(CFG["domain"], CFG["n_sub"], CFG["nodes_per_side"], CFG["enlarge"], eps_sp,
+                                       CFG["knn"])
+        sysm = AssembledSystem(ctx, mesh)
+        hs = (5e-4,) if eps_sp == 3.0 else (5e-4, 1e-4, 5e-5, 2.5e-5)
+        r = {}
+        for h in hs:
+            r["h=%g" % h] = time_to_target(ctx, sysm, target=target, h=h)
+        res["eps_spacing=%g" % eps_sp] = r
     return res
 
 
-def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=600, pilot_h=1e-3, train_steps=800,
-                   table=128, lr=3e-2, batch=4096, fit_output=True):
-    """Time to `target` RMS node error on the assembly, plain FK vs the learned
-    control variate (both FP32 stepping, same h).
+def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=600, pilot_h=1e-3, train_steps=50,
+                   table=128, lr=1e-2, batch=4096, fit_output=True, n_cal=4000, only=None, gmres=True):
+    """Time to `target` RMS row residual of the assembled system, plain FK vs
+    the learned control variate (both FP32 stepping, same h, same paths for
+    every item).
 
-    Node error of an item = its FK estimate of u at the node (exit value taken
-    exactly, so the figure does not depend on the exit stencil) minus the exact
-    u.  RMS^2 = bias^2 + mean(var)/N: each method's N comes from an untimed
-    calibration run.  The learned-CV time includes its pilot (whole-domain
-    point solves at pilot_grid^2 collocation points: boundary data only),
-    training (train_steps Adam steps, batch 4096; with fit_output the output
-    layer is then refitted by least squares on the hidden features), the
-    gradient table and the assembly with the control term."""
+    RMS^2 = bias^2 + var/N per method, from two untimed calibration
+    assemblies; the timed assembly runs at the N that this predicts for the
+    target (x 1.05), and again at a larger N if its measured RMS is above the
+    target.  The learned-CV time includes its pilot (whole-domain point solves
+    at pilot_grid^2 collocation points: boundary data only), training
+    (train_steps Adam steps; with fit_output the output layer is then refitted
+    by least squares on the hidden features), the gradient table and the
+    assembly with the control term.  Each timed assembly's system is also
+    solved by the host GMRES and its node error reported."""
     from spac_gb300 import fk
-    info = ctx.mesh_info(mesh)
-    row, ixy, stn, fr = ctx.mesh_items(mesh)
-    u_exact = _u_aniso(ixy)
     prec = fk.FP32
     b_plain = ctx.register_bvp(fk.ANISO)
+    out = {"target": target}
 
-    def rms_of(st):
-        return float(np.sqrt(np.mean((st["phi_VR"] - u_exact) ** 2)))
+    def run_to_target(bvp, bias2, var_path, floor_paths=32):
+        budget = target ** 2 - bias2
+        n = max(floor_paths, int(np.ceil(1.05 * var_path / budget)))
+        attempts = []
+        for _ in range(3):
+            kern = []
+            t, val, B, st = _assemble_host(ctx, sysm.mesh, bvp, n, prec, h, kern)
+            e = sysm.residual(val, B)
+            attempts.append({"paths_per_item": n, "seconds": t, "rms": _rms(e), "kernels_ms": kern})
+            if _rms(e) <= target:
+                break
+            n = int(np.ceil(n * 1.05 * max(_rms(e) ** 2 - bias2, 1e-30) / budget))
+        last = dict(attempts[-1])
+        if gmres:
+            last["gmres_node_error"] = sysm.gmres_rms(val, B)
+        if len(attempts) > 1:
+            last["earlier_attempts"] = attempts[:-1]
+        return last
 
-    # calibration of the plain method
-    n_cal = 4000
-    _, st = _assemble_stats(ctx, mesh, b_plain, n_cal, prec, h)
-    var_p = np.maximum(st["phiphi_VR"] - st["phi_VR"] ** 2, 0)
-    bias2 = max(rms_of(st) ** 2 - var_p.mean() / n_cal, 0.0)
-    out = {"target": target, "bias_rms_est": float(np.sqrt(bias2)), "plain_var_mean": float(var_p.mean())}
+    bias2, var_p, st_cal = sysm.calibrate(b_plain, h, n_cal)
+    out["bias_rms_est"] = float(np.sqrt(bias2))
+    # diagnostic: the same items scored with the exact exit value instead of the stencil
+    out["diagnostic_exact_exit_rms_at_calibration"] = _rms(st_cal["phi_VR"] - sysm.u_items)
+    out["plain_var_per_path"] = var_p
     if bias2 >= 0.8 * target ** 2:
-        out["unreachable"] = "bias floor at h=%g is above 0.9 x target" % h
+        out["unreachable"] = "bias floor %.2e of the row residual at h=%g is above 0.9 x target" % (np.sqrt(bias2), h)
         return out
-    budget = target ** 2 - bias2
-    n_plain = int(np.ceil(1.05 * var_p.mean() / budget))
-    kp = []
-    t_plain, st = _assemble_stats(ctx, mesh, b_plain, n_plain, prec, h, kp)
-    out["plain"] = {"paths_per_item": n_plain, "seconds": t_plain, "rms": rms_of(st), "kernels_ms": kp}
+    if only != "cv":
+        out["plain"] = run_to_target(b_plain, bias2, var_p)
 
     # learned control variate: pilot from boundary data only
     t0 = time.perf_counter()
@@ -448,10 +722,11 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=60
     mid = mid.value
     tgt = np.ascontiguousarray(pst["phi"])
     pxy = np.ascontiguousarray(pxy)
-    hist = np.zeros(train_steps, dtype=np.float32)
+    hist = np.zeros(max(train_steps, 1), dtype=np.float32)
     t1 = time.perf_counter()
-    ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp), None,
-                                 train_steps, batch, lr, 777, hist.ctypes.data_as(fk._fp)))
+    if train_steps > 0:
+        ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp),
+                                     None, train_steps, batch, lr, 777, hist.ctypes.data_as(fk._fp)))
     t_train = time.perf_counter() - t1
     t_fit = 0.0
     if fit_output:
@@ -464,36 +739,35 @@ def time_to_target(ctx, mesh, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=60
     ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
     t_table = time.perf_counter() - t2
     b_cv = ctx.register_bvp(fk.ANISO, cv=fk.CV_MLP, mlp_id=mid)
-    # calibration of the control-variate run (untimed, as for plain)
-    _, stc = _assemble_stats(ctx, mesh, b_cv, n_cal, prec, h)
-    var_c = np.maximum(stc["phiphi_VR"] - stc["phi_VR"] ** 2, 0)
-    n_cv = max(32, int(np.ceil(1.05 * var_c.mean() / budget)))
-    kc = []
-    t_run, stc = _assemble_stats(ctx, mesh, b_cv, n_cv, prec, h, kc)
-    t_cv = t_pilot + t_train + t_fit + t_table + t_run
-    out["learned_cv"] = {"paths_per_item": n_cv, "seconds": t_cv, "rms": rms_of(stc), "pilot_s": t_pilot,
-                         "train_s": t_train, "train_steps": train_steps, "fit_output_s": t_fit, "table_s": t_table,
-                         "run_s": t_run, "run_kernels_ms": kc,
-                         "pilot_kernel_ms": pilot_kernel_ms,
-                         "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
-                         "train_loss_first_last": [float(hist[0]), float(hist[-1])]}
-    out["variance_reduction"] = float(var_p.mean() / max(var_c.mean(), 1e-300))
-    out["speedup_cv_over_plain"] = t_plain / t_cv
-    out["speedup_cv_run_only"] = t_plain / t_run
+    bias2_c, var_c, _ = sysm.calibrate(b_cv, h, n_cal)
+    cv = run_to_target(b_cv, bias2_c, var_c)
+    t_fixed = t_pilot + t_train + t_fit + t_table
+    cv.update({"seconds_run": cv["seconds"], "seconds": t_fixed + cv["seconds"], "pilot_s": t_pilot,
+               "train_s": t_train, "train_steps": train_steps, "batch": batch, "lr": lr, "fit_output_s": t_fit,
+               "table_s": t_table, "pilot_kernel_ms": pilot_kernel_ms, "bias_rms_est": float(np.sqrt(bias2_c)),
+               "var_per_path": var_c,
+               "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
+               "train_loss_first_last": [float(hist[0]), float(hist[max(train_steps, 1) - 1])]})
+    out["learned_cv"] = cv
+    out["variance_reduction"] = float(var_p / max(var_c, 1e-300))
+    if "plain" in out:
+        out["speedup_cv_over_plain"] = out["plain"]["seconds"] / cv["seconds"]
+        out["speedup_cv_run_only"] = out["plain"]["seconds"] / cv["seconds_run"]
     return out
 
 
 def _mean_steps(ctx, mesh, bvp, prec, paths):
-    """Mean Euler steps per path of the workload (from the kernel's own counters)."""
+    """Mean Euler steps per path of the workload (from the kernel's own
+    counters), and the stencil windows the exits chose (None: not counted)."""
     from spac_gb300 import fk
     st = (fk.Stats * ctx.mesh_info(mesh)["n_items"])()
     rc = ctx.L.fk_assemble(ctx.h, mesh, bvp, min(paths, 2000), None, CFG["h"], prec, None, None, None, None, st)
     ctx.check(rc)
     ms = np.array([s.mean_steps for s in st])
-    return float(ms.mean())
+    return float(ms.mean()), None
 
 
-def _scatter_roofline(info, f_ms, peaks, src):
+def _scatter_roofline(info, f_ms, peaks, src, visited=None):
     """HBM roofline of the finalize/scatter kernel.  Algorithmic bytes per
     launch: per item its FP64 stencil moments (nwin x k words of the patch's
     windows), its 12 FP64 statistics, a read-modify-write of its G entries in
@@ -509,7 +783,7 @@ def _scatter_roofline(info, f_ms, peaks, src):
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": _read_profile_figures().get("finalize_dram_bytes_per_launch"), "algorithmic_bytes": bytes_,
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({src})",
-            "note": "latency-bound: CTA-wide phases per item (moments staged, window products, CSR scatter); profiles/"}
+            "note": "latency-bound: CTA-wide phases per item (moments staged, window products, CSR scatter)"}
 
 
 def _read_profile_figures():

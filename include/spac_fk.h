@@ -121,6 +121,16 @@ int fk_set_max_steps(fk_ctx* ctx, int max_steps);
 /* Launch shape of the path kernel: threads per block and paths per work
  * chunk (0 = autotuned / default). */
 int fk_set_launch(fk_ctx* ctx, int block_threads, int chunk_paths);
+/* Limits of the kernels' bounded waits, in seconds (0 restores the default).
+ * slot_wait_s: a path-kernel warp's wait for a chunk slot that another warp
+ * of its CTA is still refilling (default 60 s + 1 us x max_steps, far above
+ * any real wait, which the step cap bounds); barrier_s: a CTA's wait at a
+ * grid barrier of the persistent MLP trainer (default 5 s).  A wait that runs
+ * out ends its kernel early and the call returns FK_ERR_CUDA ("... timed
+ * out"); the context stays usable, and that call's outputs (or the network's
+ * parameters, for a training call) are incomplete.  No reference
+ * counterpart: the reference has no waits between threads. */
+int fk_set_wait_limits(fk_ctx* ctx, double slot_wait_s, double barrier_s);
 /* cudaStream_t of the context, as void* */
 int fk_cuda_stream(const fk_ctx* ctx, void** stream);
 /* Device time (ms, CUDA events on the context stream) of the kernels of the
@@ -156,20 +166,27 @@ int fk_autotune_points(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy,
 
 /* ---- point solves without any allocation ----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory while they solve: code running during CUDA stream capture, embedders
- * that reserve all device memory up front and forbid later allocations, and
- * real-time hosts that cannot afford an allocation's latency.  Same kernels
- * and random stream as fk_solve_points (point i, path p uses the Philox
- * counter (step/2, p, i, stream_id) under key seed); no fk_ctx is needed.
+ * memory when they solve: embedders that reserve all device memory up front
+ * and forbid later allocations (a framework's caching allocator owns the GPU),
+ * and real-time hosts that cannot afford an allocation's latency or the
+ * device synchronisation it may imply.  Same kernels and random stream as
+ * fk_solve_points (point i, path p uses the Philox counter
+ * (step/2, p, i, stream_id) under key seed), and every point's paths are
+ * split into chunks over the whole grid as there; no fk_ctx is needed.
  * d_xy (2n doubles), d_paths (n), d_h (n) and d_out (n fk_stats) are device
  * buffers owned by the caller; launches go on `cuda_stream` (a cudaStream_t,
  * NULL = default stream) of the current device and are not synchronised.
  * Scratch memory is one 4 MiB static device array per GPU that loads the
  * library, held until the process exits; n > FK_NOALLOC_MAX_POINTS returns
- * FK_ERR_CAPACITY.  The first call on a device looks up the array's device
- * address (make it before any stream capture).  All calls share the array:
- * calls whose kernels overlap on the GPU race and give wrong results.
- * Capped paths are reported in d_out[i].n_capped (no error code). */
+ * FK_ERR_CAPACITY.  The first call in a CUDA context (per device, and again
+ * after cudaDeviceReset) looks up the array's device address, so make it
+ * before any stream capture.  All calls share the array: calls whose kernels
+ * overlap on the GPU race and give wrong results.  FK_CV_MLP is not accepted
+ * (the learned control variate needs a context's network): FK_ERR_ARG.
+ * Errors found by the kernels are not returned (the call does not wait for
+ * them): a point solved completely has d_out[i].n_paths == d_paths[i] and
+ * d_out[i].n_capped == 0; a smaller n_paths means the kernel gave up on some
+ * of the point's paths, and n_capped counts paths stopped at max_steps. */
 #define FK_NOALLOC_MAX_POINTS 16384
 int fk_solve_points_noalloc(const fk_bvp_desc* bvp, unsigned long long seed, unsigned stream_id, int n,
                             const double* d_xy, const unsigned* d_paths, const double* d_h, int precision,

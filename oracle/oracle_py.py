@@ -215,6 +215,63 @@ def ps_disk(b, cx, cy, radius, n_circle, n_radial, theta0, periph_theta, inner_x
     return G, B
 
 
+def square_patch_mesh(dom, n_sub, nodes_per_side, enlarge):
+    """The square-patch layout of configs 2 and 5, restated in numpy for the
+    CPU side (the reference has no such geometry; its circle layout is
+    Malla::Construye_Cuadrado, Mesh/Malla.cpp:12-83, and its CSR rows come
+    from SistemaLineal::Anadir_Lista_Adyacencia, Mesh/SistemaLineal.cpp:8-18).
+
+    n_sub x n_sub subdomains of dom, each enlarged by `enlarge` of its width
+    per side; nodes_per_side equispaced nodes per patch side, kept where they
+    lie strictly inside dom, numbered patch by patch (x-index outer) along a
+    counter-clockwise chain (bottom, right, top, left) that starts after a
+    dropped node when the patch is clipped.  An item is (node, patch holding
+    the node strictly inside), in node order, then patch order.
+
+    Returns dict(nodes (n, 2), patches [dict(rect, chain (m, 2), gids)],
+    items [(gid, patch)], spacing)."""
+    dom = [float(v) for v in dom]
+    Hx, Hy = (dom[2] - dom[0]) / n_sub, (dom[3] - dom[1]) / n_sub
+    sx = (1 + 2 * enlarge) * Hx / (nodes_per_side + 1)
+    sy = (1 + 2 * enlarge) * Hy / (nodes_per_side + 1)
+    tol = 1e-12 * max(dom[2] - dom[0], dom[3] - dom[1])
+    q = np.arange(1, nodes_per_side + 1)
+    nodes, patches = [], []
+    for a in range(n_sub):
+        for b in range(n_sub):
+            r = (dom[0] + (a - enlarge) * Hx, dom[1] + (b - enlarge) * Hy,
+                 dom[0] + (a + 1 + enlarge) * Hx, dom[1] + (b + 1 + enlarge) * Hy)
+            ring = np.concatenate([np.stack([r[0] + q * sx, np.full(len(q), r[1])], 1),
+                                   np.stack([np.full(len(q), r[2]), r[1] + q * sy], 1),
+                                   np.stack([r[2] - q * sx, np.full(len(q), r[3])], 1),
+                                   np.stack([np.full(len(q), r[0]), r[3] - q * sy], 1)])
+            keep = ((ring[:, 0] > dom[0] + tol) & (ring[:, 0] < dom[2] - tol) &
+                    (ring[:, 1] > dom[1] + tol) & (ring[:, 1] < dom[3] - tol))
+            R = len(ring)
+            start = 0
+            if not keep.all():
+                start = next((i + 1) % R for i in range(R) if not keep[i] and keep[(i + 1) % R])
+            order = [(start + t) % R for t in range(R) if keep[(start + t) % R]]
+            chain = ring[order]
+            gids = np.arange(len(nodes), len(nodes) + len(chain))
+            nodes.extend(chain.tolist())
+            patches.append(dict(rect=r, chain=chain, gids=gids, cell=(a, b)))
+    nodes = np.array(nodes)
+    owner = np.concatenate([np.full(len(p["gids"]), s) for s, p in enumerate(patches)])
+    gs, ss = [], []
+    for s, p in enumerate(patches):
+        r = p["rect"]
+        inside = ((nodes[:, 0] > r[0] + tol) & (nodes[:, 0] < r[2] - tol) &
+                  (nodes[:, 1] > r[1] + tol) & (nodes[:, 1] < r[3] - tol) & (owner != s))
+        g = np.nonzero(inside)[0]
+        gs.append(g)
+        ss.append(np.full(len(g), s))
+    gs, ss = np.concatenate(gs), np.concatenate(ss)
+    order = np.lexsort((ss, gs))  # node order, then patch order
+    items = list(zip(gs[order].tolist(), ss[order].tolist()))
+    return dict(nodes=nodes, patches=patches, items=items, spacing=sx)
+
+
 def actualiza_gb(row, cols, G, b, rowptr, col, val, B):
     """SistemaLineal::Actualiza_GB(nudo) on CSR arrays (val and B updated in place);
     cols ascending, as the keys of the node's std::map."""

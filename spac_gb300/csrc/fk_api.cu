@@ -89,6 +89,7 @@ struct StencilSet {
   int nmax = 0;
   DBuf d_arcs, d_theta, d_ipsi, d_patches, d_nodes, d_ainv;
   DBuf d_e32, d_emax;  // patches: A^-1 - I in FP32 and its max |.| per patch
+  std::vector<float> emax;  // host copy of d_emax
   bool uploaded = false;
   int size_of(int s) const { return kind == 1 ? arcs[s].n : patches[s].m; }
   long long acc_of(int s) const {
@@ -123,6 +124,7 @@ struct fk_ctx {
   unsigned long long seed = 0;
   unsigned stream_id = 0;
   int max_steps = 1 << 24;
+  unsigned long long slot_wait_ns = 0, barrier_ns = 0;  // fk_set_wait_limits (0: defaults)
   int block = 256, chunk = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
@@ -252,6 +254,8 @@ int upload_stencils(fk_ctx* ctx, fk::StencilSet& S, const std::vector<char>* hav
       FK_CUDA(S.d_emax.ensure(std::max(n_p, 1) * sizeof(float)));
       FK_CUDA(fk::launch_split_inverse(S.d_patches.as<fk::PatchDev>(), n_p, S.d_ainv.as<double>(), S.d_e32.as<float>(),
                                        S.d_emax.as<float>(), s));
+      S.emax.assign(n_p, 0.f);
+      FK_CUDA(cudaMemcpyAsync(S.emax.data(), S.d_emax.p, n_p * sizeof(float), cudaMemcpyDeviceToHost, s));
       FK_CUDA(cudaStreamSynchronize(s));
     }
   }
@@ -317,9 +321,10 @@ struct RunOut {
 
 int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& it, fk::StencilSet* S,
               const std::vector<long long>* g_off, long long g_total, const int* d_csr_idx, double* d_csr_val,
-              const int* d_row, double* d_B, RunOut& out, bool multi_bvp = false) {
+              const int* d_row, double* d_B, RunOut& out, bool multi_bvp = false, bool need_item_G = true) {
   // multi_bvp: items carry their own BVP index (same functor and control mode
-  // as bvp_id); otherwise every item uses bvp_id
+  // as bvp_id); otherwise every item uses bvp_id.  need_item_G: the per-item G
+  // rows are wanted (otherwise only the CSR values receive them)
   cudaStream_t s = ctx->stream;
   const int n = static_cast<int>(it.size());
   const int kind = S ? S->kind : 0;
@@ -424,6 +429,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   a.key1 = static_cast<uint32_t>(ctx->seed >> 32);
   a.stream = ctx->stream_id;
   a.max_steps = ctx->max_steps;
+  a.wait_limit_ns = ctx->slot_wait_ns;
   a.cv = (bvp.cv == FK_CV_EXACT) ? 1 : 0;
   if (bvp.cv == FK_CV_MLP) {
     const fk::Mlp& M = *ctx->mlps[bvp.mlp];
@@ -437,15 +443,30 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   a.stencil_kind = kind;
   a.acc_words = acc_words;
   a.smem_nodes = smem_nodes;
+  // per-item G buffers
+  FK_CUDA(ctx->w_gout.ensure(std::max<size_t>(g_total * sizeof(double), 16)));
+  if (g_off) FK_CUDA(fk::upload_pinned(ctx->w_goff, ctx->h_goff, *g_off, s));
+  double* item_G = (kind && need_item_G) ? ctx->w_gout.as<double>() : nullptr;
+  // G rows in the path kernel's flush: FP32 patch stencils whose chunks are
+  // whole items and whose window corrections are small enough for FP32
+  bool fuse = precision == FK_FP32 && kind == 2 && whole_items && g_off && d_csr_idx && d_csr_val && !chunks.empty();
+  if (fuse)
+    for (float e : S->emax) fuse = fuse && e < fk::kSplitMaxE;
+  if (fuse) {
+    a.fuse_g = 1;
+    a.patch_e32 = S->d_e32.as<float>();
+    a.g_off = ctx->w_goff.as<long long>();
+    a.csr_idx = d_csr_idx;
+    a.csr_val = d_csr_val;
+    a.item_G = item_G;
+  }
   FK_CUDA(cudaEventRecord(ctx->ev[0], s));
   if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s, warp_mode));
   FK_CUDA(cudaEventRecord(ctx->ev[1], s));
 
   // finalize
-  FK_CUDA(ctx->w_gout.ensure(std::max<size_t>(g_total * sizeof(double), 16)));
   FK_CUDA(ctx->w_bout.ensure(std::max<size_t>(n * sizeof(double), 16)));
   FK_CUDA(ctx->w_sout.ensure(std::max<size_t>(static_cast<size_t>(n) * 16 * sizeof(double), 16)));
-  if (g_off) FK_CUDA(fk::upload_pinned(ctx->w_goff, ctx->h_goff, *g_off, s));
   fk::FinalizeArgs f;
   std::memset(&f, 0, sizeof(f));
   f.bvp = a.bvp;
@@ -470,7 +491,8 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   f.acc = a.acc;
   f.stencil_kind = kind;
   f.g_off = g_off ? ctx->w_goff.as<long long>() : nullptr;
-  f.item_G = kind ? ctx->w_gout.as<double>() : nullptr;
+  f.item_G = item_G;
+  f.g_fused = a.fuse_g;
   f.item_B = ctx->w_bout.as<double>();
   f.item_stats = ctx->w_sout.as<double>();
   f.csr_idx = d_csr_idx;
@@ -488,7 +510,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   ctx->timing[1] = t1;
   ctx->timing[2] = chunks.empty() ? 1 : 2;
   ctx->stream_id++;
-  out.item_G = f.item_G;
+  out.item_G = kind ? ctx->w_gout.as<double>() : nullptr;
   out.item_B = f.item_B;
   out.item_stats = f.item_stats;
   // the kernels' own checks: slot waits, completed paths, capped paths
@@ -561,6 +583,19 @@ int fk_set_max_steps(fk_ctx* ctx, int m) {
   ctx->max_steps = m;
   return FK_OK;
 }
+int fk_set_wait_limits(fk_ctx* ctx, double slot_wait_s, double barrier_s) {
+  if (!ctx) return FK_ERR_ARG;
+  if (!(slot_wait_s >= 0 && slot_wait_s <= 1e6 && barrier_s >= 0 && barrier_s <= 1e6))
+    return fail(ctx, FK_ERR_ARG, "wait limits must be in [0, 1e6] seconds");
+  // (a positive limit below 1 ns becomes 1 ns, not the default)
+  auto ns = [](double sec) -> unsigned long long {
+    return sec > 0 ? std::max(1ull, static_cast<unsigned long long>(sec * 1e9)) : 0ull;
+  };
+  ctx->slot_wait_ns = ns(slot_wait_s);
+  ctx->barrier_ns = ns(barrier_s);
+  return FK_OK;
+}
+
 int fk_set_launch(fk_ctx* ctx, int block, int chunk) {
   if (!ctx) return FK_ERR_ARG;
   if (block != 0 && (block < 32 || block > 256 || block % 32)) return fail(ctx, FK_ERR_ARG, "block must be 32..256, multiple of 32");
@@ -1120,7 +1155,7 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   FK_CUDA(cudaMemsetAsync(ctx->w_B.p, 0, hm.n_rows * sizeof(double), s));
   RunOut ro;
   rc = run_items(ctx, bvp_id, precision, it, &M->st, &M->g_off, M->g_total, M->d_csr_idx.as<int>(),
-                 ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro);
+                 ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro, false, item_G != nullptr);
   if (rc) return rc;
   if (M->disk_radial > 0 && !M->disk.disks.empty()) {
     rc = run_disks(ctx, bvp_id, M->disk, M->dbufs, nullptr, nullptr, ctx->w_val.as<double>(), ctx->w_B.as<double>(),
@@ -1188,6 +1223,7 @@ int fk_mlp_train(fk_ctx* ctx, int mlp_id, int n, const double* xy, const double*
   if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
   if (n < 1 || !xy || !target || !(lr > 0)) return fail(ctx, FK_ERR_ARG, "mlp train: need samples and lr > 0");
   cudaSetDevice(ctx->device);
+  M->barrier_ns = ctx->barrier_ns;
   const int rc = fk::mlp_train(*M, n, xy, target, region, steps, batch, lr, seed, loss_history, ctx->stream, ctx->err);
   if (rc == FK_OK) M->table_grid = 0;
   return rc;

@@ -84,6 +84,7 @@ struct LaunchArgs {
   const ItemDev* items;
   const ChunkDev* chunks;
   int n_chunks;
+  const int* n_chunks_dev; // if set, the chunk count is read from device memory (chunks built on the device)
   const ArcDev* arcs;
   const double* arc_theta;
   const PatchDev* patches;
@@ -93,6 +94,7 @@ struct LaunchArgs {
   double* acc;             // stencil accumulators
   uint32_t key0, key1, stream;
   int max_steps;
+  unsigned long long wait_limit_ns;  // slot waits give up after this (0: 60 s + 1 us x max_steps)
   int cv;                  // 0 none, 1 exact gradient functor, 2 learned (gradient table)
   const float2* cv_tab;    // [regions][grid][grid] grad u_hat
   const double* cv_rect;   // 4 per region
@@ -102,6 +104,16 @@ struct LaunchArgs {
   int acc_words;           // shared accumulator length (elements) per CTA
   int smem_nodes;          // patch nodes / arc angles staged in shared memory (max over stencils)
   const void* mlp;         // device MLP parameters (FK_CV_MLP)
+  // Fused G rows (FP32 stepping, patch stencils, every chunk a whole item):
+  // the last warp out of an item applies A_W^-1 = I + E_W to the item's
+  // moments in shared memory and adds its G row into the CSR values (and
+  // item_G if set); the moments never reach global memory.
+  int fuse_g;
+  const float* patch_e32;  // E_W = A_W^-1 - I, FP32, the layout of the FP64 inverses
+  const long long* g_off;  // item -> first entry of its G row in item_G / csr_idx
+  const int* csr_idx;      // G entry -> CSR position
+  double* csr_val;
+  double* item_G;          // may be null
 };
 
 struct FinalizeArgs {
@@ -130,6 +142,7 @@ struct FinalizeArgs {
   const int* row;           // item -> row (for B scatter)
   double* B;                // may be null
   int* flags;               // may be null: [0] |= an item had capped paths, [1] |= an item lost paths
+  int g_fused;              // 1: the path kernel already added the live items' G rows (LaunchArgs::fuse_g)
   // patch stencils: the largest nwin * k, m and the common k over the
   // launch's patches (fin_words = 0: the generic per-item path)
   int fin_words, fin_m, fin_k;
@@ -159,6 +172,12 @@ cudaError_t launch_build_windows(const PatchDev* patches, const double* nodes, i
 // E = A^-1 - I of every window in FP32, and max |E| per patch
 cudaError_t launch_split_inverse(const PatchDev* patches, int n_patches, const double* ainv, float* e32, float* emax,
                                  cudaStream_t s);
-constexpr float kSplitMaxE = 1e-2f;
+// FP32-stepping assemblies apply E_W = A_W^-1 - I in FP32 (relative error of
+// a G entry ~ 1e-7 max |E| sqrt(k), far below the Monte Carlo error of any
+// row): in the finalize kernel and in the path kernel's fused G rows.  A
+// patch with larger entries (Gaussian windows with eps * spacing well below
+// 1: max |E| is 1.2e-4 at eps * spacing = 3, 0.6 at 1 and 1.8 at 0.8) keeps
+// the finalize kernel's FP64 products.
+constexpr float kSplitMaxE = 64.0f;
 
 }  // namespace fk

@@ -97,7 +97,7 @@ __global__ void finalize_kernel(const FinalizeArgs a) {
     }
     // FP32-stepping assemblies with a well-conditioned stencil (A_W^-1 = I + E,
     // max |E| < kSplitMaxE): G = -(sum_W t_W[t] + sum_W E_W t_W) / N with the
-    // first sum in FP64 and the small correction in FP32 (relative error of G
+    // first sum in FP64 and the correction in FP32 (relative error of G
     // ~1e-7 max|E|); the moments are staged as FP32 in shared memory
     __shared__ float t32[kMaxSplitWords];
     const long long words = static_cast<long long>(P.nwin) * k;
@@ -268,8 +268,8 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
   else
     patch_window_pass<double, K>(a.patch_ainv + P.ainv_off, tw, vis, nwin, k, v64);
   __syncthreads();
-  // the identity part in FP64, the correction E_W t_W summed in FP32 (it is
-  // below 1e-2 of the identity part)
+  // the identity part in FP64, the correction E_W t_W summed in FP32 (at
+  // most a few of k window terms of size max |E| |t|, so ~1e-7 relative)
   const double ninv = s_ninv;
   for (int gi = threadIdx.x; gi < m; gi += blockDim.x) {
     double g = 0.0;
@@ -435,6 +435,23 @@ __global__ void inverse_kernel(const double* A, double* inv, const int* ns, cons
   for (int e = threadIdx.x; e < nn; e += blockDim.x) Vg[e] = v[e];
 }
 
+// Items whose G rows the path kernel already added (fused flush): statistics,
+// B and result flags only, one thread per item; items that ran no paths
+// (Dirichlet nodes, zero path counts) get zero G rows.
+template <int PROB>
+__global__ void finalize_head_kernel(const FinalizeArgs a) {
+  const int item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.n_items) return;
+  const ItemDev it = a.items[item];
+  const bool live = !it.frontera && it.paths > 0;
+  finalize_item_head<PROB>(a, item, it, live, static_cast<double>(it.paths));
+  if (!live && a.item_G && it.stencil >= 0) {
+    const int m = a.patches[it.stencil].m;
+    const long long goff = a.g_off[item];
+    for (int gi = 0; gi < m; ++gi) a.item_G[goff + gi] = 0.0;
+  }
+}
+
 // --------------------------------------------------------------- launchers --
 template <int PROB, int K>
 cudaError_t launch_patch_finalize(const FinalizeArgs& a, size_t smem, cudaStream_t s) {
@@ -452,6 +469,16 @@ cudaError_t launch_patch_finalize_k(const FinalizeArgs& a, size_t smem, cudaStre
 
 cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s) {
   if (a.n_items <= 0) return cudaSuccess;
+  if (a.g_fused) {
+    const dim3 grid((a.n_items + 255) / 256), block(256);
+    switch (problem) {
+      case 1: finalize_head_kernel<1><<<grid, block, 0, s>>>(a); break;
+      case 2: case 4: finalize_head_kernel<2><<<grid, block, 0, s>>>(a); break;
+      case 3: finalize_head_kernel<3><<<grid, block, 0, s>>>(a); break;
+      default: finalize_head_kernel<0><<<grid, block, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+  }
   const size_t psmem = finalize_patch_smem(a);
   if (psmem > 0) {
     switch (problem) {

@@ -36,6 +36,7 @@ struct Mlp {
   size_t cap_samples = 0, cap_partial = 0, cap_loss = 0, cap_hist = 0, cap_sched = 0;
   long long adam_t = 0;
   int trainer = 0;                  // fk_mlp_set_trainer: 0 auto, 1 grid-persistent, 2 per-step graph
+  unsigned long long barrier_ns = 0;  // grid-barrier waits give up after this (0: 5 s)
   Mlp() = default;
   Mlp(const Mlp&) = delete;
   Mlp& operator=(const Mlp&) = delete;

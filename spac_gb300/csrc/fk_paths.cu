@@ -186,12 +186,12 @@ __device__ void stage_stencil(const LaunchArgs& a, SlotSh<R>& sl, unsigned char*
 // slot's accumulators, stages the chunk's stencil and publishes the slot as
 // sequence position `seq`.
 template <typename R, int ST>
-__device__ void fill_slot(const LaunchArgs& a, SlotSh<R>& sl, unsigned char* mem, size_t acc_bytes, int seq,
-                          int nwarps, int lane) {
+__device__ void fill_slot(const LaunchArgs& a, int n_chunks, SlotSh<R>& sl, unsigned char* mem, size_t acc_bytes,
+                          int seq, int nwarps, int lane) {
   int c = 0;
   if (lane == 0) c = atomicAdd(a.queue, 1);
   c = __shfl_sync(kFull, c, 0);
-  if (c < a.n_chunks) {
+  if (c < n_chunks) {
     const ChunkDev ch = a.chunks[c];
     const ItemDev& itg = a.items[ch.item];
     uint4* z = reinterpret_cast<uint4*>(mem);
@@ -256,6 +256,60 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
   return L;
 }
 
+// The last warp out of a whole-item chunk (FP32 stepping, patch stencil): the
+// item's G row from its window moments t_W, held in the slot's shared
+// memory, as finalize_patch_kernel forms it,
+//   G[(W + r) mod m] = -(1/N) sum over windows W covering the node of
+//                      t_W[r] + (E_W t_W)[r],     A_W^-1 = I + E_W,
+// one visited window at a time (lane r < k takes row r: one column of E_W is
+// k consecutive FP32 words), summed in FP64 in `gbuf` (the slot's stencil
+// node area, free once every warp has left the chunk), then added to the
+// item's CSR positions (SistemaLineal::Actualiza_GB,
+// Mesh/SistemaLineal.cpp:68-88) and written to item_G if requested.
+template <typename R>
+__device__ void fused_patch_row(const LaunchArgs& a, const ItemDev& itg, int item, const PatchSh<R>& sp,
+                                const float* sacc, double* gbuf, int lane) {
+  const int m = sp.m, k = sp.k, nwin = sp.closed ? m : m - k + 1;
+  const float* E = a.patch_e32 + a.patches[itg.stencil].ainv_off;
+  for (int i = lane; i < m; i += 32) gbuf[i] = 0.0;
+  __syncwarp();
+  for (int W0 = 0; W0 < nwin; W0 += 32) {
+    const int Wl = W0 + lane;
+    bool vis = false;
+    if (Wl < nwin) {
+      const float* t = sacc + Wl * k;
+      for (int b = 0; b < k; ++b) vis |= t[b] != 0.f;
+    }
+    unsigned vm = __ballot_sync(kFull, vis);
+    while (vm) {
+      const int W = W0 + __ffs(vm) - 1;
+      vm &= vm - 1;
+      if (lane < k) {
+        const float* t = sacc + W * k;
+        const float* Ew = E + static_cast<long long>(W) * k * k + lane;
+        float v = 0.f;
+#pragma unroll 4
+        for (int b = 0; b < k; ++b) v = fmaf(__ldg(Ew + b * k), t[b], v);
+        int gi = W + lane;
+        if (gi >= m) gi -= m;
+        gbuf[gi] += f32_to_f64(t[lane]) + f32_to_f64(v);
+      }
+      __syncwarp();
+    }
+  }
+  double ninv = 0.0;
+  if (lane == 0) ninv = -1.0 / static_cast<double>(itg.paths);
+  ninv = __shfl_sync(kFull, ninv, 0);
+  const long long goff = a.g_off[item];
+  for (int gi = lane; gi < m; gi += 32) {
+    const double g = gbuf[gi] * ninv;
+    if (a.item_G) a.item_G[goff + gi] = g;
+    // a row of several items (a node inside several patches) may meet a column twice
+    atomicAdd(&a.csr_val[a.csr_idx[goff + gi]], g);
+  }
+  __syncwarp();
+}
+
 // FP64 stepping is bound by the FP64 pipe, not by latency: it trades
 // occupancy for registers (2 CTAs of 256 per SM instead of 3).
 //
@@ -288,13 +342,15 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
   const bool cv = a.cv != 0;         // any control term
   const bool cv_exact = a.cv == 1;   // F from the problem functor
   const bool cv_table = a.cv == 2;   // F from the learned gradient table
-  const unsigned long long limit_ns = 60000000000ull + 1000ull * static_cast<unsigned long long>(a.max_steps);
+  const unsigned long long limit_ns =
+      a.wait_limit_ns ? a.wait_limit_ns : 60000000000ull + 1000ull * static_cast<unsigned long long>(a.max_steps);
+  const int n_chunks = a.n_chunks_dev ? *a.n_chunks_dev : a.n_chunks;
 
   if (!WM) {
     if (threadIdx.x < S) slots[threadIdx.x].ready = -1;
     __syncthreads();
     for (int s = warp; s < S; s += nwarps)
-      fill_slot<R, ST>(a, slots[s], smem_raw + s * slot_bytes, acc_bytes, s, nwarps, lane);
+      fill_slot<R, ST>(a, n_chunks, slots[s], smem_raw + s * slot_bytes, acc_bytes, s, nwarps, lane);
   }
 
   ExitQueue<R>& q = sq[warp];
@@ -309,7 +365,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
       int cc = 0;
       if (lane == 0) cc = atomicAdd(a.queue, 1);
       c = __shfl_sync(kFull, cc, 0);
-      if (c >= a.n_chunks) break;
+      if (c >= n_chunks) break;
       stage_stencil<R, ST>(a, slots[si], smem_raw + si * slot_bytes, a.items[a.chunks[c].item].stencil, lane);
       __syncwarp();
     } else {
@@ -731,12 +787,23 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
       if (ST != 0) {
         double* gacc = a.acc + itg.acc_off;
         if (!a.acc_zeroed) {
-          // the chunk is the whole item: its moments are stored, zeros included
-          // (no memset of the accumulators and no atomics)
-          const int words = (ST == 2) ? (sp.closed ? sp.m : sp.m - sp.k + 1) * sp.k : sarc.n;
-          for (int i = lane; i < words; i += 32) {
-            if constexpr (std::is_same<SAcc, float>::value) gacc[i] = f32_to_f64(sacc[i]);
-            else gacc[i] = static_cast<double>(sacc[i]);
+          bool fused = false;
+          if constexpr (ST == 2 && std::is_same<SAcc, float>::value) {
+            if (a.fuse_g) {
+              // the item's G row straight from shared memory
+              fused_patch_row<R>(a, itg, ch.item, sp, reinterpret_cast<const float*>(sacc),
+                                 reinterpret_cast<double*>(mem + acc_bytes), lane);
+              fused = true;
+            }
+          }
+          if (!fused) {
+            // the chunk is the whole item: its moments are stored, zeros included
+            // (no memset of the accumulators and no atomics)
+            const int words = (ST == 2) ? (sp.closed ? sp.m : sp.m - sp.k + 1) * sp.k : sarc.n;
+            for (int i = lane; i < words; i += 32) {
+              if constexpr (std::is_same<SAcc, float>::value) gacc[i] = f32_to_f64(sacc[i]);
+              else gacc[i] = static_cast<double>(sacc[i]);
+            }
           }
         } else {
           for (int i = lane; i < a.acc_words; i += 32) {
@@ -752,7 +819,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         }
       }
       __syncwarp();
-      fill_slot<R, ST>(a, sl, mem, acc_bytes, g + S, nwarps, lane);
+      fill_slot<R, ST>(a, n_chunks, sl, mem, acc_bytes, g + S, nwarps, lane);
     }
   }
 }

@@ -74,6 +74,7 @@ _SIGS = {
     "fk_get_stream": (C.c_int, [C.c_void_p, _up]),
     "fk_set_max_steps": (C.c_int, [C.c_void_p, C.c_int]),
     "fk_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "fk_set_wait_limits": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
     "fk_cuda_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "fk_last_timing": (C.c_int, [C.c_void_p, _dp]),
     "fk_register_bvp": (C.c_int, [C.c_void_p, C.POINTER(BvpDesc), _ip]),
@@ -204,6 +205,10 @@ class Context:
 
     def set_max_steps(self, m):
         self.check(self.L.fk_set_max_steps(self.h, m))
+
+    def set_wait_limits(self, slot_wait_s=0.0, barrier_s=0.0):
+        """fk_set_wait_limits (seconds; 0 = the defaults)."""
+        self.check(self.L.fk_set_wait_limits(self.h, slot_wait_s, barrier_s))
 
     def set_launch(self, block=0, chunk=0):
         self.check(self.L.fk_set_launch(self.h, block, chunk))

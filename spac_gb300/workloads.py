@@ -131,7 +131,7 @@ def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp
     st, t = _sync_time(lambda: ctx.solve_points_multi(bvp_ids, xy, paths, h, fk.FP32))
     steps = float((st["mean_steps"] * paths).sum())
     out["fp32"] = {"seconds": t, "kernel_ms": ctx.last_timing()[0], "paths_per_s": paths.sum() / t,
-                   "path_steps_per_s": steps / t, "mean_steps": steps / paths.sum()}
+                   "node_solves_per_s": len(xy) / t, "path_steps_per_s": steps / t, "mean_steps": steps / paths.sum()}
     err32 = st["phi"] - u
     se32 = np.sqrt(np.maximum(st["phiphi"] - st["phi"] ** 2, 0) / paths)
     # FP64 on a subsample of the same nodes (paths scaled) for the precision comparison
@@ -223,7 +223,7 @@ def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_path
     se = np.sqrt(var / done)
     return {"items": n, "rows": info["n_rows"], "nnz": info["nnz"], "mesh_seconds": t_mesh,
             "assembly_seconds": t_total, "rounds": rounds, "total_paths": total_paths,
-            "paths_per_s": total_paths / t_total, "cv_items": int(use_cv.sum()),
+            "paths_per_s": total_paths / t_total, "node_solves_per_s": n / t_total, "cv_items": int(use_cv.sum()),
             "variance_reduction_median": float(np.median(v_plain / v_cv)),
             "se_max": float(se.max()), "se_median": float(np.median(se)),
             "items_below_target": float(np.mean(se <= se_target * 1.001)),

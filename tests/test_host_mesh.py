@@ -82,3 +82,21 @@ def test_mesh_argument_errors(host_ctx, fk):
         host_ctx.mesh_square_patches((0, 0, 1, 1), 8, 31, 0.6, 3.0, 20)
     with pytest.raises(fk.FKError):
         host_ctx.mesh_square_patches((0, 0, 1, 1), 2, 5, 0.25, 3.0, 20)  # fewer nodes than the stencil
+
+
+@pytest.mark.parametrize("n_sub,nps", [(8, 31), (3, 9), (4, 15)])
+def test_oracle_square_patch_layout_equals_product(host_ctx, orc, n_sub, nps):
+    """The CPU side's numpy restatement of the square-patch layout (used by
+    the timed CPU baseline, which must not load the product library) gives the
+    product's nodes, patch chains and items exactly."""
+    m = orc.square_patch_mesh((0, 0, 1, 1), n_sub, nps, 0.25)
+    mid = host_ctx.mesh_square_patches((0, 0, 1, 1), n_sub, nps, 0.25, 3.0, 6)
+    info = host_ctx.mesh_info(mid)
+    xy, _ = host_ctx.mesh_nodes(mid)
+    assert np.array_equal(xy, m["nodes"])
+    assert m["spacing"] == info["spacing"]
+    row, ixy, st, fr = host_ctx.mesh_items(mid)
+    it = np.array(m["items"])
+    assert np.array_equal(row, it[:, 0]) and np.array_equal(st, it[:, 1])
+    for s, p in enumerate(m["patches"]):
+        assert np.array_equal(host_ctx.mesh_stencil_nodes(mid, s), p["gids"])
