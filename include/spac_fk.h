@@ -238,6 +238,35 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
                 double h, int precision, double* val, double* B, double* item_G, double* item_B,
                 fk_stats* item_stats);
 
+/* ---- adaptive assembly in rounds ------------------------------------------
+ * For path counts chosen per item from the estimates so far (an SE target),
+ * with the path sums kept on the device between rounds: the reference solves
+ * each node once with a fixed N (Solve_OMP_Analytic, FeynmanKacSolver.cpp:344-355,
+ * then SistemaLineal::Actualiza_GB, Mesh/SistemaLineal.cpp:68-88); running it
+ * again with more paths and averaging by hand would keep only averages.
+ *  fk_assembly_begin  zeroes the mesh's running sums (square-patch meshes).
+ *  fk_assembly_round  runs paths_per_item[i] more paths of item i (0 = none)
+ *                     with BVP bvp_of_item[i] (NULL: bvp_id for every item;
+ *                     one problem functor per round, and items with a learned
+ *                     control variate share one network, so learned-CV items
+ *                     and their plain fallback share one launch), and ADDS
+ *                     their sums -- each chunk's unnormalised G row, B and the
+ *                     statistics -- to the running sums on the device.
+ *                     item_var (may be NULL) receives each item's per-path
+ *                     variance of phi_VR over this round's paths.  Every round
+ *                     uses the context's next random stream id and the same h.
+ *  fk_assembly_end    forms every item's path-weighted G row and B from the
+ *                     running sums (the same as one run of all its paths:
+ *                     G = -(sum over all paths of Y w(X_tau)) / N) and writes
+ *                     them as fk_assemble does; item_stats are over all
+ *                     rounds' paths.  It may be called after any round (the
+ *                     sums stay until the next fk_assembly_begin). */
+int fk_assembly_begin(fk_ctx* ctx, int mesh_id);
+int fk_assembly_round(fk_ctx* ctx, int mesh_id, int bvp_id, const int* bvp_of_item, const unsigned* paths_per_item,
+                      double h, int precision, double* item_var);
+int fk_assembly_end(fk_ctx* ctx, int mesh_id, double* val, double* B, double* item_G, double* item_B,
+                    fk_stats* item_stats);
+
 /* ---- pseudospectral disk rows ---------------------------------------------
  * PseudoespectralCirculoSolver::Inicializa(centro, radio, N_circunferencia,
  * N_radio, theta_0, BVP) + Resuelve(BVP, nudos_interior, nudos_periferia)

@@ -115,6 +115,13 @@ struct Mesh {
   std::vector<int> rows;         // per item
   DBuf d_val0, d_csr_idx, d_g_off, d_row;
   bool uploaded = false;
+  // adaptive assembly (fk_assembly_*): running per-item row sums and
+  // statistics on the device, paths and BVP per item on the host
+  DBuf r_gsum, r_stats, r_var;
+  std::vector<unsigned long long> r_paths;
+  std::vector<int> r_bvp;
+  double r_h = 0.0;
+  bool r_active = false;
 };
 
 }  // namespace fk
@@ -311,6 +318,19 @@ void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
   S.patches.push_back(p);
 }
 
+// Options of run_items.
+struct RunOpts {
+  bool multi_bvp = false;    // items carry their own BVP index (one problem functor)
+  bool need_item_G = true;   // the per-item G rows are wanted (else only the CSR values get them)
+  // Adaptive assembly round (fk_assembly_round): the chunks' G rows are added
+  // to g_sum (slot mode, fused rows), the call's statistics to run_stats,
+  // each item's per-path variance goes to item_var (device, may be null), and
+  // no finalize runs.
+  double* g_sum = nullptr;
+  double* run_stats = nullptr;
+  double* item_var = nullptr;
+};
+
 // Runs items through the path kernel and the finalize kernel.
 struct RunOut {
   double* item_G = nullptr;       // device workspace results
@@ -321,10 +341,12 @@ struct RunOut {
 
 int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& it, fk::StencilSet* S,
               const std::vector<long long>* g_off, long long g_total, const int* d_csr_idx, double* d_csr_val,
-              const int* d_row, double* d_B, RunOut& out, bool multi_bvp = false, bool need_item_G = true) {
-  // multi_bvp: items carry their own BVP index (same functor and control mode
-  // as bvp_id); otherwise every item uses bvp_id.  need_item_G: the per-item G
-  // rows are wanted (otherwise only the CSR values receive them)
+              const int* d_row, double* d_B, RunOut& out, const RunOpts& o = RunOpts()) {
+  // o.multi_bvp: items carry their own BVP index (same functor as bvp_id,
+  // whose control mode and network the launch takes); otherwise every item
+  // uses bvp_id
+  const bool multi_bvp = o.multi_bvp, need_item_G = o.need_item_G;
+  const bool round = o.g_sum != nullptr;
   cudaStream_t s = ctx->stream;
   const int n = static_cast<int>(it.size());
   const int kind = S ? S->kind : 0;
@@ -362,7 +384,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   // shared chunk slots.
   long long n_live = 0;
   for (auto& x : it) if (!x.frontera && x.paths > 0) ++n_live;
-  const bool warp_mode = ctx->chunk <= 0 && n_live > 0 && total_paths <= kWarpModeMaxPaths * n_live;
+  const bool warp_mode = !round && ctx->chunk <= 0 && n_live > 0 && total_paths <= kWarpModeMaxPaths * n_live;
   const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes, warp_mode, block);
   if (sacc_bytes > 200 * 1024) return fail(ctx, FK_ERR_CAPACITY, "stencil accumulators exceed shared memory");
   const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes, warp_mode);
@@ -408,8 +430,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   bool whole_items = !warp_mode;
   for (const fk::ChunkDev& c : chunks)
     if (c.p0 != 0 || c.p1 != it[c.item].paths) { whole_items = false; break; }
-  FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
-  if (acc_total > 0 && !whole_items) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
+  if (round) {
+    whole_items = false;  // (the rows go to g_sum: no moment accumulators in global memory)
+  } else {
+    FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
+    if (acc_total > 0 && !whole_items) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
+  }
   FK_CUDA(ctx->w_queue.ensure(16));
   FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));  // queue, error word, result flags
 
@@ -424,7 +450,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   if (kind == 2) { a.patches = S->d_patches.as<fk::PatchDev>(); a.patch_nodes = S->d_nodes.as<double>(); }
   a.queue = ctx->w_queue.as<int>();
   a.stats = ctx->w_stats.as<double>();
-  a.acc = ctx->w_acc.as<double>();
+  a.acc = round ? nullptr : ctx->w_acc.as<double>();
   a.key0 = static_cast<uint32_t>(ctx->seed);
   a.key1 = static_cast<uint32_t>(ctx->seed >> 32);
   a.stream = ctx->stream_id;
@@ -452,17 +478,41 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   bool fuse = precision == FK_FP32 && kind == 2 && whole_items && g_off && d_csr_idx && d_csr_val && !chunks.empty();
   if (fuse)
     for (float e : S->emax) fuse = fuse && e < fk::kSplitMaxE;
-  if (fuse) {
-    a.fuse_g = 1;
-    a.patch_e32 = S->d_e32.as<float>();
+  if (round && !(kind == 2 && g_off)) return fail(ctx, FK_ERR_ARG, "adaptive rounds need a square-patch mesh");
+  if (fuse || round) {
+    a.fuse_g = round ? 2 : 1;
+    // FP32 moments with small window corrections: I + E_W in FP32; otherwise the FP64 inverses
+    bool e32 = precision == FK_FP32;
+    for (float e : S->emax) e32 = e32 && e < fk::kSplitMaxE;
+    a.patch_e32 = e32 ? S->d_e32.as<float>() : nullptr;
+    a.patch_ainv = S->d_ainv.as<double>();
     a.g_off = ctx->w_goff.as<long long>();
     a.csr_idx = d_csr_idx;
     a.csr_val = d_csr_val;
     a.item_G = item_G;
+    a.g_sum = o.g_sum;
   }
   FK_CUDA(cudaEventRecord(ctx->ev[0], s));
   if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s, warp_mode));
   FK_CUDA(cudaEventRecord(ctx->ev[1], s));
+  if (round) {
+    FK_CUDA(fk::launch_round_stats(a.items, n, a.stats, o.run_stats, o.item_var, ctx->w_queue.as<int>() + 2, s));
+    FK_CUDA(cudaEventRecord(ctx->ev[2], s));
+    FK_CUDA(cudaStreamSynchronize(s));
+    float t0 = 0, t1 = 0;
+    cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[2]);
+    ctx->timing[0] = t0;
+    ctx->timing[1] = t1;
+    ctx->timing[2] = chunks.empty() ? 1 : 2;
+    ctx->stream_id++;
+    int q[4] = {0, 0, 0, 0};
+    FK_CUDA(cudaMemcpy(q, ctx->w_queue.p, sizeof(q), cudaMemcpyDeviceToHost));
+    if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
+    if (q[3] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
+    out.capped = q[2] != 0;
+    return FK_OK;
+  }
 
   // finalize
   FK_CUDA(ctx->w_bout.ensure(std::max<size_t>(n * sizeof(double), 16)));
@@ -725,7 +775,9 @@ int fk_solve_points_multi(fk_ctx* ctx, int n, const int* bvp_ids, const double* 
   std::vector<fk::ItemDev> items;
   if ((rc = build_multi(ctx, n, bvp_ids, xy, paths, h, 1.0, items))) return rc;
   RunOut ro;
-  rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro, true);
+  RunOpts opts;
+  opts.multi_bvp = true;
+  rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro, opts);
   if (rc) return rc;
   if ((rc = read_stats(ctx, ro.item_stats, n, out))) return rc;
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
@@ -754,8 +806,10 @@ int fk_autotune_points(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy,
       double t = 1e300;
       for (int rep = 0; rep < 2; ++rep) {
         RunOut ro;
+        RunOpts opts;
+        opts.multi_bvp = true;
         rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro,
-                       true);
+                       opts);
         if (rc && rc != FK_ERR_STEP_CAP) {
           ctx->stream_id = saved_stream;
           return rc;
@@ -1154,8 +1208,10 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   FK_CUDA(cudaMemcpyAsync(ctx->w_val.p, M->d_val0.p, hm.nnz * sizeof(double), cudaMemcpyDeviceToDevice, s));
   FK_CUDA(cudaMemsetAsync(ctx->w_B.p, 0, hm.n_rows * sizeof(double), s));
   RunOut ro;
+  RunOpts asm_opts;
+  asm_opts.need_item_G = item_G != nullptr;
   rc = run_items(ctx, bvp_id, precision, it, &M->st, &M->g_off, M->g_total, M->d_csr_idx.as<int>(),
-                 ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro, false, item_G != nullptr);
+                 ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro, asm_opts);
   if (rc) return rc;
   if (M->disk_radial > 0 && !M->disk.disks.empty()) {
     rc = run_disks(ctx, bvp_id, M->disk, M->dbufs, nullptr, nullptr, ctx->w_val.as<double>(), ctx->w_B.as<double>(),
@@ -1171,6 +1227,176 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   }
   FK_CUDA(cudaStreamSynchronize(s));
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+// ---- adaptive assembly in rounds ---------------------------------------------
+// Items of a mesh as solve records (fk_assemble's layout), paths and BVP per item.
+static void mesh_items_dev(const fk::HostMesh& hm, std::vector<fk::ItemDev>& it, double h,
+                           const unsigned long long* paths, const int* bvp) {
+  const int n = static_cast<int>(hm.items.size());
+  it.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const fk::MeshItem& q = hm.items[i];
+    fk::ItemDev& d = it[i];
+    std::memset(&d, 0, sizeof(d));
+    d.x = q.x; d.y = q.y; d.h = h; d.sqrth = std::sqrt(h);
+    d.paths = static_cast<unsigned>(paths[i]);
+    d.stencil = q.stencil; d.frontera = q.frontera ? 1 : 0;
+    d.bvp = bvp[i];
+    const fk::MeshStencil& S = hm.stencils[q.stencil];
+    if (hm.kind == 1) { d.sub_shape = FK_SHAPE_CIRCLE; d.sub[0] = S.radius; d.sub[1] = S.cx; d.sub[2] = S.cy; }
+    else { d.sub_shape = FK_SHAPE_RECT; for (int k = 0; k < 4; ++k) d.sub[k] = S.rect[k]; }
+  }
+}
+
+int fk_assembly_begin(fk_ctx* ctx, int mesh_id) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (M->host.kind != 2) return fail(ctx, FK_ERR_ARG, "adaptive rounds need a square-patch mesh");
+  int rc = need_device(ctx);
+  if (rc) return rc;
+  if ((rc = upload_mesh(ctx, M))) return rc;
+  const int n = static_cast<int>(M->host.items.size());
+  cudaStream_t s = ctx->stream;
+  FK_CUDA(M->r_gsum.ensure(std::max<size_t>(M->g_total * sizeof(double), 16)));
+  FK_CUDA(M->r_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
+  FK_CUDA(M->r_var.ensure(std::max<size_t>(n * sizeof(double), 16)));
+  FK_CUDA(cudaMemsetAsync(M->r_gsum.p, 0, M->g_total * sizeof(double), s));
+  FK_CUDA(cudaMemsetAsync(M->r_stats.p, 0, static_cast<size_t>(n) * fk::kNumStats * sizeof(double), s));
+  FK_CUDA(cudaStreamSynchronize(s));
+  M->r_paths.assign(n, 0ull);
+  M->r_bvp.assign(n, -1);
+  M->r_h = 0.0;
+  M->r_active = true;
+  return FK_OK;
+}
+
+int fk_assembly_round(fk_ctx* ctx, int mesh_id, int bvp_id, const int* bvp_of_item, const unsigned* paths_per_item,
+                      double h, int precision, double* item_var) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (!M->r_active) return fail(ctx, FK_ERR_ARG, "fk_assembly_round before fk_assembly_begin");
+  if (!paths_per_item) return fail(ctx, FK_ERR_ARG, "null argument");
+  int rc = check_bvp(ctx, bvp_id);
+  if (rc) return rc;
+  if (!(h > 0)) return fail(ctx, FK_ERR_ARG, "h must be > 0");
+  if (M->r_h > 0 && h != M->r_h) return fail(ctx, FK_ERR_ARG, "every round of an assembly takes the same h");
+  if ((rc = need_device(ctx))) return rc;
+  const fk::HostMesh& hm = M->host;
+  const int n = static_cast<int>(hm.items.size());
+  // one problem functor; the items' control variates may differ, and the
+  // items with a learned one share one network (whose BVP the launch takes)
+  std::vector<int> bv(n, bvp_id);
+  int launch_bvp = bvp_id;
+  const fk::BvpDev& b0 = ctx->bvps[bvp_id];
+  int mlp = b0.cv == FK_CV_MLP ? b0.mlp : -1;
+  for (int i = 0; i < n; ++i) {
+    if (bvp_of_item) bv[i] = bvp_of_item[i];
+    if ((rc = check_bvp(ctx, bv[i]))) return rc;
+    const fk::BvpDev& b = ctx->bvps[bv[i]];
+    if (b.problem != b0.problem) return fail(ctx, FK_ERR_ARG, "one round needs BVPs of one problem functor");
+    if (b.cv == FK_CV_MLP) {
+      if (mlp >= 0 && b.mlp != mlp) return fail(ctx, FK_ERR_ARG, "one round takes one learned network");
+      mlp = b.mlp;
+      if (paths_per_item[i] > 0) launch_bvp = bv[i];
+    }
+  }
+  if (ctx->bvps.size() * sizeof(fk::BvpDev) > ctx->d_bvps.bytes) FK_CUDA(fk::upload(ctx->d_bvps, ctx->bvps, ctx->stream));
+  std::vector<unsigned long long> p(paths_per_item, paths_per_item + n);
+  std::vector<fk::ItemDev>& it = ctx->tmp_items;
+  mesh_items_dev(hm, it, h, p.data(), bv.data());
+  RunOut ro;
+  RunOpts o;
+  o.multi_bvp = true;
+  o.g_sum = M->r_gsum.as<double>();
+  o.run_stats = M->r_stats.as<double>();
+  o.item_var = item_var ? M->r_var.as<double>() : nullptr;
+  rc = run_items(ctx, launch_bvp, precision, it, &M->st, &M->g_off, M->g_total, M->d_csr_idx.as<int>(), nullptr,
+                 nullptr, nullptr, ro, o);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) {
+    M->r_paths[i] += paths_per_item[i];
+    if (paths_per_item[i] > 0 || M->r_bvp[i] < 0) M->r_bvp[i] = bv[i];
+  }
+  M->r_h = h;
+  if (item_var) {
+    FK_CUDA(copy_out(item_var, M->r_var.p, n * sizeof(double), ctx->stream));
+    FK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
+  return FK_OK;
+}
+
+int fk_assembly_end(fk_ctx* ctx, int mesh_id, double* val, double* B, double* item_G, double* item_B,
+                    fk_stats* item_stats) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (!M->r_active) return fail(ctx, FK_ERR_ARG, "fk_assembly_end before fk_assembly_begin");
+  int rc = need_device(ctx);
+  if (rc) return rc;
+  const fk::HostMesh& hm = M->host;
+  const int n = static_cast<int>(hm.items.size());
+  cudaStream_t s = ctx->stream;
+  std::vector<int> bv(M->r_bvp);
+  int problem = 0;
+  for (int i = 0; i < n; ++i) {
+    if (bv[i] < 0) bv[i] = 0;  // (an item no round gave paths: B = g(x) or 0, no G)
+    problem = ctx->bvps.empty() ? 0 : ctx->bvps[bv[i]].problem;
+  }
+  if (ctx->bvps.empty()) return fail(ctx, FK_ERR_REGISTRY, "no BVP registered");
+  std::vector<fk::ItemDev>& it = ctx->tmp_items;
+  mesh_items_dev(hm, it, M->r_h > 0 ? M->r_h : 1.0, M->r_paths.data(), bv.data());
+  for (int i = 0; i < n; ++i)
+    if (M->r_paths[i] > 0xffffffffull) return fail(ctx, FK_ERR_CAPACITY, "an item ran more than 2^32 - 1 paths");
+  FK_CUDA(fk::upload_pinned(ctx->w_items, ctx->h_items, it, s));
+  FK_CUDA(fk::upload_pinned(ctx->w_goff, ctx->h_goff, M->g_off, s));
+  FK_CUDA(ctx->w_val.ensure(std::max<size_t>(hm.nnz * sizeof(double), 16)));
+  FK_CUDA(ctx->w_B.ensure(std::max<size_t>(hm.n_rows * sizeof(double), 16)));
+  FK_CUDA(ctx->w_gout.ensure(std::max<size_t>(M->g_total * sizeof(double), 16)));
+  FK_CUDA(ctx->w_bout.ensure(std::max<size_t>(n * sizeof(double), 16)));
+  FK_CUDA(ctx->w_sout.ensure(std::max<size_t>(static_cast<size_t>(n) * 16 * sizeof(double), 16)));
+  FK_CUDA(ctx->w_queue.ensure(16));
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));
+  FK_CUDA(cudaMemcpyAsync(ctx->w_val.p, M->d_val0.p, hm.nnz * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  FK_CUDA(cudaMemsetAsync(ctx->w_B.p, 0, hm.n_rows * sizeof(double), s));
+  fk::FinalizeArgs f;
+  std::memset(&f, 0, sizeof(f));
+  f.bvp = ctx->d_bvps.as<fk::BvpDev>();
+  f.items = ctx->w_items.as<fk::ItemDev>();
+  f.n_items = n;
+  f.patches = M->st.d_patches.as<fk::PatchDev>();
+  f.stats = M->r_stats.as<double>();
+  f.stencil_kind = 2;
+  f.g_off = ctx->w_goff.as<long long>();
+  f.item_G = item_G ? ctx->w_gout.as<double>() : nullptr;
+  f.item_B = ctx->w_bout.as<double>();
+  f.item_stats = ctx->w_sout.as<double>();
+  f.row = M->d_row.as<int>();
+  f.B = ctx->w_B.as<double>();
+  f.flags = ctx->w_queue.as<int>() + 2;
+  f.g_fused = 1;  // statistics and B only; the rows come from the running sums
+  FK_CUDA(cudaEventRecord(ctx->ev[0], s));
+  FK_CUDA(fk::launch_finalize(f, problem, s));
+  FK_CUDA(fk::launch_rows_from_sums(f.items, n, f.patches, f.g_off, M->r_gsum.as<double>(), M->d_csr_idx.as<int>(),
+                                    ctx->w_val.as<double>(), f.item_G, s));
+  FK_CUDA(cudaEventRecord(ctx->ev[1], s));
+  FK_CUDA(copy_out(val, ctx->w_val.p, hm.nnz * sizeof(double), s));
+  FK_CUDA(copy_out(B, ctx->w_B.p, hm.n_rows * sizeof(double), s));
+  FK_CUDA(copy_out(item_G, ctx->w_gout.p, M->g_total * sizeof(double), s));
+  FK_CUDA(copy_out(item_B, ctx->w_bout.p, n * sizeof(double), s));
+  if (item_stats) {
+    if ((rc = read_stats(ctx, ctx->w_sout.as<double>(), n, item_stats))) return rc;
+  }
+  FK_CUDA(cudaStreamSynchronize(s));
+  float t1 = 0;
+  cudaEventElapsedTime(&t1, ctx->ev[0], ctx->ev[1]);
+  ctx->timing[0] = 0;
+  ctx->timing[1] = t1;
+  ctx->timing[2] = 2;
+  int q[4] = {0, 0, 0, 0};
+  FK_CUDA(cudaMemcpy(q, ctx->w_queue.p, sizeof(q), cudaMemcpyDeviceToHost));
+  if (q[2] != 0) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
   return FK_OK;
 }
 

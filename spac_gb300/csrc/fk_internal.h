@@ -104,12 +104,15 @@ struct LaunchArgs {
   int acc_words;           // shared accumulator length (elements) per CTA
   int smem_nodes;          // patch nodes / arc angles staged in shared memory (max over stencils)
   const void* mlp;         // device MLP parameters (FK_CV_MLP)
-  // Fused G rows (FP32 stepping, patch stencils, every chunk a whole item):
-  // the last warp out of an item applies A_W^-1 = I + E_W to the item's
-  // moments in shared memory and adds its G row into the CSR values (and
-  // item_G if set); the moments never reach global memory.
+  // Fused G rows (patch stencils, slot mode): the last warp out of a chunk
+  // applies A_W^-1 to the chunk's moments in shared memory, so that the
+  // moments never reach global memory.  1: every chunk is a whole item, whose
+  // G row goes into the CSR values (and item_G if set); 2: adaptive rounds,
+  // the chunk's unnormalised row is added to g_sum.
   int fuse_g;
-  const float* patch_e32;  // E_W = A_W^-1 - I, FP32, the layout of the FP64 inverses
+  const float* patch_e32;  // FP32 moments: E_W = A_W^-1 - I, the layout of the FP64 inverses
+  const double* patch_ainv;  // FP64 moments: A_W^-1
+  double* g_sum;           // fuse_g == 2: running row sums, g_off indexed
   const long long* g_off;  // item -> first entry of its G row in item_G / csr_idx
   const int* csr_idx;      // G entry -> CSR position
   double* csr_val;
@@ -169,6 +172,14 @@ cudaError_t launch_build_psi(const ArcDev* arcs, const double* theta, int n_arcs
 cudaError_t launch_build_windows(const PatchDev* patches, const double* nodes, int n_patches,
                                  const long long* win_base, long long total_windows, int k, double* out,
                                  cudaStream_t s);
+// adaptive assembly rounds (fk_assembly_*): a round's statistics into the
+// running sums (and its per-path variance per item); the rows from the
+// running row sums at the end
+cudaError_t launch_round_stats(const ItemDev* items, int n, const double* stats, double* run_stats, double* item_var,
+                               int* flags, cudaStream_t s);
+cudaError_t launch_rows_from_sums(const ItemDev* items, int n, const PatchDev* patches, const long long* g_off,
+                                  const double* g_sum, const int* csr_idx, double* csr_val, double* item_G,
+                                  cudaStream_t s);
 // E = A^-1 - I of every window in FP32, and max |E| per patch
 cudaError_t launch_split_inverse(const PatchDev* patches, int n_patches, const double* ainv, float* e32, float* emax,
                                  cudaStream_t s);

@@ -452,6 +452,66 @@ __global__ void finalize_head_kernel(const FinalizeArgs a) {
   }
 }
 
+// ------------------------------------------------ adaptive assembly rounds --
+// After a round: its per-item statistics are added to the running sums, its
+// per-path variance of phi_VR is reported per item, and the result flags are
+// raised as the finalize kernels raise them.
+__global__ void round_stats_kernel(const ItemDev* items, int n, const double* stats, double* run_stats,
+                                   double* item_var, int* flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const ItemDev it = items[i];
+  const double* S = stats + static_cast<long long>(i) * kNumStats;
+  double* R = run_stats + static_cast<long long>(i) * kNumStats;
+  for (int j = 0; j < kNumStats; ++j) R[j] += S[j];
+  const bool live = !it.frontera && it.paths > 0;
+  double var = 0.0;
+  if (live) {
+    const double N = static_cast<double>(it.paths), m = S[kStatVR] / N;
+    var = fmax(S[kStatVR2] / N - m * m, 0.0);
+    if (flags) {
+      if (S[kStatCap] > 0.0) atomicOr(&flags[0], 1);
+      if (S[kStatPaths] != N) atomicOr(&flags[1], 1);
+    }
+  }
+  if (item_var) item_var[i] = var;
+}
+
+// End of an adaptive assembly: item i's G row is its running row sum over
+// its total path count N_i (items[i].paths), added to its CSR positions and
+// written to item_G if requested; one warp per item.
+__global__ void rows_from_sums_kernel(const ItemDev* items, int n, const PatchDev* patches, const long long* g_off,
+                                      const double* g_sum, const int* csr_idx, double* csr_val, double* item_G) {
+  const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const ItemDev it = items[i];
+  if (it.stencil < 0) return;
+  const int m = patches[it.stencil].m;
+  const long long goff = g_off[i];
+  const bool live = !it.frontera && it.paths > 0;
+  const double ninv = live ? 1.0 / static_cast<double>(it.paths) : 0.0;
+  for (int gi = lane; gi < m; gi += 32) {
+    const double g = live ? g_sum[goff + gi] * ninv : 0.0;
+    if (item_G) item_G[goff + gi] = g;
+    if (csr_val && live) atomicAdd(&csr_val[csr_idx[goff + gi]], g);
+  }
+}
+
+cudaError_t launch_round_stats(const ItemDev* items, int n, const double* stats, double* run_stats, double* item_var,
+                               int* flags, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  round_stats_kernel<<<(n + 255) / 256, 256, 0, s>>>(items, n, stats, run_stats, item_var, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rows_from_sums(const ItemDev* items, int n, const PatchDev* patches, const long long* g_off,
+                                  const double* g_sum, const int* csr_idx, double* csr_val, double* item_G,
+                                  cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  rows_from_sums_kernel<<<(n + 7) / 8, 256, 0, s>>>(items, n, patches, g_off, g_sum, csr_idx, csr_val, item_G);
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------------- launchers --
 template <int PROB, int K>
 cudaError_t launch_patch_finalize(const FinalizeArgs& a, size_t smem, cudaStream_t s) {

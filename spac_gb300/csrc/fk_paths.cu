@@ -256,56 +256,82 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
   return L;
 }
 
-// The last warp out of a whole-item chunk (FP32 stepping, patch stencil): the
-// item's G row from its window moments t_W, held in the slot's shared
-// memory, as finalize_patch_kernel forms it,
-//   G[(W + r) mod m] = -(1/N) sum over windows W covering the node of
-//                      t_W[r] + (E_W t_W)[r],     A_W^-1 = I + E_W,
-// one visited window at a time (lane r < k takes row r: one column of E_W is
-// k consecutive FP32 words), summed in FP64 in `gbuf` (the slot's stencil
-// node area, free once every warp has left the chunk), then added to the
-// item's CSR positions (SistemaLineal::Actualiza_GB,
-// Mesh/SistemaLineal.cpp:68-88) and written to item_G if requested.
-template <typename R>
+// The last warp out of a chunk (slot mode, patch stencil) turns the chunk's
+// window moments t_W, held in the slot's shared memory, into the chunk's
+// part of the item's G row, as finalize_patch_kernel does for a whole item:
+//   row[(W + r) mod m] = sum over the windows W covering the node of
+//                        (A_W^-1 t_W)[r],
+// with A_W^-1 t_W = t_W + E_W t_W in FP32 for FP32 moments (E_W = A_W^-1 - I,
+// when patch_e32 is set) and the FP64 inverse otherwise, one visited window
+// at a time (lane
+// r < k takes row r: one column of the matrix is k consecutive words),
+// summed in FP64 in `gbuf` (the slot's stencil node area, free once every
+// warp has left the chunk).  Then either
+//   fuse_g == 1 (the chunk is the whole item): G = -row / N is added to the
+//     item's CSR positions (SistemaLineal::Actualiza_GB,
+//     Mesh/SistemaLineal.cpp:68-88) and written to item_G if requested;
+//   fuse_g == 2 (rounds of an adaptive assembly): -row is added to the
+//     item's running row sum g_sum, normalised once by the total path count
+//     at the end of the assembly.
+__device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }  // (integer pipes)
+__device__ __forceinline__ double widen(double v) { return v; }
+
+template <typename R, typename SAcc>
 __device__ void fused_patch_row(const LaunchArgs& a, const ItemDev& itg, int item, const PatchSh<R>& sp,
-                                const float* sacc, double* gbuf, int lane) {
+                                const SAcc* sacc, double* gbuf, int lane) {
+  constexpr bool k32 = std::is_same<SAcc, float>::value;
   const int m = sp.m, k = sp.k, nwin = sp.closed ? m : m - k + 1;
-  const float* E = a.patch_e32 + a.patches[itg.stencil].ainv_off;
+  const long long moff = a.patches[itg.stencil].ainv_off;
   for (int i = lane; i < m; i += 32) gbuf[i] = 0.0;
   __syncwarp();
   for (int W0 = 0; W0 < nwin; W0 += 32) {
     const int Wl = W0 + lane;
     bool vis = false;
     if (Wl < nwin) {
-      const float* t = sacc + Wl * k;
-      for (int b = 0; b < k; ++b) vis |= t[b] != 0.f;
+      const SAcc* t = sacc + Wl * k;
+      for (int b = 0; b < k; ++b) vis |= t[b] != SAcc(0);
     }
     unsigned vm = __ballot_sync(kFull, vis);
     while (vm) {
       const int W = W0 + __ffs(vm) - 1;
       vm &= vm - 1;
       if (lane < k) {
-        const float* t = sacc + W * k;
-        const float* Ew = E + static_cast<long long>(W) * k * k + lane;
-        float v = 0.f;
-#pragma unroll 4
-        for (int b = 0; b < k; ++b) v = fmaf(__ldg(Ew + b * k), t[b], v);
+        const SAcc* t = sacc + W * k;
         int gi = W + lane;
         if (gi >= m) gi -= m;
-        gbuf[gi] += f32_to_f64(t[lane]) + f32_to_f64(v);
+        if (k32 && a.patch_e32) {
+          const float* Ew = a.patch_e32 + moff + static_cast<long long>(W) * k * k + lane;
+          float v = 0.f;
+#pragma unroll 4
+          for (int b = 0; b < k; ++b) v = fmaf(__ldg(Ew + b * k), static_cast<float>(t[b]), v);
+          gbuf[gi] += widen(t[lane]) + f32_to_f64(v);
+        } else {
+          const double* Aw = a.patch_ainv + moff + static_cast<long long>(W) * k * k + lane;
+          double v = 0.0;
+#pragma unroll 4
+          for (int b = 0; b < k; ++b) v = fma(__ldg(Aw + b * k), static_cast<double>(t[b]), v);
+          gbuf[gi] += v;
+        }
       }
       __syncwarp();
     }
   }
-  double ninv = 0.0;
-  if (lane == 0) ninv = -1.0 / static_cast<double>(itg.paths);
-  ninv = __shfl_sync(kFull, ninv, 0);
   const long long goff = a.g_off[item];
-  for (int gi = lane; gi < m; gi += 32) {
-    const double g = gbuf[gi] * ninv;
-    if (a.item_G) a.item_G[goff + gi] = g;
-    // a row of several items (a node inside several patches) may meet a column twice
-    atomicAdd(&a.csr_val[a.csr_idx[goff + gi]], g);
+  if (a.fuse_g == 2) {
+    for (int gi = lane; gi < m; gi += 32) {
+      const double g = gbuf[gi];
+      if (g != 0.0) atomicAdd(&a.g_sum[goff + gi], -g);
+    }
+  } else {
+    double ninv = 0.0;
+    if (lane == 0) ninv = -1.0 / static_cast<double>(itg.paths);
+    ninv = __shfl_sync(kFull, ninv, 0);
+    for (int gi = lane; gi < m; gi += 32) {
+      const double g = gbuf[gi] * ninv;
+      if (a.item_G) a.item_G[goff + gi] = g;
+      // a row of several items (a node inside several patches) may meet a column twice
+      atomicAdd(&a.csr_val[a.csr_idx[goff + gi]], g);
+    }
   }
   __syncwarp();
 }
@@ -339,9 +365,6 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
                                : paths_slot_bytes(kPrec, ST, a.acc_words, a.smem_nodes);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const bool cv = a.cv != 0;         // any control term
-  const bool cv_exact = a.cv == 1;   // F from the problem functor
-  const bool cv_table = a.cv == 2;   // F from the learned gradient table
   const unsigned long long limit_ns =
       a.wait_limit_ns ? a.wait_limit_ns : 60000000000ull + 1000ull * static_cast<unsigned long long>(a.max_steps);
   const int n_chunks = a.n_chunks_dev ? *a.n_chunks_dev : a.n_chunks;
@@ -396,8 +419,13 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     const ArcDev& sarc = sl.sarc;
     const unsigned n_ch = ch.p1 - ch.p0;
 
-    // the item's BVP (independent problems of one functor share a launch)
+    // the item's BVP (independent problems of one functor share a launch; the
+    // control variate is the item's own, so learned-CV items and their plain
+    // fallback can share one launch)
     const BvpDev& bvp = a.bvp[itg.bvp];
+    const bool cv_exact = bvp.cv == 1;                // F from the problem functor
+    const bool cv_table = a.cv == 2 && bvp.cv == 2;   // F from the learned gradient table
+    const bool cv = cv_exact || cv_table;             // any control term
     const R d0 = R(bvp.dom[0]), d1 = R(bvp.dom[1]), d2 = R(bvp.dom[2]), d3 = R(bvp.dom[3]);
     const R h = R(itg.h), sqrth = R(itg.sqrth), x0 = R(itg.x), y0 = R(itg.y);
     const R s0 = R(itg.sub[0]), s1 = R(itg.sub[1]), s2 = R(itg.sub[2]), s3 = R(itg.sub[3]);
@@ -784,26 +812,23 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     if (left == 1) {
       // last warp out: flush the chunk's stencil moments, refill the slot
       __threadfence_block();
-      if (ST != 0) {
+      bool fused = false;
+      if constexpr (ST == 2) {
+        if (a.fuse_g) {
+          // the chunk's G row straight from shared memory
+          fused_patch_row<R, SAcc>(a, itg, ch.item, sp, sacc, reinterpret_cast<double*>(mem + acc_bytes), lane);
+          fused = true;
+        }
+      }
+      if (ST != 0 && !fused) {
         double* gacc = a.acc + itg.acc_off;
         if (!a.acc_zeroed) {
-          bool fused = false;
-          if constexpr (ST == 2 && std::is_same<SAcc, float>::value) {
-            if (a.fuse_g) {
-              // the item's G row straight from shared memory
-              fused_patch_row<R>(a, itg, ch.item, sp, reinterpret_cast<const float*>(sacc),
-                                 reinterpret_cast<double*>(mem + acc_bytes), lane);
-              fused = true;
-            }
-          }
-          if (!fused) {
-            // the chunk is the whole item: its moments are stored, zeros included
-            // (no memset of the accumulators and no atomics)
-            const int words = (ST == 2) ? (sp.closed ? sp.m : sp.m - sp.k + 1) * sp.k : sarc.n;
-            for (int i = lane; i < words; i += 32) {
-              if constexpr (std::is_same<SAcc, float>::value) gacc[i] = f32_to_f64(sacc[i]);
-              else gacc[i] = static_cast<double>(sacc[i]);
-            }
+          // the chunk is the whole item: its moments are stored, zeros included
+          // (no memset of the accumulators and no atomics)
+          const int words = (ST == 2) ? (sp.closed ? sp.m : sp.m - sp.k + 1) * sp.k : sarc.n;
+          for (int i = lane; i < words; i += 32) {
+            if constexpr (std::is_same<SAcc, float>::value) gacc[i] = f32_to_f64(sacc[i]);
+            else gacc[i] = static_cast<double>(sacc[i]);
           }
         } else {
           for (int i = lane; i < a.acc_words; i += 32) {

@@ -97,6 +97,9 @@ _SIGS = {
     "fk_mesh_csr": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp]),
     "fk_assemble": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint, _up, C.c_double, C.c_int, _dp, _dp, _dp,
                               _dp, C.POINTER(Stats)]),
+    "fk_assembly_begin": (C.c_int, [C.c_void_p, C.c_int]),
+    "fk_assembly_round": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip, _up, C.c_double, C.c_int, _dp]),
+    "fk_assembly_end": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
     "fk_solve_disks_ps": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(DiskDesc), _dp, _dp]),
     "fk_mesh_set_disk_solver": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_create": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_ulonglong, _ip]),
@@ -419,6 +422,41 @@ class Context:
                                 G.ctypes.data_as(_dp) if G is not None else None,
                                 iB.ctypes.data_as(_dp) if items else None, st if items else None)
         self.check(rc, allow)
+        return dict(val=val, B=B, item_G=G, item_B=iB, item_stats=stats_array(st) if items else None)
+
+
+    # -- adaptive assembly in rounds (device-resident sums)
+    def assembly_begin(self, mesh):
+        self.check(self.L.fk_assembly_begin(self.h, mesh))
+
+    def assembly_round(self, mesh, bvp, paths_per_item, h, precision=FP64, bvp_of_item=None, want_var=True,
+                       allow=()):
+        """fk_assembly_round; returns each item's per-path variance of this round (or None)."""
+        pp, ppp = _u(paths_per_item)
+        pb = None
+        if bvp_of_item is not None:
+            bo, pb = _i(bvp_of_item)
+        var = np.zeros(len(pp)) if want_var else None
+        self.check(self.L.fk_assembly_round(self.h, mesh, bvp, pb, ppp, h, precision,
+                                            var.ctypes.data_as(_dp) if want_var else None), allow)
+        return var
+
+    def assembly_end(self, mesh, csr=True, items=True, item_G=True, allow=()):
+        info = self.mesh_info(mesh)
+        val = np.zeros(info["nnz"]) if csr else None
+        B = np.zeros(info["n_rows"]) if csr else None
+        G = iB = st = None
+        if items:
+            if item_G:
+                sizes = [len(self.mesh_stencil_nodes(mesh, s)) for s in range(info["n_stencils"])]
+                _, _, stn, _ = self.mesh_items(mesh)
+                G = np.zeros(int(sum(sizes[s] for s in stn)))
+            iB = np.zeros(info["n_items"])
+            st = (Stats * info["n_items"])()
+        self.check(self.L.fk_assembly_end(self.h, mesh, val.ctypes.data_as(_dp) if csr else None,
+                                          B.ctypes.data_as(_dp) if csr else None,
+                                          G.ctypes.data_as(_dp) if G is not None else None,
+                                          iB.ctypes.data_as(_dp) if items else None, st if items else None), allow)
         return dict(val=val, B=B, item_G=G, item_B=iB, item_stats=stats_array(st) if items else None)
 
 

@@ -159,76 +159,124 @@ def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp
     return out
 
 
+def collocation_pilot(ctx, bvp, grid=64, paths=500, h=1e-3, precision=fk.FP32):
+    """Whole-domain plain point solves on a grid x grid lattice of the unit
+    square: estimates of u that use the boundary data only (the training
+    targets of the learned control variate)."""
+    g = (np.arange(grid) + 0.5) / grid
+    xy = np.ascontiguousarray(np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2))
+    st = ctx.solve_points(bvp, xy, paths, h, precision)
+    return xy, np.ascontiguousarray(st["phi"])
+
+
+def learned_cv(ctx, problem, pxy, target, steps=50, lr=1e-2, table=256, seed=99):
+    """A one-region network on [0,1]^2 trained on (pxy, target): Adam steps,
+    the output-layer refit and the gradient table; returns the BVP id that
+    uses it."""
+    rects = np.array([[0.0, 0.0, 1.0, 1.0]])
+    mid = fk.C.c_int()
+    ctx.check(ctx.L.fk_mlp_create(ctx.h, 1, rects.ctypes.data_as(fk._dp), seed, fk.C.byref(mid)))
+    mid = mid.value
+    if steps > 0:
+        ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(target), pxy.ctypes.data_as(fk._dp),
+                                     target.ctypes.data_as(fk._dp), None, steps, 4096, lr, 5, None))
+    ctx.check(ctx.L.fk_mlp_fit_output(ctx.h, mid, len(target), pxy.ctypes.data_as(fk._dp),
+                                      target.ctypes.data_as(fk._dp), None, 1e-6))
+    ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
+    return ctx.register_bvp(problem, cv=fk.CV_MLP, mlp_id=mid)
+
+
 def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_paths=256, max_rounds=6,
-          max_paths=4_000_000, train_steps=2000, table=256, lr=1e-2, fit_output=False):
-    """Adaptive assembly: per item, paths until SE < se_target, learned control
-    variate where it lowers the variance, plain FK otherwise."""
-    mesh, t_mesh = _sync_time(lambda: ctx.mesh_square_patches((0, 0, 1, 1), n_sub, nodes_per_side, 0.25, 3.0, 20))
+          max_paths=4_000_000, eps_spacing=3.0):
+    """Adaptive assembly of the full CSR G/B: per item, paths until the
+    standard error of its estimate is below se_target, learned control
+    variate where it lowers the variance and plain FK as the fallback, with
+    the per-item path sums (G rows, B, statistics) kept on the device across
+    rounds (fk_assembly_begin/round/end).
+
+    The network learns u from whole-domain point solves at 64 x 64
+    collocation points (boundary data only).  The first two rounds run
+    pilot_paths per item with each method; each later round runs the paths
+    that the chosen method's variance asks for."""
+    mesh, t_mesh = _sync_time(lambda: ctx.mesh_square_patches((0, 0, 1, 1), n_sub, nodes_per_side, 0.25,
+                                                               eps_spacing, 20))
     info = ctx.mesh_info(mesh)
     n = info["n_items"]
     row, ixy, stn, fr = ctx.mesh_items(mesh)
-    u = franke(ixy[:, 0], ixy[:, 1])
     b_plain = ctx.register_bvp(fk.FRANKE)
     t0 = time.perf_counter()
-    # pilot: plain assembly with few paths; its node estimates train the network
+    pxy, tgt = collocation_pilot(ctx, b_plain)
+    t_pilot = time.perf_counter() - t0
+    b_cv = learned_cv(ctx, fk.FRANKE, pxy, tgt)
+    t_net = time.perf_counter() - t0 - t_pilot
+    ctx.assembly_begin(mesh)
     p0 = np.full(n, pilot_paths, dtype=np.uint32)
-    r0 = ctx.assemble(mesh, b_plain, 0, h, fk.FP32, paths_per_item=p0, item_G=False, csr=False)
-    nodes_xy, _ = ctx.mesh_nodes(mesh)
-    # node estimates: mean over the items of each row (the row's FK value estimates)
-    est = np.bincount(row, weights=r0["item_stats"]["phi_VR"], minlength=info["n_rows"]) / \
-        np.maximum(np.bincount(row, minlength=info["n_rows"]), 1)
-    rects = np.array([[0.0, 0.0, 1.0, 1.0]])
-    mid = fk.C.c_int()
-    ctx.check(ctx.L.fk_mlp_create(ctx.h, 1, rects.ctypes.data_as(fk._dp), 99, fk.C.byref(mid)))
-    mid = mid.value
-    nx = np.ascontiguousarray(nodes_xy)
-    tg = np.ascontiguousarray(est)
-    ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tg), nx.ctypes.data_as(fk._dp), tg.ctypes.data_as(fk._dp), None,
-                                 train_steps, 4096, lr, 5, None))
-    if fit_output:
-        ctx.check(ctx.L.fk_mlp_fit_output(ctx.h, mid, len(tg), nx.ctypes.data_as(fk._dp), tg.ctypes.data_as(fk._dp),
-                                          None, 1e-6))
-    ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
-    b_cv = ctx.register_bvp(fk.FRANKE, cv=fk.CV_MLP, mlp_id=mid)
-    rc = ctx.assemble(mesh, b_cv, 0, h, fk.FP32, paths_per_item=p0, item_G=False, csr=False)
-    v_plain = np.maximum(r0["item_stats"]["phiphi_VR"] - r0["item_stats"]["phi_VR"] ** 2, 1e-30)
-    v_cv = np.maximum(rc["item_stats"]["phiphi_VR"] - rc["item_stats"]["phi_VR"] ** 2, 1e-30)
-    use_cv = v_cv < v_plain  # plain FK is the fallback where the control variate does not help
-    var = np.where(use_cv, v_cv, v_plain)
-    # running sums per item (B, G rows and the estimate), weighted by paths
-    done = np.full(n, pilot_paths, dtype=np.int64)
-    sum_phi = np.where(use_cv, rc["item_stats"]["phi_VR"], r0["item_stats"]["phi_VR"]) * pilot_paths
-    sum_B = np.where(use_cv, rc["item_B"], r0["item_B"]) * pilot_paths
-    rounds, total_paths = 0, int(2 * pilot_paths * n)
-    while rounds < max_rounds:
-        need = np.ceil(var / se_target ** 2).astype(np.int64) - done
-        need = np.clip(need, 0, max_paths)
-        if need.max() <= 0:
+    v_cv = np.maximum(ctx.assembly_round(mesh, b_cv, p0, h, fk.FP32), 1e-30)
+    v_pl = np.maximum(ctx.assembly_round(mesh, b_plain, p0, h, fk.FP32), 1e-30)
+    use_cv = v_cv < v_pl  # plain FK is the fallback where the control variate does not help
+    n_cv = np.full(n, pilot_paths, dtype=np.int64)
+    n_pl = np.full(n, pilot_paths, dtype=np.int64)
+    sv_cv, sv_pl = v_cv * pilot_paths, v_pl * pilot_paths  # path-weighted variance sums per method
+    total_paths, rounds, kern_ms = int(2 * pilot_paths * n), 2, []
+    bvp_of = np.where(use_cv, b_cv, b_plain).astype(np.int32)
+
+    def se2():
+        N = n_cv + n_pl
+        return (n_cv * (sv_cv / n_cv) + n_pl * (sv_pl / n_pl)) / N ** 2
+
+    while rounds < max_rounds + 2:
+        v = np.where(use_cv, sv_cv / n_cv, sv_pl / n_pl)
+        N = n_cv + n_pl
+        # extra paths x of the chosen method: (S + x v) / (N + x)^2 <= se^2
+        S = n_cv * (sv_cv / n_cv) + n_pl * (sv_pl / n_pl)
+        a2 = se_target ** 2
+        disc = np.maximum((2 * N * a2 - v) ** 2 - 4 * a2 * (a2 * N * N - S), 0.0)
+        x = np.where(se2() > a2, np.ceil(((v - 2 * N * a2) + np.sqrt(disc)) / (2 * a2)), 0)
+        need = np.clip(x, 0, max_paths).astype(np.uint32)
+        if need.max() == 0:
             break
-        for bvp_id, mask in ((b_cv, use_cv), (b_plain, ~use_cv)):
-            pp = np.where(mask, need, 0).astype(np.uint32)
-            if pp.max() == 0:
-                continue
-            r = ctx.assemble(mesh, bvp_id, 0, h, fk.FP32, paths_per_item=pp, item_G=False, csr=False)
-            m = pp > 0
-            sum_phi[m] += r["item_stats"]["phi_VR"][m] * pp[m]
-            sum_B[m] += r["item_B"][m] * pp[m]
-            vr = np.maximum(r["item_stats"]["phiphi_VR"] - r["item_stats"]["phi_VR"] ** 2, 1e-30)
-            var[m] = vr[m]
-            done[m] += pp[m]
-            total_paths += int(pp.sum())
+        vr = np.maximum(ctx.assembly_round(mesh, b_plain, need, h, fk.FP32, bvp_of_item=bvp_of), 1e-30)
+        kern_ms.append(ctx.last_timing()[0])
+        m = need > 0
+        cvm, plm = m & use_cv, m & ~use_cv
+        sv_cv[cvm] += vr[cvm] * need[cvm]
+        n_cv[cvm] += need[cvm]
+        sv_pl[plm] += vr[plm] * need[plm]
+        n_pl[plm] += need[plm]
+        total_paths += int(need.sum())
         rounds += 1
+    r = ctx.assembly_end(mesh, items=True, item_G=False)
     t_total = time.perf_counter() - t0
-    phi = sum_phi / done
-    se = np.sqrt(var / done)
-    return {"items": n, "rows": info["n_rows"], "nnz": info["nnz"], "mesh_seconds": t_mesh,
+    end_ms = ctx.last_timing()[1]
+    # the end pass per G entry: the running row sum (8 B) and its CSR position
+    # (4 B) read, the CSR value read and written (16 B); per item its 12
+    # statistics read and its 16 written, B read and written
+    g_entries = int(sum(len(ctx.mesh_stencil_nodes(mesh, s)) * c for s, c in
+                        enumerate(np.bincount(stn, minlength=info["n_stencils"]))))
+    end_bytes = g_entries * (8 + 4 + 16) + n * (12 * 8 + 16 * 8 + 16)
+    # row residual of the assembled system with the exact solution
+    rp, col, v0 = ctx.mesh_csr(mesh)
+    nxy, _ = ctx.mesh_nodes(mesh)
+    u_nodes = franke(nxy[:, 0], nxy[:, 1])
+    diag = v0[rp[:-1] + np.array([np.searchsorted(col[rp[i]:rp[i + 1]], i) for i in range(len(rp) - 1)])]
+    resid = (np.add.reduceat(r["val"] * u_nodes[col], rp[:-1]) - r["B"]) / diag
+    se = np.sqrt(se2())
+    u = franke(ixy[:, 0], ixy[:, 1])
+    phi = r["item_stats"]["phi_VR"]
+    return {"items": n, "rows": info["n_rows"], "nnz": info["nnz"], "g_entries": g_entries,
+            "mesh_seconds": t_mesh, "pilot_seconds": t_pilot, "network_seconds": t_net,
             "assembly_seconds": t_total, "rounds": rounds, "total_paths": total_paths,
-            "paths_per_s": total_paths / t_total, "node_solves_per_s": n / t_total, "cv_items": int(use_cv.sum()),
-            "variance_reduction_median": float(np.median(v_plain / v_cv)),
+            "paths_per_s": total_paths / t_total, "node_solves_per_s": n / t_total,
+            "round_kernel_ms": kern_ms, "cv_items": int(use_cv.sum()),
+            "variance_reduction_median": float(np.median(v_pl / v_cv)),
             "se_max": float(se.max()), "se_median": float(np.median(se)),
             "items_below_target": float(np.mean(se <= se_target * 1.001)),
-            "rms_node_error": float(np.sqrt(np.mean((phi - u) ** 2))),
-            "paths_per_item_median": float(np.median(done))}
+            "rms_row_residual": float(np.sqrt(np.mean(resid ** 2))),
+            "rms_node_error_exact_exit": float(np.sqrt(np.mean((phi - u) ** 2))),
+            "paths_per_item_median": float(np.median(n_cv + n_pl)),
+            "end_pass": {"ms": end_ms, "algorithmic_bytes": end_bytes,
+                         "GB_per_s": end_bytes / (end_ms * 1e-3) / 1e9 if end_ms > 0 else None,
+                         "what": "rows from the device-resident sums into the CSR values and B"}}
 
 
 def disk_rows(ctx, n_disks=900, n_circle=44, n_radial=43, n_inner=44, seed=7, repeats=5):
