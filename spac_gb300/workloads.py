@@ -21,7 +21,11 @@
                 FP64) for perimeter circles, pseudospectral rows (N_radio 43)
                 for interior circles, GMRES on the host, node error
 
-  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows|serial_driver [--scale s]
+  assembly_cv   the 8 x 8 assembly (eps = 1/spacing) with the learned control
+                variate at 870 paths per item, h = 5e-5: pilot, training,
+                refit, table and three assemblies
+
+  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows|serial_driver|robin|assembly_cv [--scale s]
 
 All inputs are seeded synthetic data; nothing is read from disk.
 """
@@ -186,6 +190,22 @@ def learned_cv(ctx, problem, pxy, target, steps=50, lr=1e-2, table=256, seed=99)
     return ctx.register_bvp(problem, cv=fk.CV_MLP, mlp_id=mid)
 
 
+def assembly_cv(ctx, paths=870, h=5e-5, eps_spacing=1.0, pilot_grid=24, pilot_paths=600, pilot_h=1e-3, steps=50,
+                lr=1e-2, table=128, repeats=3):
+    """The 8 x 8 assembly with the learned control variate (the metric's CV
+    arm at a fixed path count): pilot point solves, training, output refit,
+    gradient table, then `repeats` assemblies; path and finalize kernel times."""
+    mesh = ctx.mesh_square_patches((0, 0, 1, 1), 8, 31, 0.25, eps_spacing, 20)
+    b_plain = ctx.register_bvp(fk.ANISO)
+    pxy, tgt = collocation_pilot(ctx, b_plain, pilot_grid, pilot_paths, pilot_h)
+    b_cv = learned_cv(ctx, fk.ANISO, pxy, tgt, steps=steps, lr=lr, table=table)
+    out = []
+    for _ in range(repeats):
+        r, t = _sync_time(lambda: ctx.assemble(mesh, b_cv, paths, h, fk.FP32, items=False))
+        out.append({"seconds": t, "kernels_ms": ctx.last_timing()[:2]})
+    return {"paths_per_item": paths, "h": h, "runs": out}
+
+
 def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_paths=256, max_rounds=6,
           max_paths=4_000_000, eps_spacing=3.0):
     """Adaptive assembly of the full CSR G/B: per item, paths until the
@@ -337,7 +357,8 @@ def serial_driver(ctx, paths=1000, h=1e-5, n_radial=43, precision=fk.FP64, repea
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows", "serial_driver", "robin"])
+    ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows", "serial_driver", "robin",
+                                         "assembly_cv"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=2026)
     a = ap.parse_args()
@@ -350,6 +371,8 @@ def main():
         r = disk_rows(ctx, n_disks=max(1, int(900 * a.scale)))
     elif a.workload == "serial_driver":
         r = serial_driver(ctx, paths=max(16, int(1000 * a.scale)))
+    elif a.workload == "assembly_cv":
+        r = assembly_cv(ctx, paths=max(32, int(870 * a.scale)))
     elif a.workload == "robin":
         r = robin(ctx, paths=max(64, int(4000 * a.scale)))
     else:
