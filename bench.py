@@ -649,7 +649,7 @@ def time_to_target_all(ctx, target=1e-3):
         mesh = ctx.mesh_square_patches(CFG["domain"], CFG["n_sub"], CFG["nodes_per_side"], CFG["enlarge"], eps_sp,
                                        CFG["knn"])
         sysm = AssembledSystem(ctx, mesh)
-        hs = (5e-4,) if eps_sp == 3.0 else (5e-4, 1e-4, 5e-5, 2.5e-5)
+        hs = (5e-4,) if eps_sp == 3.0 else (5e-4, 1e-4, 5e-5, 2.5e-5, 1e-5)
         r = {}
         for h in hs:
             r["h=%g" % h] = time_to_target(ctx, sysm, target=target, h=h)

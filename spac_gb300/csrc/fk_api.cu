@@ -154,6 +154,9 @@ struct fk_ctx {
 
 namespace {
 
+// shared memory per CTA of warp mode with per-warp moment accumulators (5
+// such CTAs fit on an SM)
+constexpr size_t kWmsCtaBytes = 45 * 1024;
 // items of at most this many paths on average run the path kernel in warp
 // mode (on the 8x8 assembly at h = 5e-5 warp mode is 26 % faster at 800 paths
 // per item, 4 % at 2000, and 6 % slower at 4000)
@@ -384,11 +387,30 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   // shared chunk slots.
   long long n_live = 0;
   for (auto& x : it) if (!x.frontera && x.paths > 0) ++n_live;
-  const bool warp_mode = !round && ctx->chunk <= 0 && n_live > 0 && total_paths <= kWarpModeMaxPaths * n_live;
-  const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes, warp_mode, block);
+  bool warp_mode = ctx->chunk <= 0 && n_live > 0 && total_paths <= kWarpModeMaxPaths * n_live;
+  // Adaptive rounds with items of few paths: warp mode with per-warp FP32
+  // moment accumulators in shared memory, so that the kernel forms the G rows
+  // (the rounds keep no moments in global memory).  CTAs of 4 warps (2 for
+  // large patches).  The accumulators and exit queues bound such a launch to
+  // about 12 warps per SM: on the 8 x 8 assembly at 870 paths per item the
+  // plain warp mode with global FP64 moments and the finalize kernel measured
+  // 5.9 ms against 7.9 ms, so CSR assemblies keep it.
+  int lblock = block;
+  bool wms = false;
+  if (warp_mode && kind == 2 && precision == FK_FP32 && round) {
+    const size_t P = fk::paths_slot_bytes(precision, kind, acc_words, smem_nodes);
+    const int wpb = 4 * P <= kWmsCtaBytes ? 4 : (2 * P <= kWmsCtaBytes ? 2 : 0);
+    if (wpb) {
+      wms = true;
+      lblock = 32 * wpb;
+    }
+  }
+  if (round && warp_mode && !wms) warp_mode = false;  // (rounds need rows formed in the kernel)
+  const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes, warp_mode, lblock, wms);
   if (sacc_bytes > 200 * 1024) return fail(ctx, FK_ERR_CAPACITY, "stencil accumulators exceed shared memory");
-  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, block, sacc_bytes, warp_mode);
+  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, lblock, sacc_bytes, warp_mode);
   const int grid = std::max(1, ctx->num_sms * occ);
+  const int block_used = lblock;
   // Chunk size.  Slots: at least 4 chunks per CTA of the persistent grid, at
   // most 32768 paths.  Warp mode: about 2 chunks per warp, 64..4096 paths
   // (measured on the 8x8 assembly and on point solves, finer chunks cost
@@ -396,11 +418,11 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   // split into equal chunks (no small remainder).
   long long chunk = ctx->chunk;
   if (chunk <= 0 && warp_mode) {
-    chunk = total_paths / (2LL * grid * (block / 32));
+    chunk = total_paths / (2LL * grid * (block_used / 32));
     chunk = std::max<long long>(64, std::min<long long>(chunk, 4096));
   } else if (chunk <= 0) {
     chunk = total_paths / (4LL * grid);
-    chunk = std::max<long long>(block, std::min<long long>(chunk, 32768));
+    chunk = std::max<long long>(block_used, std::min<long long>(chunk, 32768));
   }
   std::vector<fk::ChunkDev>& chunks = ctx->tmp_chunks;  // (reused: no page faults per call)
   chunks.clear();
@@ -427,11 +449,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   FK_CUDA(cudaMemsetAsync(ctx->w_stats.p, 0, static_cast<size_t>(n) * fk::kNumStats * sizeof(double), s));
   // slot mode with every item in one chunk: the chunks store their moments,
   // so the accumulators need no zeroing
-  bool whole_items = !warp_mode;
+  bool all_whole = true;
   for (const fk::ChunkDev& c : chunks)
-    if (c.p0 != 0 || c.p1 != it[c.item].paths) { whole_items = false; break; }
-  if (round) {
-    whole_items = false;  // (the rows go to g_sum: no moment accumulators in global memory)
+    if (c.p0 != 0 || c.p1 != it[c.item].paths) { all_whole = false; break; }
+  bool whole_items = !warp_mode && all_whole;
+  if (round || wms) {
+    whole_items = false;  // (the rows are formed in the kernel: no moment accumulators in global memory)
   } else {
     FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
     if (acc_total > 0 && !whole_items) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
@@ -475,12 +498,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   double* item_G = (kind && need_item_G) ? ctx->w_gout.as<double>() : nullptr;
   // G rows in the path kernel's flush: FP32 patch stencils whose chunks are
   // whole items and whose window corrections are small enough for FP32
-  bool fuse = precision == FK_FP32 && kind == 2 && whole_items && g_off && d_csr_idx && d_csr_val && !chunks.empty();
-  if (fuse)
-    for (float e : S->emax) fuse = fuse && e < fk::kSplitMaxE;
+  const bool fuse = precision == FK_FP32 && kind == 2 && all_whole && (wms || !warp_mode) && g_off && d_csr_idx &&
+                    d_csr_val && !chunks.empty();
   if (round && !(kind == 2 && g_off)) return fail(ctx, FK_ERR_ARG, "adaptive rounds need a square-patch mesh");
   if (fuse || round) {
     a.fuse_g = round ? 2 : 1;
+    a.wm_shared = wms ? 1 : 0;
     // FP32 moments with small window corrections: I + E_W in FP32; otherwise the FP64 inverses
     bool e32 = precision == FK_FP32;
     for (float e : S->emax) e32 = e32 && e < fk::kSplitMaxE;
@@ -493,7 +516,8 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
     a.g_sum = o.g_sum;
   }
   FK_CUDA(cudaEventRecord(ctx->ev[0], s));
-  if (!chunks.empty()) FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block, sacc_bytes, s, warp_mode));
+  if (!chunks.empty())
+    FK_CUDA(fk::launch_paths(a, bvp.problem, precision, grid, block_used, sacc_bytes, s, warp_mode));
   FK_CUDA(cudaEventRecord(ctx->ev[1], s));
   if (round) {
     FK_CUDA(fk::launch_round_stats(a.items, n, a.stats, o.run_stats, o.item_var, ctx->w_queue.as<int>() + 2, s));

@@ -110,6 +110,7 @@ struct LaunchArgs {
   // G row goes into the CSR values (and item_G if set); 2: adaptive rounds,
   // the chunk's unnormalised row is added to g_sum.
   int fuse_g;
+  int wm_shared;           // warp mode: moments in per-warp shared FP32 accumulators, rows fused
   const float* patch_e32;  // FP32 moments: E_W = A_W^-1 - I, the layout of the FP64 inverses
   const double* patch_ainv;  // FP64 moments: A_W^-1
   double* g_sum;           // fuse_g == 2: running row sums, g_off indexed
@@ -155,8 +156,9 @@ struct FinalizeArgs {
 // warp_mode: every warp works its own chunks and adds the stencil moments to
 // the items' global accumulators (items of few paths); otherwise the CTA's
 // warps share chunk slots with shared-memory accumulators
+// wm_shared: warp mode with per-warp FP32 moment accumulators in shared memory
 size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes, bool warp_mode = false,
-                        int block = 256);
+                        int block = 256, bool wm_shared = false);
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block,
                          size_t smem, cudaStream_t s, bool warp_mode = false);
 int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem,

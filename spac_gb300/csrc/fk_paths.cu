@@ -360,9 +360,12 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ SlotSh<R> slots[S];
   __shared__ ExitQueue<R> sq[kMaxBlockWarps];
-  const size_t acc_bytes = WM ? 0 : paths_slot_acc_bytes(kPrec, ST, a.acc_words);
-  const size_t slot_bytes = WM ? paths_slot_bytes(kPrec, ST, 0, a.smem_nodes)
-                               : paths_slot_bytes(kPrec, ST, a.acc_words, a.smem_nodes);
+  // warp mode with per-warp FP32 moment accumulators in shared memory (FP32
+  // patch stencils): the warp forms its chunk's G row itself when it leaves
+  constexpr bool kWmsCapable = WM && ST == 2 && std::is_same<R, float>::value;
+  const bool wms = kWmsCapable && a.wm_shared;
+  const size_t acc_bytes = (!WM || wms) ? paths_slot_acc_bytes(kPrec, ST, a.acc_words) : 0;
+  const size_t slot_bytes = paths_slot_bytes(kPrec, ST, (!WM || wms) ? a.acc_words : 0, a.smem_nodes);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const unsigned long long limit_ns =
@@ -389,7 +392,12 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
       if (lane == 0) cc = atomicAdd(a.queue, 1);
       c = __shfl_sync(kFull, cc, 0);
       if (c >= n_chunks) break;
-      stage_stencil<R, ST>(a, slots[si], smem_raw + si * slot_bytes, a.items[a.chunks[c].item].stencil, lane);
+      if (wms) {
+        uint4* z = reinterpret_cast<uint4*>(smem_raw + si * slot_bytes);
+        for (int i = lane; i < static_cast<int>(acc_bytes / 16); i += 32) z[i] = make_uint4(0u, 0u, 0u, 0u);
+      }
+      stage_stencil<R, ST>(a, slots[si], smem_raw + si * slot_bytes + acc_bytes, a.items[a.chunks[c].item].stencil,
+                           lane);
       __syncwarp();
     } else {
       if (dead == (1u << S) - 1u) break;
@@ -412,6 +420,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     // stencil moments: the slot's shared accumulators, or (warp mode) the
     // item's FP64 accumulators in global memory
     SAcc* sacc = WM ? reinterpret_cast<SAcc*>(a.acc + itg.acc_off) : reinterpret_cast<SAcc*>(mem);
+    float* wacc = reinterpret_cast<float*>(mem);  // (wms: the warp's FP32 moments)
     const R* snx = reinterpret_cast<const R*>(mem + acc_bytes);
     const R* sny = snx + a.smem_nodes;
     const double* sth = reinterpret_cast<const double*>(mem + acc_bytes);
@@ -536,9 +545,10 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
             const R arg = e2 * (dx * dx + dy * dy);
             if (!(arg < R(kPhiCut))) return false;
             const R wv = Yv * fexp(-arg);
-            if constexpr (WM && std::is_same<R, float>::value)
-              atomicAdd(&sacc[L * kk + j], f32_to_f64(wv));  // the item's FP64 accumulator in global memory
-            else
+            if constexpr (WM && std::is_same<R, float>::value) {
+              if (wms) atomicAdd(&wacc[L * kk + j], wv);     // the warp's FP32 moments in shared memory
+              else atomicAdd(&sacc[L * kk + j], f32_to_f64(wv));  // the item's FP64 accumulator in global memory
+            } else
               atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(wv));
             return true;
           };
@@ -804,7 +814,13 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
       if (n_done) atomicAdd(&sums[kStatPaths], static_cast<double>(n_done));
     }
     __syncwarp();
-    if (WM) continue;  // the warp's moments are already in global memory
+    if (WM) {
+      if constexpr (kWmsCapable) {
+        // the chunk's G row from the warp's own moments
+        if (wms) fused_patch_row<R, float>(a, itg, ch.item, sp, wacc, reinterpret_cast<double*>(mem + acc_bytes), lane);
+      }
+      continue;  // (otherwise the warp's moments are already in global memory)
+    }
     __threadfence_block();
     int left = 0;
     if (lane == 0) left = atomicSub(&sl.warps_left, 1);
@@ -892,8 +908,11 @@ const void* select_paths(int problem, int precision, int st, bool warp_mode, int
 
 }  // namespace
 
-size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes, bool warp_mode, int block) {
-  if (warp_mode) return static_cast<size_t>(block / 32) * paths_slot_bytes(precision, stencil_kind, 0, smem_nodes);
+size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes, bool warp_mode, int block,
+                        bool wm_shared) {
+  if (warp_mode)
+    return static_cast<size_t>(block / 32) *
+           paths_slot_bytes(precision, stencil_kind, wm_shared ? acc_words : 0, smem_nodes);
   return static_cast<size_t>(paths_slots(precision)) * paths_slot_bytes(precision, stencil_kind, acc_words, smem_nodes);
 }
 
