@@ -35,7 +35,8 @@ Mlp::~Mlp() {
   for (void* p : {static_cast<void*>(d_master), d_bf16, static_cast<void*>(d_m), static_cast<void*>(d_v),
                   static_cast<void*>(d_norm), static_cast<void*>(d_partial), static_cast<void*>(d_loss),
                   static_cast<void*>(d_rect), static_cast<void*>(d_table), static_cast<void*>(d_samples),
-                  static_cast<void*>(d_hist), static_cast<void*>(d_sync), static_cast<void*>(d_sched), d_fit})
+                  static_cast<void*>(d_hist), static_cast<void*>(d_sync), static_cast<void*>(d_sched), d_fit,
+                  d_tabwork})
     if (p) cudaFree(p);
 }
 
@@ -1223,19 +1224,34 @@ int mlp_fit_output(Mlp& M, int n, const double* xy, const double* target, const 
 int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err) {
   if (G < 2 || G > 2048) { err = "table grid must be 2..2048"; return FK_ERR_ARG; }
   const long long npts = static_cast<long long>(M.n_regions) * G * G;
-  if (M.d_tex) cudaDestroyTextureObject(static_cast<cudaTextureObject_t>(M.d_tex));
-  M.d_tex = 0;
-  if (M.d_table) cudaFree(M.d_table);
-  M.d_table = nullptr;
-  float2* d_pts = nullptr;
-  int* d_reg = nullptr;
-  float* d_eval = nullptr;
-  if (cudaMalloc(&M.d_table, npts * sizeof(float2)) != cudaSuccess ||
-      cudaMalloc(&d_pts, npts * sizeof(float2)) != cudaSuccess || cudaMalloc(&d_reg, npts * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&d_eval, 3 * npts * sizeof(float)) != cudaSuccess) {
-    err = "mlp table buffers";
-    return FK_ERR_CUDA;
+  // the table and its scratch only grow: a rebuild of the same size allocates nothing
+  const size_t tab_bytes = npts * sizeof(float2);
+  const bool same = M.d_table && M.table_cap >= tab_bytes && M.d_tex && M.tex_grid == G;
+  if (M.d_tex && !same) cudaDestroyTextureObject(static_cast<cudaTextureObject_t>(M.d_tex));
+  if (!same) {
+    M.d_tex = 0;
+    M.tex_grid = 0;
   }
+  if (M.table_cap < tab_bytes) {
+    if (M.d_table) cudaFree(M.d_table);
+    M.d_table = nullptr;
+    M.table_cap = 0;
+    if (cudaMalloc(&M.d_table, tab_bytes) != cudaSuccess) { err = "mlp table buffers"; return FK_ERR_CUDA; }
+    M.table_cap = tab_bytes;
+  }
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t b_pts = up(npts * sizeof(float2)), b_reg = up(npts * sizeof(int)), b_eval = up(3 * npts * sizeof(float));
+  if (M.tabwork_bytes < b_pts + b_reg + b_eval) {
+    if (M.d_tabwork) cudaFree(M.d_tabwork);
+    M.d_tabwork = nullptr;
+    M.tabwork_bytes = 0;
+    if (cudaMalloc(&M.d_tabwork, b_pts + b_reg + b_eval) != cudaSuccess) { err = "mlp table buffers"; return FK_ERR_CUDA; }
+    M.tabwork_bytes = b_pts + b_reg + b_eval;
+  }
+  unsigned char* wk = static_cast<unsigned char*>(M.d_tabwork);
+  float2* d_pts = reinterpret_cast<float2*>(wk);
+  int* d_reg = reinterpret_cast<int*>(wk + b_pts);
+  float* d_eval = reinterpret_cast<float*>(wk + b_pts + b_reg);
   mlp_grid_points<<<256, 256, 0, s>>>(M.d_rect, M.n_regions, G, d_pts, d_reg);
   cudaError_t e = cudaSuccess;
   for (int r = 0; r < M.n_regions && e == cudaSuccess; ++r)
@@ -1246,10 +1262,11 @@ int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err) {
     mlp_pack_table<<<256, 256, 0, s>>>(d_eval, npts, M.d_table);
     e = cudaStreamSynchronize(s);
   }
-  cudaFree(d_pts);
-  cudaFree(d_reg);
-  cudaFree(d_eval);
   if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
+  if (same) {
+    M.table_grid = G;  // (the texture object still describes this table)
+    return FK_OK;
+  }
   M.table_grid = G;
   // The texture unit interpolates the FP32 lookups (bilinear with 8-bit
   // fractional weights: the control term stays a martingale whatever grad
@@ -1281,8 +1298,12 @@ int mlp_build_table(Mlp& M, int G, cudaStream_t s, std::string& err) {
     td.readMode = cudaReadModeElementType;
     td.normalizedCoords = 0;
     cudaTextureObject_t t = 0;
-    if (cudaCreateTextureObject(&t, &rd, &td, nullptr) == cudaSuccess) M.d_tex = t;
-    else cudaGetLastError();
+    if (cudaCreateTextureObject(&t, &rd, &td, nullptr) == cudaSuccess) {
+      M.d_tex = t;
+      M.tex_grid = G;
+    } else {
+      cudaGetLastError();
+    }
   }
   return FK_OK;
 }

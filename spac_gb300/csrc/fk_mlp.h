@@ -31,6 +31,10 @@ struct Mlp {
   unsigned long long d_tex = 0;
   void* d_fit = nullptr;            // output-layer refit scratch (kept across calls)
   size_t fit_bytes = 0;
+  void* d_tabwork = nullptr;        // table build scratch: grid points, regions, evaluations (kept across calls)
+  size_t tabwork_bytes = 0;
+  size_t table_cap = 0;             // capacity of d_table (bytes)
+  int tex_grid = 0;                 // grid of the table that d_tex describes
   // capacities (bytes) of the training buffers, which only grow: a training
   // call allocates nothing once they are large enough
   size_t cap_samples = 0, cap_partial = 0, cap_loss = 0, cap_hist = 0, cap_sched = 0;
