@@ -276,10 +276,87 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
 __device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }  // (integer pipes)
 __device__ __forceinline__ double widen(double v) { return v; }
 
+// Fast path of fused_patch_row for FP32 moments, k = 20 and E_W in FP32:
+// each lane takes whole visited windows, W = lane, lane + 32, ...: the
+// window's 20 moments into registers, E_W's 100 float4 words loaded with all
+// loads in flight (one L2 round trip per window instead of one per row), and
+// v_W = t_W + E_W t_W written back over the moments; then lane gi sums the
+// (at most k) window terms of node gi in FP64 in a fixed order, with no
+// atomics.  Returns false where it does not apply.
+constexpr int kFastK = 20;
+template <typename R>
+__device__ bool fused_patch_row_fast(const LaunchArgs& a, const ItemDev& itg, int item, const PatchSh<R>& sp,
+                                     float* sacc, int lane) {
+  const int m = sp.m, k = sp.k, nwin = sp.closed ? m : m - k + 1;
+  if (k != kFastK || !a.patch_e32) return false;
+  const float* E = a.patch_e32 + a.patches[itg.stencil].ainv_off;
+  for (int W = lane; W < nwin; W += 32) {
+    float* t = sacc + W * kFastK;
+    float tv[kFastK];
+    bool vis = false;
+#pragma unroll
+    for (int b = 0; b < kFastK; ++b) {
+      tv[b] = t[b];
+      vis |= tv[b] != 0.f;
+    }
+    if (!vis) continue;
+    const float4* Ew = reinterpret_cast<const float4*>(E + static_cast<long long>(W) * kFastK * kFastK);
+    float v[kFastK];
+#pragma unroll
+    for (int r = 0; r < kFastK; ++r) v[r] = 0.f;
+#pragma unroll
+    for (int b = 0; b < kFastK; ++b) {  // column b of E_W: rows 0..19 in 5 float4 words
+#pragma unroll
+      for (int q = 0; q < kFastK / 4; ++q) {
+        const float4 e = __ldg(Ew + b * (kFastK / 4) + q);
+        v[4 * q] = fmaf(e.x, tv[b], v[4 * q]);
+        v[4 * q + 1] = fmaf(e.y, tv[b], v[4 * q + 1]);
+        v[4 * q + 2] = fmaf(e.z, tv[b], v[4 * q + 2]);
+        v[4 * q + 3] = fmaf(e.w, tv[b], v[4 * q + 3]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kFastK; ++r) t[r] = tv[r] + v[r];
+  }
+  __syncwarp();
+  const long long goff = a.g_off[item];
+  double ninv = 0.0;
+  if (a.fuse_g == 1) {
+    if (lane == 0) ninv = -1.0 / static_cast<double>(itg.paths);
+    ninv = __shfl_sync(kFull, ninv, 0);
+  }
+  for (int gi = lane; gi < m; gi += 32) {
+    double g = 0.0;
+    if (sp.closed) {
+      for (int tt = 0; tt < kFastK; ++tt) {
+        int W = gi - tt;
+        if (W < 0) W += m;
+        g += f32_to_f64(sacc[W * kFastK + tt]);
+      }
+    } else {
+      const int wlo = max(0, gi - kFastK + 1), whi = min(gi, m - kFastK);
+      for (int W = wlo; W <= whi; ++W) g += f32_to_f64(sacc[W * kFastK + gi - W]);
+    }
+    if (a.fuse_g == 2) {
+      if (g != 0.0) atomicAdd(&a.g_sum[goff + gi], -g);
+    } else {
+      g *= ninv;
+      if (a.item_G) a.item_G[goff + gi] = g;
+      // a row of several items (a node inside several patches) may meet a column twice
+      atomicAdd(&a.csr_val[a.csr_idx[goff + gi]], g);
+    }
+  }
+  __syncwarp();
+  return true;
+}
+
 template <typename R, typename SAcc>
 __device__ void fused_patch_row(const LaunchArgs& a, const ItemDev& itg, int item, const PatchSh<R>& sp,
-                                const SAcc* sacc, double* gbuf, int lane) {
+                                SAcc* sacc, double* gbuf, int lane) {
   constexpr bool k32 = std::is_same<SAcc, float>::value;
+  if constexpr (k32) {
+    if (fused_patch_row_fast<R>(a, itg, item, sp, sacc, lane)) return;
+  }
   const int m = sp.m, k = sp.k, nwin = sp.closed ? m : m - k + 1;
   const long long moff = a.patches[itg.stencil].ainv_off;
   for (int i = lane; i < m; i += 32) gbuf[i] = 0.0;
