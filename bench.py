@@ -800,22 +800,22 @@ def _mean_steps(ctx, mesh, bvp, prec, paths):
 
 
 def _scatter_roofline(info, f_ms, peaks, src, visited=None):
-    """HBM roofline of the finalize/scatter kernel.  Algorithmic bytes per
-    launch: per item its FP64 stencil moments (nwin x k words of the patch's
-    windows), its 12 FP64 statistics, a read-modify-write of its G entries in
-    the CSR values (16 B each) and of its B (16 B); per patch the FP32 window
-    corrections E_W (nwin x k^2) read once."""
-    k = CFG["knn"]
-    m = info["max_stencil"]            # patch-boundary nodes = windows of a closed chain
-    per_item = m * k * 8 + 12 * 8 + m * 16 + 16
-    per_patch = m * k * k * 4
-    bytes_ = info["n_items"] * per_item + info["n_stencils"] * per_patch
-    achieved = bytes_ / (f_ms * 1e-3) / 1e9
-    peak = peaks.get("hbm_gbs", 6800.0)
-    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": _read_profile_figures().get("finalize_dram_bytes_per_launch"), "algorithmic_bytes": bytes_,
+    """The G/B scatter of the 8x8 assembly.  It is fused into the path kernel:
+    the last warp out of an item forms the item's G row from its moments in
+    shared memory and adds it to the CSR values, so the window moments never
+    reach DRAM and the scatter's time cannot be separated from the path
+    kernel's.  Algorithmic DRAM bytes (per row: its CSR entries written, 12 B
+    each with their column, and B, 12 B) against the path kernel's measured
+    DRAM traffic per launch; the finalize launch that remains writes only
+    statistics and B.  The standalone HBM-bound scatter is config 5's end pass
+    (configs.config5.gpu.end_pass)."""
+    bytes_ = info["nnz"] * 12 + info["n_rows"] * 12
+    traffic = _read_profile_figures().get("paths_kernel_dram_bytes_per_launch")
+    return {"bound": "hbm", "fused_into": "paths_kernel", "algorithmic_bytes": bytes_, "traffic": traffic,
+            "traffic_over_algorithmic": traffic / bytes_ if traffic else None, "finalize_head_ms": f_ms,
+            "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({src})",
-            "note": "latency-bound: CTA-wide phases per item (moments staged, window products, CSR scatter)"}
+            "note": "traffic: ncu dram bytes of one path-kernel launch (committed capture, slot mode, whole items)"}
 
 
 def _read_profile_figures():
