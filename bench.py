@@ -514,6 +514,10 @@ def other_configs(ctx, cpu=None):
     out["config3"] = {"gpu": c3}
     c5 = wl.large(ctx)
     out["config5"] = {"gpu": c5}
+    # the same adaptive assembly with the stencil shape whose rows interpolate
+    # the exit value accurately (eps = 1/spacing; the specified 3/spacing
+    # leaves an O(0.1) row residual)
+    out["config5_eps_spacing_1"] = {"gpu": wl.large(ctx, eps_spacing=1.0)}
     if cpu:
         for k in out:
             out[k]["cpu"] = cpu.get(k)

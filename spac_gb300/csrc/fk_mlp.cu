@@ -711,10 +711,16 @@ __global__ void __launch_bounds__(256) mlp_gram_kernel(const float* feat, const 
 // Ridge solve (A^T A + lambda I) w = A^T t by Cholesky in FP64, lambda =
 // ridge x mean diagonal; writes W4 (w[0..W)) and b4 (w[W]) into the region's
 // FP32 parameters.  flag is set if the matrix is not positive definite.
+// One CTA: right-looking factorisation with the pivot's reciprocal (one FP64
+// division per column) and the trailing update over the lower triangle only,
+// then both triangular solves column by column across the CTA (a row's
+// unknown, then every later row updated in parallel), instead of one thread
+// walking the 65 x 65 triangles.
 __global__ void __launch_bounds__(256) mlp_lsq_kernel(const double* gram, float* params, double ridge, int* flag) {
   constexpr int N = W + 1;
   __shared__ double M[N][N + 1];
   __shared__ double rhs[N];
+  __shared__ double rinv[N];
   __shared__ double s_lam;
   __shared__ int s_bad;
   const int tid = threadIdx.x;
@@ -732,35 +738,49 @@ __global__ void __launch_bounds__(256) mlp_lsq_kernel(const double* gram, float*
   }
   for (int i = tid; i < N; i += blockDim.x) rhs[i] = gram[i * kGramCols + W + 1];
   __syncthreads();
-  // right-looking Cholesky: M = L L^T, L in the lower triangle
+  // M = L L^T, L in the lower triangle
   for (int k = 0; k < N; ++k) {
     if (tid == 0) {
       const double d = M[k][k];
       if (!(d > 0.0)) s_bad = 1;
-      M[k][k] = sqrt(d > 0.0 ? d : 1.0);
+      const double piv = sqrt(d > 0.0 ? d : 1.0);
+      M[k][k] = piv;
+      rinv[k] = 1.0 / piv;
     }
     __syncthreads();
-    const double piv = M[k][k];
-    for (int i = k + 1 + tid; i < N; i += blockDim.x) M[i][k] /= piv;
+    const double r = rinv[k];
+    for (int i = k + 1 + tid; i < N; i += blockDim.x) M[i][k] *= r;
     __syncthreads();
-    for (int e = tid; e < N * N; e += blockDim.x) {
-      const int i = e / N, j = e % N;
-      if (i > k && j > k && j <= i) M[i][j] -= M[i][k] * M[j][k];
+    // rows i > k, columns k < j <= i: T (T + 1) / 2 entries, T = N - k - 1
+    const int T = N - k - 1;
+    for (int e = tid; e < T * (T + 1) / 2; e += blockDim.x) {
+      // e -> (a, b), 0 <= b <= a < T, row-major over the triangle
+      int a = static_cast<int>((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
+      if ((a + 1) * (a + 2) / 2 <= e) ++a;
+      if (a * (a + 1) / 2 > e) --a;
+      const int b = e - a * (a + 1) / 2;
+      const int i = k + 1 + a, j = k + 1 + b;
+      M[i][j] -= M[i][k] * M[j][k];
     }
     __syncthreads();
   }
+  // L y = rhs: y_i, then every later row updated
+  for (int i = 0; i < N; ++i) {
+    if (tid == 0) rhs[i] *= rinv[i];
+    __syncthreads();
+    const double yi = rhs[i];
+    for (int j = i + 1 + tid; j < N; j += blockDim.x) rhs[j] -= M[j][i] * yi;
+    __syncthreads();
+  }
+  // L^T w = y: w_i, then every earlier row updated
+  for (int i = N - 1; i >= 0; --i) {
+    if (tid == 0) rhs[i] *= rinv[i];
+    __syncthreads();
+    const double wi = rhs[i];
+    for (int j = tid; j < i; j += blockDim.x) rhs[j] -= M[i][j] * wi;
+    __syncthreads();
+  }
   if (tid == 0) {
-    // L y = rhs, L^T w = y
-    for (int i = 0; i < N; ++i) {
-      double v = rhs[i];
-      for (int j = 0; j < i; ++j) v -= M[i][j] * rhs[j];
-      rhs[i] = v / M[i][i];
-    }
-    for (int i = N - 1; i >= 0; --i) {
-      double v = rhs[i];
-      for (int j = i + 1; j < N; ++j) v -= M[j][i] * rhs[j];
-      rhs[i] = v / M[i][i];
-    }
     if (s_bad) {
       atomicOr(flag, 1);
     } else {

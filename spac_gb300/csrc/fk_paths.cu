@@ -796,8 +796,17 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         const R stq = Problem<PROB>::template state<R>(bvp, inside ? x : w.ex, inside ? y : w.ey);
         if (inside) st = stq;
         const R sg = Problem<PROB>::template sigma_of<R>(stq);
-        const R nsx = w.nx * sg, nsy = w.ny * sg;
-        const R thr = R(kGobet) * fsqrt(nsx * nsx + nsy * nsy) * sqrth;
+        // Gobet shift kGobet |sigma^T n| sqrt(h) (FeynmanKacSolver.cpp:85,92).
+        // Every registered sigma is s I, and the normals are unit vectors (axes
+        // or the normalised diagonal), so FP32 stepping takes |sigma^T n| = s;
+        // FP64 stepping forms the norm as the reference does.
+        R thr;
+        if constexpr (std::is_same<R, float>::value) {
+          thr = R(kGobet) * sg * sqrth;
+        } else {
+          const R nsx = w.nx * sg, nsy = w.ny * sg;
+          thr = R(kGobet) * fsqrt(nsx * nsx + nsy * nsy) * sqrth;
+        }
         capped = k >= a.max_steps;
         exits = !(w.d < thr) || capped;
         if constexpr (RobinOf<PROB>::value) {
