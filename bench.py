@@ -662,7 +662,8 @@ def time_to_target_all(ctx, target=1e-3):
 
 
 def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=600, pilot_h=1e-3, train_steps=50,
-                   table=128, lr=1e-2, batch=4096, fit_output=True, n_cal=4000, only=None, gmres=True):
+                   table=128, lr=1e-2, batch=4096, fit_output=True, n_cal=4000, only=None, gmres=True,
+                   rep_streams=(7101, 7102)):
     """Time to `target` RMS row residual of the assembled system, plain FK vs
     the learned control variate (both FP32 stepping, same h, same paths for
     every item).
@@ -675,7 +676,9 @@ def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=60
     (train_steps Adam steps; with fit_output the output layer is then refitted
     by least squares on the hidden features), the gradient table and the
     assembly with the control term.  Each timed assembly's system is also
-    solved by the host GMRES and its node error reported."""
+    solved by the host GMRES and its node error reported.  Each method is
+    then timed again on the replicate streams at the same paths per item
+    (the CV's whole pipeline included) and the median time is reported."""
     from spac_gb300 import fk
     prec = fk.FP32
     b_plain = ctx.register_bvp(fk.ANISO)
@@ -700,6 +703,65 @@ def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=60
             last["earlier_attempts"] = attempts[:-1]
         return last
 
+    def replicate(bvp, n, before):
+        """Timed assemblies at n paths per item on the replicate streams;
+        `before()` runs first on each stream (its result is returned beside
+        the assembly time).  Returns ([(seconds, before()), ...], [rms, ...])."""
+        saved = ctx.get_stream()
+        ts, rs = [], []
+        for s in rep_streams:
+            ctx.set_stream(s)
+            f = before()
+            t, val, B, _ = _assemble_host(ctx, sysm.mesh, bvp, n, prec, h)
+            ts.append((t, f))
+            rs.append(_rms(sysm.residual(val, B)))
+        ctx.set_stream(saved)
+        return ts, rs
+
+    def cv_pipeline(drop=False):
+        """Pilot, training, output refit and gradient table of the learned
+        control variate (the network's weights reset to their initial values
+        first, untimed, as creating the network is); returns the stage times."""
+        t0 = time.perf_counter()
+        g = (np.arange(pilot_grid) + 0.5) / pilot_grid
+        pxy = np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2)  # x outer, y inner
+        # the pilot only has to approximate u (any u_hat keeps the estimator
+        # unbiased), so it runs at the coarse step pilot_h
+        pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec)
+        t_pilot = time.perf_counter() - t0
+        pilot_kernel_ms = ctx.last_timing()[0]
+        tgt = np.ascontiguousarray(pst["phi"])
+        pxy = np.ascontiguousarray(pxy)
+        # one network per context; its device buffers persist
+        mid = _cv_network(ctx, pxy, tgt, table)
+        t_reset0 = time.perf_counter()
+        ctx.check(ctx.L.fk_mlp_set_params(ctx.h, mid, _CV_NET[ctx.h.value][1].ctypes.data_as(fk._fp)))
+        t_reset = time.perf_counter() - t_reset0
+        hist = np.zeros(max(train_steps, 1), dtype=np.float32)
+        t1 = time.perf_counter()
+        if train_steps > 0:
+            ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp),
+                                         tgt.ctypes.data_as(fk._dp), None, train_steps, batch, lr, 777,
+                                         hist.ctypes.data_as(fk._fp)))
+        t_train = time.perf_counter() - t1
+        t_fit = 0.0
+        if fit_output:
+            # output layer refitted by least squares on the trained hidden layers
+            t3 = time.perf_counter()
+            ctx.check(ctx.L.fk_mlp_fit_output(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp),
+                                              tgt.ctypes.data_as(fk._dp), None, 1e-6))
+            t_fit = time.perf_counter() - t3
+        t2 = time.perf_counter()
+        ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
+        t_table = time.perf_counter() - t2
+        r = {"pilot_s": t_pilot, "train_s": t_train, "fit_output_s": t_fit, "table_s": t_table,
+             "fixed_s": t_pilot + t_train + t_fit + t_table, "untimed_weight_reset_s": t_reset,
+             "pilot_kernel_ms": pilot_kernel_ms}
+        if not drop:
+            r["mlp_id"] = mid
+            r["hist"] = hist
+        return r
+
     bias2, var_p, st_cal = sysm.calibrate(b_plain, h, n_cal)
     out["bias_rms_est"] = float(np.sqrt(bias2))
     # diagnostic: the same items scored with the exact exit value instead of the stencil
@@ -709,58 +771,44 @@ def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=60
         out["unreachable"] = "bias floor %.2e of the row residual at h=%g is above 0.9 x target" % (np.sqrt(bias2), h)
         return out
     if only != "cv":
-        out["plain"] = run_to_target(b_plain, bias2, var_p)
+        out["plain"] = plain = run_to_target(b_plain, bias2, var_p)
+        ts, rs = replicate(b_plain, plain["paths_per_item"], lambda: {})
+        plain["seconds_first"] = plain["seconds"]
+        plain["seconds_each"] = [plain["seconds"]] + [t for t, _ in ts]
+        plain["rms_each"] = [plain["rms"]] + rs
+        plain["seconds"] = float(np.median(plain["seconds_each"]))
 
     # learned control variate: pilot from boundary data only
-    t0 = time.perf_counter()
-    g = (np.arange(pilot_grid) + 0.5) / pilot_grid
-    pxy = np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2)  # x outer, y inner
-    # the pilot only has to approximate u (any u_hat keeps the estimator
-    # unbiased), so it runs at the coarse step pilot_h
-    pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec)
-    t_pilot = time.perf_counter() - t0
-    pilot_kernel_ms = ctx.last_timing()[0]
-    tgt = np.ascontiguousarray(pst["phi"])
-    pxy = np.ascontiguousarray(pxy)
-    # the network object is set up once per context (its device buffers
-    # persist) and reset to its initial weights for every run (untimed, as
-    # creating it is)
-    mid = _cv_network(ctx, pxy, tgt, table)
-    t_reset0 = time.perf_counter()
-    ctx.check(ctx.L.fk_mlp_set_params(ctx.h, mid, _CV_NET[ctx.h.value][1].ctypes.data_as(fk._fp)))
-    t_reset = time.perf_counter() - t_reset0
-    hist = np.zeros(max(train_steps, 1), dtype=np.float32)
-    t1 = time.perf_counter()
-    if train_steps > 0:
-        ctx.check(ctx.L.fk_mlp_train(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp),
-                                     None, train_steps, batch, lr, 777, hist.ctypes.data_as(fk._fp)))
-    t_train = time.perf_counter() - t1
-    t_fit = 0.0
-    if fit_output:
-        # output layer refitted by least squares on the trained hidden layers
-        t3 = time.perf_counter()
-        ctx.check(ctx.L.fk_mlp_fit_output(ctx.h, mid, len(tgt), pxy.ctypes.data_as(fk._dp),
-                                          tgt.ctypes.data_as(fk._dp), None, 1e-6))
-        t_fit = time.perf_counter() - t3
-    t2 = time.perf_counter()
-    ctx.check(ctx.L.fk_mlp_build_table(ctx.h, mid, table))
-    t_table = time.perf_counter() - t2
+    fixed0 = cv_pipeline()
+    mid = fixed0.pop("mlp_id")
     b_cv = ctx.register_bvp(fk.ANISO, cv=fk.CV_MLP, mlp_id=mid)
     bias2_c, var_c, _ = sysm.calibrate(b_cv, h, n_cal)
     cv = run_to_target(b_cv, bias2_c, var_c)
-    t_fixed = t_pilot + t_train + t_fit + t_table
-    cv.update({"seconds_run": cv["seconds"], "seconds": t_fixed + cv["seconds"], "pilot_s": t_pilot,
-               "untimed_weight_reset_s": t_reset,
-               "train_s": t_train, "train_steps": train_steps, "batch": batch, "lr": lr, "fit_output_s": t_fit,
-               "table_s": t_table, "pilot_kernel_ms": pilot_kernel_ms, "bias_rms_est": float(np.sqrt(bias2_c)),
-               "var_per_path": var_c,
-               "pilot": f"{len(pxy)} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
+    hist = fixed0.pop("hist")
+    cv.update(fixed0)
+    first_total = fixed0["fixed_s"] + cv["seconds"]
+    cv.update({"seconds_run": cv["seconds"], "seconds_first": first_total,
+               "train_steps": train_steps, "batch": batch, "lr": lr,
+               "bias_rms_est": float(np.sqrt(bias2_c)), "var_per_path": var_c,
+               "pilot": f"{pilot_grid ** 2} collocation points x {pilot_paths} whole-domain paths, h={pilot_h:g}",
                "train_loss_first_last": [float(hist[0]), float(hist[max(train_steps, 1) - 1])]})
+    # the whole pipeline again (weights reset, new pilot, training, refit,
+    # table, assembly) on other random streams
+    ts, rs = replicate(b_cv, cv["paths_per_item"], lambda: cv_pipeline(drop=True))
+    cv["seconds_each"] = [first_total] + [t + f["fixed_s"] for t, f in ts]
+    cv["seconds_run_each"] = [cv["seconds_run"]] + [t for t, _ in ts]
+    cv["fixed_s_each"] = [fixed0["fixed_s"]] + [f["fixed_s"] for _, f in ts]
+    cv["rms_each"] = [cv["rms"]] + rs
+    cv["seconds"] = float(np.median(cv["seconds_each"]))
+    cv["seconds_run"] = float(np.median(cv["seconds_run_each"]))
     out["learned_cv"] = cv
     out["variance_reduction"] = float(var_p / max(var_c, 1e-300))
     if "plain" in out:
         out["speedup_cv_over_plain"] = out["plain"]["seconds"] / cv["seconds"]
         out["speedup_cv_run_only"] = out["plain"]["seconds"] / cv["seconds_run"]
+        out["timing"] = (f"median of {1 + len(rep_streams)} timed runs per method: the run that met the target "
+                         f"and {len(rep_streams)} replicates at its paths per item on other random streams "
+                         "(each CV replicate redoes the pilot, training, refit and table)")
     return out
 
 

@@ -687,9 +687,9 @@ int fk_last_timing(const fk_ctx* ctx, double out[3]) {
 
 int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* d, int* id) {
   if (!ctx || !d || !id) return fail(ctx, FK_ERR_ARG, "null argument");
-  if (d->problem < 0 || d->problem > 4) return fail(ctx, FK_ERR_REGISTRY, "unknown problem functor");
+  if (d->problem < 0 || d->problem >= fk::kNumProblems) return fail(ctx, FK_ERR_REGISTRY, "unknown problem functor");
   if (d->cv < FK_CV_NONE || d->cv > FK_CV_MLP) return fail(ctx, FK_ERR_ARG, "unknown control-variate mode");
-  const int need_shape = (d->problem == FK_PROBLEM_DISK) ? FK_SHAPE_CIRCLE : FK_SHAPE_RECT;
+  const int need_shape = fk::problem_domain_shape(d->problem);
   if (d->dom_shape != need_shape) return fail(ctx, FK_ERR_ARG, "domain shape does not match the problem functor");
   if (d->cv == FK_CV_MLP && (d->mlp_id < 0 || d->mlp_id >= static_cast<int>(ctx->mlps.size())))
     return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");

@@ -4,6 +4,9 @@
 // or double); accumulations above the path level are FP64.
 #pragma once
 #include <cstdint>
+#include <type_traits>
+#include <utility>
+
 #include <cuda_runtime.h>
 
 namespace fk {
@@ -410,6 +413,39 @@ template <>
 struct RobinOf<4> {
   static constexpr bool value = true;
 };
+
+// ---- the compiled problem functor sets --------------------------------------
+// Every BVP functor set the library compiles, indexed by FK_PROBLEM_*
+// (include/spac_fk.h).  To add one: write its Problem<N> (state, sigma_of,
+// step and u as above, all for both stepping types; psi and a RobinOf<N>
+// specialisation if it has reflecting sides; a DomainOf<N> specialisation if
+// its domain is a circle), give it FK_PROBLEM_ value N = kNumProblems and
+// raise kNumProblems.  with_problem then instantiates and dispatches every
+// kernel (paths, finalize, disk rows) for it; the registry accepts it and
+// checks its domain shape.
+constexpr int kNumProblems = 5;
+template <int PROB>
+struct DomainOf {
+  static constexpr int shape = 0;  // FK_SHAPE_RECT: Dominios/Rectangulo.hpp
+};
+template <>
+struct DomainOf<3> {
+  static constexpr int shape = 1;  // FK_SHAPE_CIRCLE: Dominios/Circulo.hpp
+};
+template <int P>
+using ProblemTag = std::integral_constant<int, P>;
+// f(ProblemTag<problem>{}) for a problem id in [0, kNumProblems) (host code:
+// picks the kernel instantiation of a launch).
+template <int P = 0, typename F>
+inline auto with_problem(int problem, F&& f) -> decltype(f(ProblemTag<0>{})) {
+  if constexpr (P + 1 < kNumProblems) {
+    if (problem != P) return with_problem<P + 1>(problem, std::forward<F>(f));
+  }
+  return f(ProblemTag<P>{});
+}
+inline int problem_domain_shape(int problem) {
+  return with_problem(problem, [](auto t) { return DomainOf<decltype(t)::value>::shape; });
+}
 
 // Side of a rectangle that Dentro's nearest boundary point lies on (0: x = x0,
 // 1: y = y0, 2: x = x1, 3: y = y1), if it is in the reflecting mask; -1 for

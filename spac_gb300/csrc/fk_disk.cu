@@ -628,12 +628,7 @@ bool disk_prepare(const std::vector<DiskHost>& in, DiskBatch& out, std::string& 
 cudaError_t disk_launch(int problem, const DiskArgs& a, const DiskBatch& b, cudaStream_t s, cudaEvent_t* ev) {
   if (a.n_disks == 0) return cudaSuccess;
   if (ev) cudaEventRecord(ev[0], s);
-  switch (problem) {
-    case 0: disk_coef_kernel<0><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
-    case 1: disk_coef_kernel<1><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
-    case 2: case 4: disk_coef_kernel<2><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;  // ROBIN: ANISO's c, f
-    default: disk_coef_kernel<3><<<a.n_disks, kCoefThreads, 0, s>>>(a); break;
-  }
+  with_problem(problem, [&](auto t) { disk_coef_kernel<decltype(t)::value><<<a.n_disks, kCoefThreads, 0, s>>>(a); });
   const size_t mode_smem = static_cast<size_t>(kModeWarps) * b.max_half * (2 * b.max_half + 1) * sizeof(double);
   cudaError_t em = cudaFuncSetAttribute(disk_modes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(mode_smem));

@@ -531,30 +531,14 @@ cudaError_t launch_finalize(const FinalizeArgs& a, int problem, cudaStream_t s) 
   if (a.n_items <= 0) return cudaSuccess;
   if (a.g_fused) {
     const dim3 grid((a.n_items + 255) / 256), block(256);
-    switch (problem) {
-      case 1: finalize_head_kernel<1><<<grid, block, 0, s>>>(a); break;
-      case 2: case 4: finalize_head_kernel<2><<<grid, block, 0, s>>>(a); break;
-      case 3: finalize_head_kernel<3><<<grid, block, 0, s>>>(a); break;
-      default: finalize_head_kernel<0><<<grid, block, 0, s>>>(a); break;
-    }
+    with_problem(problem, [&](auto t) { finalize_head_kernel<decltype(t)::value><<<grid, block, 0, s>>>(a); });
     return cudaGetLastError();
   }
   const size_t psmem = finalize_patch_smem(a);
-  if (psmem > 0) {
-    switch (problem) {
-      case 1: return launch_patch_finalize_k<1>(a, psmem, s);
-      case 2: case 4: return launch_patch_finalize_k<2>(a, psmem, s);
-      case 3: return launch_patch_finalize_k<3>(a, psmem, s);
-      default: return launch_patch_finalize_k<0>(a, psmem, s);
-    }
-  }
+  if (psmem > 0)
+    return with_problem(problem, [&](auto t) { return launch_patch_finalize_k<decltype(t)::value>(a, psmem, s); });
   const dim3 grid(a.n_items), block(kFinalizeThreads);
-  switch (problem) {
-    case 1: finalize_kernel<1><<<grid, block, 0, s>>>(a); break;
-    case 2: case 4: finalize_kernel<2><<<grid, block, 0, s>>>(a); break;  // ROBIN: the ANISO u
-    case 3: finalize_kernel<3><<<grid, block, 0, s>>>(a); break;
-    default: finalize_kernel<0><<<grid, block, 0, s>>>(a); break;
-  }
+  with_problem(problem, [&](auto t) { finalize_kernel<decltype(t)::value><<<grid, block, 0, s>>>(a); });
   return cudaGetLastError();
 }
 

@@ -208,11 +208,11 @@ extern "C" int fk_solve_points_noalloc(const fk_bvp_desc* d, unsigned long long 
   using namespace fk;
   if (!d || n < 0 || (n > 0 && (!d_xy || !d_paths || !d_h || !d_out))) return FK_ERR_ARG;
   if (n > FK_NOALLOC_MAX_POINTS) return FK_ERR_CAPACITY;  // beyond the reserved scratch array
-  if (d->problem < 0 || d->problem > 4 || d->cv < FK_CV_NONE || d->cv > FK_CV_EXACT) return FK_ERR_ARG;
+  if (d->problem < 0 || d->problem >= kNumProblems || d->cv < FK_CV_NONE || d->cv > FK_CV_EXACT) return FK_ERR_ARG;
   if (d->problem == FK_PROBLEM_ROBIN &&
       !(d->prob[0] >= 0 && d->prob[0] <= 15 && d->prob[0] == std::floor(d->prob[0]) && d->prob[2] >= 0))
     return FK_ERR_ARG;
-  if (d->dom_shape != ((d->problem == FK_PROBLEM_DISK) ? FK_SHAPE_CIRCLE : FK_SHAPE_RECT)) return FK_ERR_ARG;
+  if (d->dom_shape != problem_domain_shape(d->problem)) return FK_ERR_ARG;
   if (precision != FK_FP64 && precision != FK_FP32) return FK_ERR_ARG;
   if (max_steps < 1 || max_steps > (1 << 30)) return FK_ERR_ARG;
   for (int i = 0; i < 4; ++i)

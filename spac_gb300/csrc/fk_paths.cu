@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     // Dentro's signed distance) than the domain boundary, wherever the path
     // is, so the domain distance cannot decide an exit and is not evaluated.
     bool dom_can_win = true;
-    if (has_sub && PROB != 3) {
+    if (has_sub && DomainOf<PROB>::shape == 0) {
       if (sub_circle)  // (r, cx, cy)
         dom_can_win = !(s1 - s0 > d0 && s1 + s0 < d2 && s2 - s0 > d1 && s2 + s0 < d3);
       else             // (x0, y0, x1, y1)
@@ -781,7 +781,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         // ---- exit rule (Dentro, FeynmanKacSolver.cpp:68-106)
         Bnd<R> w;
         if (dom_can_win) {
-          w = (PROB == 3) ? circle_dist<R>(x, y, d0, d1, d2) : rect_dist<R>(x, y, d0, d1, d2, d3);
+          w = (DomainOf<PROB>::shape == 1) ? circle_dist<R>(x, y, d0, d1, d2) : rect_dist<R>(x, y, d0, d1, d2, d3);
           if (has_sub) {
             const Bnd<R> sb = sub_circle ? circle_dist<R>(x, y, s0, s1, s2) : rect_dist<R>(x, y, s0, s1, s2, s3);
             if (!(w.d >= sb.d)) { w = sb; dom_wins = false; }
@@ -965,13 +965,7 @@ const void* paths_fn(int st, bool four) {
 }
 template <typename R, bool WM>
 const void* paths_fn_r(int problem, int st, bool four) {
-  switch (problem) {
-    case 1: return paths_fn<R, 1, WM>(st, four);
-    case 2: return paths_fn<R, 2, WM>(st, four);
-    case 3: return paths_fn<R, 3, WM>(st, four);
-    case 4: return paths_fn<R, 4, WM>(st, four);
-    default: return paths_fn<R, 0, WM>(st, four);
-  }
+  return with_problem(problem, [&](auto t) { return paths_fn<R, decltype(t)::value, WM>(st, four); });
 }
 const void* select_paths_v(int problem, int precision, int st, bool warp_mode, bool four) {
   if (warp_mode)
