@@ -52,8 +52,17 @@ extern "C" {
  *                      prob[0] = side mask (1: x = x0, 2: y = y0, 4: x = x1, 8: y = y1),
  *                      prob[1] = varphi (Y += varphi Y dL), prob[2] = rho (the
  *                      reflecting step runs within rho of the side); psi =
- *                      d_n u - varphi u (Z += psi Y dL), so u is the exact solution. */
-enum { FK_PROBLEM_FRANKE = 0, FK_PROBLEM_MONEGROS = 1, FK_PROBLEM_ANISO = 2, FK_PROBLEM_DISK = 3, FK_PROBLEM_ROBIN = 4 };
+ *                      d_n u - varphi u (Z += psi Y dL), so u is the exact solution.
+ *  FK_PROBLEM_MONEGROS_POISSON  BVPs/Monegros_Poisson.hpp:4-74 (the Monegros u
+ *                      with c = 0, f = -Lap u: the problem of main_test_mpi.cpp) */
+enum {
+  FK_PROBLEM_FRANKE = 0,
+  FK_PROBLEM_MONEGROS = 1,
+  FK_PROBLEM_ANISO = 2,
+  FK_PROBLEM_DISK = 3,
+  FK_PROBLEM_ROBIN = 4,
+  FK_PROBLEM_MONEGROS_POISSON = 5
+};
 /* Frontera distance functors: Dominios/Rectangulo.hpp:7-229 (x0,y0,x1,y1) and
  * Dominios/Circulo.hpp:7-22 (r,cx,cy). */
 enum { FK_SHAPE_RECT = 0, FK_SHAPE_CIRCLE = 1 };

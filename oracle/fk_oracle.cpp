@@ -196,7 +196,8 @@ struct Franke {
   }
 };
 
-// Monegros with c = -1 (BVPs/Monegros_Revamped.hpp:4-75).
+// The Monegros solution u and its derivatives, the same in
+// BVPs/Monegros_Revamped.hpp:4-40 and BVPs/Monegros_Poisson.hpp:4-40.
 const double mk1 = 1.0, mk2 = 0.01, mk3 = 0.02, mk4 = 0.12, mk5 = 0.05, mk6 = 0.05, mk7 = -0.12, msf = 0.333;
 double mon_u(double x, double y) {
   return 3.0 + msf * (std::sin(std::sqrt(mk1 + mk2 * x * x + mk3 * y * y)) +
@@ -262,11 +263,16 @@ Coef coefficients(const orc_bvp* B, double x, double y) {
       M2 nt{-c.s.a00, -c.s.a10, -c.s.a01, -c.s.a11};  // -(sigma^T)
       c.F = mul(nt, gr);
     }
-  } else if (B->problem == ORC_PROBLEM_MONEGROS) {
+  } else if (B->problem == ORC_PROBLEM_MONEGROS || B->problem == ORC_PROBLEM_MONEGROS_POISSON) {
     c.u = mon_u(x, y);
     c.g = c.u;
-    c.c = -1.0;
-    c.f = -mon_d2udx2(x, y) - mon_d2udy2(x, y) - c.c * c.u;
+    if (B->problem == ORC_PROBLEM_MONEGROS) {  // Monegros_Revamped.hpp:41-43,57-59
+      c.c = -1.0;
+      c.f = -mon_d2udx2(x, y) - mon_d2udy2(x, y) - c.c * c.u;
+    } else {  // Monegros_Poisson.hpp:41-43,57-59
+      c.c = -0.0;
+      c.f = -mon_d2udx2(x, y) - mon_d2udy2(x, y);
+    }
     c.b = V2{0.0, 0.0};
     c.s = M2{1.41421356237, 0.0, 0.0, 1.41421356237};
     if (B->cv == 1) {

@@ -22,9 +22,11 @@ extern "C" {
 enum { ORC_RNG_PHILOX = 0, ORC_RNG_SEQUENTIAL = 1 };
 enum { ORC_SHAPE_RECT = 0, ORC_SHAPE_CIRCLE = 1 };
 /* ORC_PROBLEM_ROBIN: ANISO with reflecting rectangle sides, prob = (side
- * mask 1: x = x0, 2: y = y0, 4: x = x1, 8: y = y1; varphi; rho; -) */
+ * mask 1: x = x0, 2: y = y0, 4: x = x1, 8: y = y1; varphi; rho; -).
+ * ORC_PROBLEM_MONEGROS: BVPs/Monegros_Revamped.hpp (c = -1);
+ * ORC_PROBLEM_MONEGROS_POISSON: BVPs/Monegros_Poisson.hpp (c = 0). */
 enum { ORC_PROBLEM_FRANKE = 0, ORC_PROBLEM_MONEGROS = 1, ORC_PROBLEM_ANISO = 2, ORC_PROBLEM_DISK = 3,
-       ORC_PROBLEM_ROBIN = 4 };
+       ORC_PROBLEM_ROBIN = 4, ORC_PROBLEM_MONEGROS_POISSON = 5 };
 enum { ORC_OUT_INSIDE = 0, ORC_OUT_DOMAIN = 1, ORC_OUT_SUBDOMAIN = 2 };
 
 typedef struct {

@@ -120,6 +120,7 @@ def philox(ctr, key):
 
 
 ROBIN = 4  # ORC_PROBLEM_ROBIN: prob = (side mask, varphi, rho, 0)
+MONEGROS_POISSON = 5  # ORC_PROBLEM_MONEGROS_POISSON: BVPs/Monegros_Poisson.hpp (c = 0)
 STAT_NAMES = ("phi", "phiphi", "phi_VR", "phiphi_VR", "xi", "xixi", "xiphi", "APL", "RNGC")
 
 

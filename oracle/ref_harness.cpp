@@ -11,6 +11,7 @@
 //   1 = Monegros, c = -1      BVPs/Monegros_Revamped.hpp (built in ref_harness_monegros.cpp)
 //   2 = anisotropic advection-reaction problem on [0,1]^2 (coefficients
 //       defined below with the reference's typedefs; u = Franke * (1+xy))
+//   5 = Monegros, c = 0       BVPs/Monegros_Poisson.hpp (built in ref_harness_monegros_poisson.cpp)
 #include <cstdio>
 #include <cstring>
 #include <unistd.h>
@@ -28,6 +29,7 @@
 // Defined in ref_harness_monegros.cpp (separate TU: the Monegros headers
 // reuse inline names of Franke_Poisson.hpp).
 void ref_fill_monegros(BVP& bvp);
+void ref_fill_monegros_poisson(BVP& bvp);
 
 namespace {
 
@@ -89,8 +91,11 @@ void fill_bvp(BVP& bvp, int problem, int use_F) {
     bvp.sigma.Inicializa(Franke_sigma);
     bvp.b.Inicializa(Franke_b);
     if (use_F) bvp.F.Inicializa(Franke_F);
-  } else if (problem == 1) {
-    ref_fill_monegros(bvp);
+  } else if (problem == 1 || problem == 5) {
+    if (problem == 1)
+      ref_fill_monegros(bvp);
+    else
+      ref_fill_monegros_poisson(bvp);
     if (!use_F) {
       Coeficiente_Vectorial zero;
       bvp.F = zero;

@@ -404,6 +404,32 @@ struct Problem<4> : Problem<2> {
   }
 };
 
+// FK_PROBLEM_MONEGROS_POISSON: BVPs/Monegros_Poisson.hpp, the Monegros u of
+// FK_PROBLEM_MONEGROS with c = 0 and f = -Lap u (the problem of the MPI
+// drivers, main_test_mpi.cpp:3,24-30).
+template <>
+struct Problem<5> {
+  template <typename R>
+  __device__ static R state(const BvpDev&, R, R) { return R(0); }
+  template <typename R>
+  __device__ static R sigma_of(R) { return R(1.41421356237); }
+  template <typename R>
+  __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
+    MonegrosEval<R> M(x, y);
+    o.s = R(1.41421356237);
+    o.c = R(0);
+    o.f = -M.lap;
+    o.bx = R(0);
+    o.by = R(0);
+    if (cv) {
+      o.Fx = -o.s * M.ux;
+      o.Fy = -o.s * M.uy;
+    }
+  }
+  template <typename R>
+  __device__ static R u(const BvpDev&, R x, R y) { return MonegrosEval<R>(x, y).u; }
+};
+
 // Problems with reflecting sides (the Paso_Reflejante branch of the step).
 template <int PROB>
 struct RobinOf {
@@ -423,7 +449,7 @@ struct RobinOf<4> {
 // raise kNumProblems.  with_problem then instantiates and dispatches every
 // kernel (paths, finalize, disk rows) for it; the registry accepts it and
 // checks its domain shape.
-constexpr int kNumProblems = 5;
+constexpr int kNumProblems = 6;
 template <int PROB>
 struct DomainOf {
   static constexpr int shape = 0;  // FK_SHAPE_RECT: Dominios/Rectangulo.hpp

@@ -14,7 +14,7 @@ from . import lib_path
 FK_OK = 0
 FK_ERR_ARG, FK_ERR_CUDA, FK_ERR_REGISTRY, FK_ERR_STEP_CAP = -1, -2, -3, -4
 FK_ERR_NOT_FOUND, FK_ERR_NO_DEVICE, FK_ERR_CAPACITY = -5, -6, -7
-FRANKE, MONEGROS, ANISO, DISK, ROBIN = 0, 1, 2, 3, 4
+FRANKE, MONEGROS, ANISO, DISK, ROBIN, MONEGROS_POISSON = 0, 1, 2, 3, 4, 5
 # reflecting sides of FK_PROBLEM_ROBIN (prob[0] is their sum)
 SIDE_X0, SIDE_Y0, SIDE_X1, SIDE_Y1 = 1, 2, 4, 8
 RECT, CIRCLE = 0, 1

@@ -4,7 +4,8 @@ against oracle/shim (oracle/Makefile target `ref`, library oracle/_ref/).
 
 Run where the reference sources exist:  python tests/golden/make_golden.py
 (`python tests/golden/make_golden.py ps` writes only the pseudospectral disk
-fixtures ps_disks.npz and ps_rows_*.npz.)
+fixtures ps_disks.npz and ps_rows_*.npz; `... points` only points.npy and
+coefs_monegros.npz.)
 The random stream is the shim's sequential stream with one OpenMP thread,
 which the oracle reproduces in its sequential mode.
 """
@@ -46,7 +47,12 @@ POINTS = [  # (problem, use_F, dom, (x, y), sub_kind, sub, N, h)
     (1, 1, (-200, -200, 200, 200), (150.0, 40.0), 2, (149.7, 39.8, 150.25, 40.3), 200, 1e-2),
     (2, 0, (0, 0, 1, 1), (0.5, 0.5), 1, (0.2, 0.5, 0.5), 200, 1e-3),
     (2, 1, (0, 0, 1, 1), (0.05, 0.93), 0, None, 200, 1e-3),
+    # Monegros_Poisson (c = 0), the problem of main_test_mpi.cpp
+    (5, 0, (-200, -200, 200, 200), (-72.0, -38.0), 2, (-72.3, -38.2, -71.75, -37.7), 200, 1e-3),
+    (5, 1, (-200, -200, 200, 200), (10.0, -20.0), 1, (0.3, 10.1, -20.05), 200, 1e-2),
 ]
+# coefficient probes of the two Monegros problems (1: c = -1, 5: c = 0) on their domain
+MONEGROS_PROBES = 64
 
 
 def ref():
@@ -170,12 +176,43 @@ def ps_fixtures(L):
                             params=np.array([problem, nr]))
 
 
+def point_fixtures(L):
+    """points.npy (reference point solves) and coefs_monegros.npz."""
+    # point solves: each on a fresh session (sequential stream from the start)
+    pts = []
+    for problem, use_F, dom, (x, y), sk, sub, N, h in POINTS:
+        s = L.ref_solver_new(1)
+        out = (C.c_double * 9)()
+        sp = (C.c_double * 4)(*(sub if sub else (0, 0, 0, 0)))
+        L.ref_point_solve(s, problem, use_F, (C.c_double * 4)(*dom), sk, sp, x, y, N, h, out)
+        L.ref_solver_free(C.c_void_p(s))
+        subv = list(sub) if sub else [0, 0, 0, 0]
+        subv += [0] * (4 - len(subv))
+        pts.append([problem, use_F, *dom, x, y, sk, *subv, N, h, *list(out)])
+    np.save(os.path.join(HERE, "points.npy"), np.array(pts))
+    rng = np.random.default_rng(11)
+    probe = rng.uniform(-200.0, 200.0, size=(MONEGROS_PROBES, 2))
+    o12 = (C.c_double * 12)()
+    coefs = []
+    for x, y in probe:
+        row = []
+        for p in (1, 5):
+            L.ref_coefficients(p, x, y, o12)
+            row += list(o12)
+        coefs.append(row)
+    np.savez_compressed(os.path.join(HERE, "coefs_monegros.npz"), probe=probe, coefs=np.array(coefs))
+
+
 def main():
     L = ref()
     L.ref_solver_free.argtypes = [C.c_void_p]
     if sys.argv[1:] == ["ps"]:
         ps_fixtures(L)
         print("pseudospectral fixtures written to", HERE)
+        return 0
+    if sys.argv[1:] == ["points"]:
+        point_fixtures(L)
+        print("point fixtures written to", HERE)
         return 0
     for name, dom, Nl, sup, th0, npc in MESHES:
         m = mesh_and_assembly(L, name, 0, 0, 1, 1e-3, False)
@@ -200,18 +237,7 @@ def main():
     for f in ("G.txt", "B.txt", "G_i.txt", "G_j.txt", "G_ij.txt", "knot_position.txt"):
         shutil.copy(os.path.join(tmp, "Output", f), os.path.join(out, f))
     shutil.rmtree(tmp)
-    # point solves: each on a fresh session (sequential stream from the start)
-    pts = []
-    for problem, use_F, dom, (x, y), sk, sub, N, h in POINTS:
-        s = L.ref_solver_new(1)
-        out = (C.c_double * 9)()
-        sp = (C.c_double * 4)(*(sub if sub else (0, 0, 0, 0)))
-        L.ref_point_solve(s, problem, use_F, (C.c_double * 4)(*dom), sk, sp, x, y, N, h, out)
-        L.ref_solver_free(C.c_void_p(s))
-        subv = list(sub) if sub else [0, 0, 0, 0]
-        subv += [0] * (4 - len(subv))
-        pts.append([problem, use_F, *dom, x, y, sk, *subv, N, h, *list(out)])
-    np.save(os.path.join(HERE, "points.npy"), np.array(pts))
+    point_fixtures(L)
     # distance functors and coefficients at probe points, incl. centre lines and corners
     rng = np.random.default_rng(7)
     probe = np.concatenate([rng.uniform(-0.3, 1.3, size=(200, 2)),

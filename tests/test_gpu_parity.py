@@ -41,6 +41,8 @@ CASES = [  # problem, cv, dom, points, sub (shape, params) or None, h
     (2, 1, (0, 0, 1, 1), [(0.6, 0.45)], None, 1e-3),
     (1, 1, (-200, -200, 200, 200), [(-72.0, -38.0)], (0, (-72.3, -38.2, -71.75, -37.7)), 1e-3),
     (3, 0, (0.8, 0.1, -0.2), [(0.3, 0.1), (-0.5, -0.4)], None, 1e-3),
+    (5, 0, (-200, -200, 200, 200), [(10.0, -20.0)], (1, (0.3, 10.1, -20.05, 0.0)), 1e-3),
+    (5, 1, (-200, -200, 200, 200), [(-72.0, -38.0)], (0, (-72.3, -38.2, -71.75, -37.7)), 1e-3),
 ]
 
 

@@ -34,6 +34,15 @@ def test_distance_functors_and_coefficients(orc):
     assert orc.circulo(g["circ"], 0.5, 0.45) == list(g["circ_center"])
 
 
+def test_monegros_coefficients(orc):
+    """Both Monegros problems (Monegros_Revamped.hpp, c = -1; Monegros_Poisson.hpp, c = 0)."""
+    g = np.load(os.path.join(GOLDEN, "coefs_monegros.npz"))
+    b1, b5 = orc.bvp(1, cv=1), orc.bvp(orc.MONEGROS_POISSON, cv=1)
+    for i, (x, y) in enumerate(g["probe"]):
+        assert orc.coefficients(b1, x, y) == list(g["coefs"][i][:12])
+        assert orc.coefficients(b5, x, y) == list(g["coefs"][i][12:])
+
+
 def test_point_solves_bit_exact(orc):
     pts = np.load(os.path.join(GOLDEN, "points.npy"))
     for row in pts:
