@@ -12,7 +12,7 @@
  *    cudaPointerGetAttributes); device pointers are written in place on the
  *    context's stream and the call returns after the stream has drained.
  *  - Random numbers: counter-based Philox4x32-10.  Path p of item i in a call
- *    with stream id s uses counter (step/2, p, i, s) and key (seed lo, seed hi);
+ *    with stream id s uses counter (step, p, i, s) and key (seed lo, seed hi);
  *    the stream id advances by one after every solve call unless set with
  *    fk_set_stream.  Results are therefore reproducible for a given seed and
  *    call sequence, independent of the launch shape.
@@ -180,7 +180,7 @@ int fk_autotune_points(fk_ctx* ctx, int n, const int* bvp_ids, const double* xy,
  * and real-time hosts that cannot afford an allocation's latency or the
  * device synchronisation it may imply.  Same kernels and random stream as
  * fk_solve_points (point i, path p uses the Philox counter
- * (step/2, p, i, stream_id) under key seed), and every point's paths are
+ * (step, p, i, stream_id) under key seed), and every point's paths are
  * split into chunks over the whole grid as there; no fk_ctx is needed.
  * d_xy (2n doubles), d_paths (n), d_h (n) and d_out (n fk_stats) are device
  * buffers owned by the caller; launches go on `cuda_stream` (a cudaStream_t,

@@ -65,20 +65,20 @@ struct Session {
 };
 
 // Brownian increment for step k of a path (Actualiza_Incremento,
-// FeynmanKacSolver.cpp:2-6).  Philox mode: counter (k/2, path, item, stream),
-// key (seed lo, seed hi); words (r0,r1) feed even steps, (r2,r3) odd steps.
+// FeynmanKacSolver.cpp:2-6).  Philox mode: counter (k, path, item, stream),
+// key (seed lo, seed hi); words (r0, r1) feed the step's Box-Muller pair.
 void increment(Session& S, uint32_t item, uint32_t path, int k, double sqrth, double dW[2]) {
   if (S.mode == ORC_RNG_SEQUENTIAL) {
     dW[0] = sqrth * S.seq_normal();
     dW[1] = sqrth * S.seq_normal();
     return;
   }
-  uint32_t ctr[4] = {static_cast<uint32_t>(k >> 1), path, item, S.stream};
+  uint32_t ctr[4] = {static_cast<uint32_t>(k), path, item, S.stream};
   uint32_t key[2] = {static_cast<uint32_t>(S.seed), static_cast<uint32_t>(S.seed >> 32)};
   uint32_t r[4];
   philox(ctr, key, r);
-  uint32_t a = (k & 1) ? r[2] : r[0];
-  uint32_t b = (k & 1) ? r[3] : r[1];
+  uint32_t a = r[0];
+  uint32_t b = r[1];
   double u1 = (static_cast<double>(a) + 0.5) * kInv32;
   double u2 = (static_cast<double>(b) + 0.5) * kInv32;
   double rad = std::sqrt(-2.0 * std::log(u1));

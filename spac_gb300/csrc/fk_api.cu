@@ -85,9 +85,10 @@ struct StencilSet {
   std::vector<PatchDev> patches;
   std::vector<double> patch_nodes;
   std::vector<int> patch_gids;
+  std::vector<unsigned short> knn_tab;  // window tables (PatchDev::knn_off)
   long long ipsi_total = 0, ainv_total = 0;
   int nmax = 0;
-  DBuf d_arcs, d_theta, d_ipsi, d_patches, d_nodes, d_ainv;
+  DBuf d_arcs, d_theta, d_ipsi, d_patches, d_nodes, d_ainv, d_knn;
   DBuf d_e32, d_emax;  // patches: A^-1 - I in FP32 and its max |.| per patch
   std::vector<float> emax;  // host copy of d_emax
   bool uploaded = false;
@@ -240,6 +241,7 @@ int upload_stencils(fk_ctx* ctx, fk::StencilSet& S, const std::vector<char>* hav
   } else if (S.kind == 2) {
     FK_CUDA(fk::upload(S.d_patches, S.patches, s));
     FK_CUDA(fk::upload(S.d_nodes, S.patch_nodes, s));
+    FK_CUDA(fk::upload(S.d_knn, S.knn_tab, s));
     FK_CUDA(S.d_ainv.ensure(std::max<long long>(S.ainv_total, 1) * sizeof(double)));
     const int n_p = static_cast<int>(S.patches.size());
     std::vector<long long> win_base(n_p + 1, 0);
@@ -289,6 +291,129 @@ void add_arc(fk::StencilSet& S, const fk::MeshStencil& M, const int* gids_overri
   S.arcs.push_back(a);
 }
 
+// Largest chain offset |d| between an exit's nearest node and a node within
+// the weight cutoff rcut of the exit (a bound).  The exit e lies on the patch
+// boundary within d_en of its nearest node n (half a side step, or the gap
+// between a side's end node and the corner); consecutive chain nodes are at
+// least s_min apart, so the boundary path from e to the node d places away is
+// at least |d| s_min - d_en long.  On one side or two adjacent sides of a
+// rectangle the straight distance is at least that path / sqrt 2 (nodes of the
+// opposite side are beyond the cutoff wherever a walk is used), so a node
+// within rcut has |d| < (sqrt 2 rcut + d_en) / s_min.
+int patch_span_bound(const fk::MeshStencil& M, double rcut) {
+  const int m = static_cast<int>(M.nodes.size());
+  if (m < 2) return 1 << 20;
+  double s_min = 1e300, d_en = 0.0;
+  for (int i = 0; i + 1 < m + (M.closed ? 1 : 0); ++i) {
+    const fk::MeshNode& a = M.nodes[i];
+    const fk::MeshNode& b = M.nodes[(i + 1) % m];
+    s_min = std::min(s_min, std::hypot(b.x - a.x, b.y - a.y));
+  }
+  for (int s = 0; s < 4; ++s) {
+    const int c = M.side_count[s];
+    if (c <= 0) continue;
+    const int ax = M.side_axis[s];  // the coordinate that varies along the side
+    const double lo = ax == 0 ? M.rect[0] : M.rect[1], hi = ax == 0 ? M.rect[2] : M.rect[3];
+    double cmin = 1e300, cmax = -1e300;
+    for (int i = 0; i < c; ++i) {
+      const fk::MeshNode& nd = M.nodes[M.side_first[s] + i];
+      const double v = ax == 0 ? nd.x : nd.y;
+      cmin = std::min(cmin, v);
+      cmax = std::max(cmax, v);
+    }
+    d_en = std::max(d_en, std::max(0.5 * std::fabs(M.side_step[s]), std::max(cmin - lo, hi - cmax)));
+  }
+  if (!(s_min > 0.0)) return 1 << 20;
+  return static_cast<int>(std::floor((std::sqrt(2.0) * rcut + d_en) / s_min));
+}
+
+// The k-window start of a point on the patch boundary by the path kernel's
+// sliding search (knn_window in fk_paths.cu), in FP64.
+int knn_window_host(const fk::MeshStencil& M, int k, double ex, double ey) {
+  const int m = static_cast<int>(M.nodes.size());
+  int best_s = -1;
+  double best = 1e300;
+  for (int s = 0; s < 4; ++s) {
+    if (M.side_count[s] > 0) {
+      const double dist = std::fabs((M.side_axis[s] == 0 ? ey : ex) - M.side_fixed[s]);
+      if (dist < best) { best = dist; best_s = s; }
+    }
+  }
+  int nearest = 0;
+  if (best_s >= 0) {
+    const double coord = M.side_axis[best_s] == 0 ? ex : ey;
+    int j = static_cast<int>(std::rint((coord - M.side_start[best_s]) * (1.0 / M.side_step[best_s])));
+    j = std::max(0, std::min(M.side_count[best_s] - 1, j));
+    nearest = M.side_first[best_s] + j;
+  }
+  auto d2 = [&](int idx) {
+    if (idx >= m) idx -= m;
+    if (idx < 0) idx += m;
+    const double dx = ex - M.nodes[idx].x, dy = ey - M.nodes[idx].y;
+    return dx * dx + dy * dy;
+  };
+  int L = nearest - k / 2;
+  if (M.closed) {
+    if (L < 0) L += m;
+    for (int it = 0; it < m && d2(L - 1) < d2(L + k - 1); ++it) { --L; if (L < 0) L += m; }
+    for (int it = 0; it < m && d2(L + k) < d2(L); ++it) { ++L; if (L >= m) L -= m; }
+  } else {
+    L = std::max(0, std::min(m - k, L));
+    while (L > 0 && d2(L - 1) < d2(L + k - 1)) --L;
+    while (L < m - k && d2(L + k) < d2(L)) ++L;
+  }
+  return L;
+}
+
+// Window table of a patch: for each side, the window start at kKnnBins bins
+// per side step over the side's whole extent (corner to corner).  Along the
+// boundary the k-window moves monotonically with the exit point, so a bin
+// whose two ends (and middle) have windows L0 and L0 or L0 + 1 holds only
+// those two: the path kernel picks L0 + 1 iff node L0 + k is nearer than node
+// L0, the sliding search's own step.  Other bins are marked kKnnFull.
+void add_knn_table(fk::StencilSet& S, fk::PatchDev& p, const fk::MeshStencil& M, int k) {
+  const int m = static_cast<int>(M.nodes.size());
+  p.knn_off = static_cast<long long>(S.knn_tab.size());
+  int base = 0;
+  for (int s = 0; s < 4; ++s) {
+    p.knn_base[s] = base;
+    p.knn_n[s] = 0;
+    p.knn_u0[s] = 0.0;
+    const int c = M.side_count[s];
+    if (c <= 0 || !(M.side_step[s] != 0.0) || m < k) continue;
+    const int ax = M.side_axis[s];
+    const double lo = ax == 0 ? M.rect[0] : M.rect[1], hi = ax == 0 ? M.rect[2] : M.rect[3];
+    const double ua = (lo - M.side_start[s]) / M.side_step[s], ub = (hi - M.side_start[s]) / M.side_step[s];
+    const double u0 = std::min(ua, ub), u1 = std::max(ua, ub);
+    const int nb = std::max(1, static_cast<int>(std::ceil((u1 - u0) * fk::kKnnBins)));
+    auto point_at = [&](double u, double& x, double& y) {
+      const double along = M.side_start[s] + u * M.side_step[s];
+      x = ax == 0 ? along : M.side_fixed[s];
+      y = ax == 0 ? M.side_fixed[s] : along;
+    };
+    auto win_at = [&](double u) {
+      double x, y;
+      point_at(u, x, y);
+      return knn_window_host(M, k, x, y);
+    };
+    int left = win_at(u0);
+    for (int b = 0; b < nb; ++b) {
+      const int right = win_at(u0 + static_cast<double>(b + 1) / fk::kKnnBins);
+      const int mid = win_at(u0 + (b + 0.5) / fk::kKnnBins);
+      int step = right - left;
+      if (M.closed && step < 0) step += m;
+      int smid = mid - left;
+      if (M.closed && smid < 0) smid += m;
+      const bool ok = (step == 0 || step == 1) && (smid == 0 || smid == step) && left < 0x4000;
+      S.knn_tab.push_back(ok ? static_cast<unsigned short>(left) : fk::kKnnFull);
+      left = right;
+    }
+    p.knn_n[s] = nb;
+    p.knn_u0[s] = u0;
+    base += nb;
+  }
+}
+
 void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
   fk::PatchDev p;
   std::memset(&p, 0, sizeof(p));
@@ -308,7 +433,9 @@ void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
   // always beyond the weight cutoff, a walk outward from the exit may stop
   // at its first cut node (0.9 W leaves a margin for rounding).
   const double W = 0.9 * std::min(M.rect[2] - M.rect[0], M.rect[3] - M.rect[1]);
-  p.walk = (p.eps2 * W * W >= static_cast<double>(fk::kPhiCut)) ? 1 : 0;
+  p.walk = (p.eps2 * W * W >= static_cast<double>(fk::kPhiCut)) ? fk::kWalkStop : fk::kWalkFull;
+  if (p.walk == fk::kWalkStop && patch_span_bound(M, std::sqrt(static_cast<double>(fk::kPhiCut) / p.eps2)) <= fk::kSpanMax)
+    p.walk = fk::kWalkSpan;
   p.node_off = static_cast<long long>(S.patch_nodes.size());
   p.ainv_off = S.ainv_total;
   S.ainv_total += static_cast<long long>(p.nwin) * k * k;
@@ -318,6 +445,7 @@ void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
     S.patch_gids.push_back(nd.gid);
   }
   S.nmax = std::max(S.nmax, p.m);
+  add_knn_table(S, p, M, k);
   S.patches.push_back(p);
 }
 
@@ -470,7 +598,11 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   a.chunks = ctx->w_chunks.as<fk::ChunkDev>();
   a.n_chunks = static_cast<int>(chunks.size());
   if (kind == 1) { a.arcs = S->d_arcs.as<fk::ArcDev>(); a.arc_theta = S->d_theta.as<double>(); }
-  if (kind == 2) { a.patches = S->d_patches.as<fk::PatchDev>(); a.patch_nodes = S->d_nodes.as<double>(); }
+  if (kind == 2) {
+    a.patches = S->d_patches.as<fk::PatchDev>();
+    a.patch_nodes = S->d_nodes.as<double>();
+    a.knn_tab = S->d_knn.as<unsigned short>();
+  }
   a.queue = ctx->w_queue.as<int>();
   a.stats = ctx->w_stats.as<double>();
   a.acc = round ? nullptr : ctx->w_acc.as<double>();

@@ -14,8 +14,8 @@ namespace fk {
 constexpr double kGobet = -0.5826;  // Gobet-Menozzi shift, FeynmanKacSolver.cpp:169,184
 
 // ------------------------------------------------------------------ Philox ----
-// Philox4x32-10 (Salmon et al., SC'11).  Counter (step/2, path, item, stream),
-// key (seed lo, seed hi).
+// Philox4x32-10 (Salmon et al., SC'11).  Counter (step, path, item, stream),
+// key (seed lo, seed hi); the step's Box-Muller pair takes words x and y.
 __device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {

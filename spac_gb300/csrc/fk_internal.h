@@ -39,13 +39,19 @@ struct PatchDev {
   double rect[4];
   double eps2;
   int m, k, closed, nwin;
-  int walk;             // 1: the stencil walk may stop at its first cut node
+  int walk;             // kWalkFull, kWalkStop or kWalkSpan (how an exit visits its window's nodes)
   long long node_off;   // 2*m doubles (x, y) in chain order
   long long ainv_off;   // nwin * k * k doubles, column-major per window
   // sides: chain index of the first node, node count, axis (0: node x varies),
   // fixed coordinate, coordinate of the first node and signed step
   int side_first[4], side_count[4], side_axis[4];
   double side_fixed[4], side_start[4], side_step[4];
+  // window table (kKnnBins bins per side step): side s has knn_n[s] entries
+  // from knn_off + knn_base[s], bin b covering u in knn_u0[s] + [b, b+1) /
+  // kKnnBins, u = (coordinate along the side - side_start) / side_step
+  long long knn_off;
+  int knn_base[4], knn_n[4];
+  double knn_u0[4];
 };
 
 // Per-item FP64 sums written by the path kernel: score, score^2, xi + xi^2
@@ -64,6 +70,19 @@ constexpr int kSlotsFP32 = 3;
 
 // Gaussian stencil weights exp(-arg) with arg >= kPhiCut (< 1e-30) are not added.
 constexpr float kPhiCut = 69.0f;
+// How an exit visits the nodes of its k-window (PatchDev::walk):
+//   kWalkFull  every node of the window;
+//   kWalkStop  outward from the exit's nearest node, each way until the first
+//              node beyond the weight cutoff;
+//   kWalkSpan  the nodes within kSpanMax chain places of the nearest node, a
+//              fixed unrolled range that holds every node within the cutoff.
+constexpr int kWalkFull = 0, kWalkStop = 1, kWalkSpan = 2;
+constexpr int kSpanMax = 4;
+// Window table of a patch side: the exit's k-window is L0 or L0 + 1 (the
+// latter iff node L0 + k is nearer than node L0); an entry with kKnnFull set
+// sends the exit to the sliding search.
+constexpr int kKnnBins = 16;
+constexpr unsigned short kKnnFull = 0x8000;
 __host__ __device__ inline int paths_slots(int precision) { return precision == 0 ? 2 : kSlotsFP32; }
 __host__ __device__ inline size_t paths_slot_acc_bytes(int precision, int stencil_kind, int acc_words) {
   const size_t w = (precision == 0 || stencil_kind == 1) ? 8 : 4;
@@ -89,6 +108,7 @@ struct LaunchArgs {
   const double* arc_theta;
   const PatchDev* patches;
   const double* patch_nodes;
+  const unsigned short* knn_tab;  // window tables of the patches (PatchDev::knn_off)
   int* queue;              // [0] chunk counter, [1] error word (both zeroed before launch)
   double* stats;           // n_items * kNumStats
   double* acc;             // stencil accumulators

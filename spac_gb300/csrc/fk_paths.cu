@@ -102,6 +102,9 @@ struct PatchSh {
   int side_first[4], side_count[4], side_axis[4];
   R side_fixed[4], side_start[4], side_inv_step[4];
   R e2;
+  const unsigned short* ktab;  // the patch's window table
+  int knn_base[4], knn_n[4];
+  R knn_u0[4];
 };
 
 // A chunk slot.  `ready` is written last, after the slot's contents.
@@ -165,6 +168,9 @@ __device__ void stage_stencil(const LaunchArgs& a, SlotSh<R>& sl, unsigned char*
       sl.sp.side_fixed[s] = R(P.side_fixed[s]);
       sl.sp.side_start[s] = R(P.side_start[s]);
       sl.sp.side_inv_step[s] = R(1.0 / P.side_step[s]);
+      sl.sp.knn_base[s] = P.knn_base[s];
+      sl.sp.knn_n[s] = P.knn_n[s];
+      sl.sp.knn_u0[s] = R(P.knn_u0[s]);
     }
     if (lane == 0) {
       sl.sp.m = P.m;
@@ -172,6 +178,7 @@ __device__ void stage_stencil(const LaunchArgs& a, SlotSh<R>& sl, unsigned char*
       sl.sp.closed = P.closed;
       sl.sp.walk = P.walk;
       sl.sp.e2 = R(P.eps2);
+      sl.sp.ktab = a.knn_tab + P.knn_off;
     }
   }
   if (ST == 1) {
@@ -229,19 +236,36 @@ __device__ __forceinline__ int knn_window(const PatchSh<R>& P, const R* __restri
     }
   }
   const int m = P.m, k = P.k;
-  int nearest = 0;
-  if (best_s >= 0) {
-    const R coord = P.side_axis[best_s] == 0 ? ex : ey;
-    int j = static_cast<int>(rint((coord - P.side_start[best_s]) * P.side_inv_step[best_s]));
-    j = max(0, min(P.side_count[best_s] - 1, j));
-    nearest = P.side_first[best_s] + j;
-  }
   auto d2 = [&](int idx) -> R {
     if (idx >= m) idx -= m;
     if (idx < 0) idx += m;
     const R dx = ex - nx[idx], dy = ey - ny[idx];
     return dx * dx + dy * dy;
   };
+  int nearest = 0;
+  if (best_s >= 0) {
+    const R coord = P.side_axis[best_s] == 0 ? ex : ey;
+    const R u = (coord - P.side_start[best_s]) * P.side_inv_step[best_s];
+    int j = static_cast<int>(rint(u));
+    j = max(0, min(P.side_count[best_s] - 1, j));
+    nearest = P.side_first[best_s] + j;
+    // the window table: L0 or L0 + 1, by the sliding search's own comparison
+    const int nb = P.knn_n[best_s];
+    if (nb > 0) {
+      int b = static_cast<int>(floor((u - P.knn_u0[best_s]) * R(kKnnBins)));
+      b = max(0, min(nb - 1, b));
+      const unsigned short e = __ldg(P.ktab + P.knn_base[best_s] + b);
+      if (!(e & kKnnFull)) {
+        int L = e;
+        const int up = L + k;  // the node that enters the window when it moves up
+        if (P.closed || up < m) {
+          if (d2(up) < d2(L)) L = (L + 1 == m) ? 0 : L + 1;
+        }
+        nearest_out = nearest;
+        return L;
+      }
+    }
+  }
   int L = nearest - k / 2;
   if (P.closed) {
     if (L < 0) L += m;
@@ -559,7 +583,6 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     unsigned n_dom = 0, n_cap = 0, n_done = 0;
     R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0;
     int k = 0;
-    uint32_t w2 = 0, w3 = 0;
     // every lane's first path of the chunk (chunk-local index); in warp mode
     // the warp owns the chunk and counts its paths in a register
     unsigned base = 0, wnext = 32u;
@@ -629,7 +652,13 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
               atomicAdd(&sacc[L * kk + j], static_cast<SAcc>(wv));
             return true;
           };
-          if (sp.walk && jn < kk) {
+          if (sp.walk == kWalkSpan && jn < kk) {
+#pragma unroll
+            for (int t = -kSpanMax; t <= kSpanMax; ++t) {
+              const int j = jn + t;
+              if (j >= 0 && j < kk) add(j);
+            }
+          } else if (sp.walk == kWalkStop && jn < kk) {
             for (int j = jn; j >= 0; --j)
               if (!add(j) && j < jn - 1) break;
             for (int j = jn + 1; j < kk; ++j)
@@ -694,14 +723,12 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
           co.Fx = -co.s * gx;
           co.Fy = -co.s * gy;
         }
-        uint32_t wa, wb;
-        if ((k & 1) == 0) {
-          const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k >> 1), ch.p0 + pl, item, a.stream), a.key0,
-                                   a.key1);
-          wa = r.x; wb = r.y; w2 = r.z; w3 = r.w;
-        } else {
-          wa = w2; wb = w3;
-        }
+        // one Philox block per step, counter (step, path, item, stream), words
+        // x and y: every lane computes a block at every step, so the warp
+        // stays converged (a block split over two steps put the lanes' step
+        // parities, and with them the Philox branch, out of step)
+        const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k), ch.p0 + pl, item, a.stream), a.key0, a.key1);
+        const uint32_t wa = r.x, wb = r.y;
         R z0, z1;
         box_muller(wa, wb, z0, z1);
         const R dWx = sqrth * z0, dWy = sqrth * z1;

@@ -4,7 +4,7 @@ path-weighted G row and B.
 
 On a 4 x 4 square-patch mesh in FP64, against the oracle's node solves on
 each round's Philox stream (item i, path p of the round with stream id s uses
-the counter (step/2, p, i, s), as one fk_assemble call does):
+the counter (step, p, i, s), as one fk_assemble call does):
  - after one round, G rows and B equal the oracle's for that round's paths;
  - after a second round (other path counts, some items given none), they
    equal the path-weighted combination of the two rounds' oracle solves,
