@@ -14,7 +14,7 @@ OUT = os.path.join(HERE, "_build")
 INC = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libspac_fk.so")
 
-CUDA_SOURCES = ["fk_paths.cu", "fk_kernels.cu", "fk_api.cu", "fk_mlp.cu", "fk_noalloc.cu", "fk_disk.cu"]
+CUDA_SOURCES = ["fk_paths.cu", "fk_paths_plain.cu", "fk_kernels.cu", "fk_api.cu", "fk_mlp.cu", "fk_noalloc.cu", "fk_disk.cu"]
 CXX_SOURCES = ["fk_mesh.cpp", "fk_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

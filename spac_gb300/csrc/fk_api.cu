@@ -138,6 +138,7 @@ struct fk_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double timing[3] = {0, 0, 0};
+  size_t acc_clean = 0;  // bytes at the start of w_acc known to be zero (left so by warp-mode fused launches)
   std::string err;
   std::vector<fk::BvpDev> bvps;
   fk::DBuf d_bvps;
@@ -328,7 +329,7 @@ int patch_span_bound(const fk::MeshStencil& M, double rcut) {
 }
 
 // The k-window start of a point on the patch boundary by the path kernel's
-// sliding search (knn_window in fk_paths.cu), in FP64.
+// sliding search (knn_window in fk_paths_kernel.cuh), in FP64.
 int knn_window_host(const fk::MeshStencil& M, int k, double ex, double ey) {
   const int m = static_cast<int>(M.nodes.size());
   int best_s = -1;
@@ -433,9 +434,12 @@ void add_patch(fk::StencilSet& S, const fk::MeshStencil& M, int k, double eps) {
   // always beyond the weight cutoff, a walk outward from the exit may stop
   // at its first cut node (0.9 W leaves a margin for rounding).
   const double W = 0.9 * std::min(M.rect[2] - M.rect[0], M.rect[3] - M.rect[1]);
-  p.walk = (p.eps2 * W * W >= static_cast<double>(fk::kPhiCut)) ? fk::kWalkStop : fk::kWalkFull;
-  if (p.walk == fk::kWalkStop && patch_span_bound(M, std::sqrt(static_cast<double>(fk::kPhiCut) / p.eps2)) <= fk::kSpanMax)
-    p.walk = fk::kWalkSpan;
+  auto walk_mode = [&](double cut, int span_max) {
+    if (p.eps2 * W * W < cut) return fk::kWalkFull;
+    return patch_span_bound(M, std::sqrt(cut / p.eps2)) <= span_max ? fk::kWalkSpan : fk::kWalkStop;
+  };
+  p.walk = walk_mode(static_cast<double>(fk::kPhiCut), fk::kSpanMax);
+  p.walk32 = walk_mode(static_cast<double>(fk::kPhiCut32), fk::kSpanMax32);
   p.node_off = static_cast<long long>(S.patch_nodes.size());
   p.ainv_off = S.ainv_total;
   S.ainv_total += static_cast<long long>(p.nwin) * k * k;
@@ -490,8 +494,10 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   int n_stencils = 0;
   if (S) n_stencils = static_cast<int>(S->kind == 1 ? S->arcs.size() : S->patches.size());
   const bool per_stencil = bvp.cv == FK_CV_MLP && n_stencils > 0 && ctx->mlps[bvp.mlp]->n_regions == n_stencils;
+  bool any_cv = false;  // some item has a control variate: the kernel build with the xi terms
   for (auto& x : it) {
     if (!multi_bvp) x.bvp = bvp_id;
+    if (x.bvp >= 0 && x.bvp < static_cast<int>(ctx->bvps.size()) && ctx->bvps[x.bvp].cv != FK_CV_NONE) any_cv = true;
     x.cv_region = (per_stencil && x.stencil >= 0) ? x.stencil : 0;
     x.acc_off = acc_total;
     if (kind != 0 && x.stencil >= 0) {
@@ -536,7 +542,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   if (round && warp_mode && !wms) warp_mode = false;  // (rounds need rows formed in the kernel)
   const size_t sacc_bytes = fk::paths_smem_bytes(precision, kind, acc_words, smem_nodes, warp_mode, lblock, wms);
   if (sacc_bytes > 200 * 1024) return fail(ctx, FK_ERR_CAPACITY, "stencil accumulators exceed shared memory");
-  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, bvp.cv, lblock, sacc_bytes, warp_mode);
+  const int occ = fk::paths_kernel_occupancy(bvp.problem, precision, kind, any_cv ? 1 : 0, lblock, sacc_bytes, warp_mode);
   const int grid = std::max(1, ctx->num_sms * occ);
   const int block_used = lblock;
   // Chunk size.  Slots: at least 4 chunks per CTA of the persistent grid, at
@@ -581,12 +587,30 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   for (const fk::ChunkDev& c : chunks)
     if (c.p0 != 0 || c.p1 != it[c.item].paths) { all_whole = false; break; }
   bool whole_items = !warp_mode && all_whole;
+  // Warp mode with FP32 patch stencils (k = 20, window corrections in FP32)
+  // and whole items into the CSR values: each warp forms its item's G row
+  // from the item's global moments and zeroes them again (wfuse).
+  bool wfuse = warp_mode && !wms && !round && precision == FK_FP32 && kind == 2 && all_whole && g_off && d_csr_idx &&
+               d_csr_val && !chunks.empty();
+  if (wfuse) {
+    for (const fk::PatchDev& P : S->patches) wfuse = wfuse && P.k == 20;
+    for (float e : S->emax) wfuse = wfuse && e < fk::kSplitMaxE;
+  }
+  const size_t acc_need = static_cast<size_t>(acc_total) * sizeof(double);
   if (round || wms) {
     whole_items = false;  // (the rows are formed in the kernel: no moment accumulators in global memory)
   } else {
-    FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_total * sizeof(double), 16)));
-    if (acc_total > 0 && !whole_items) FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_total * sizeof(double), s));
+    void* before = ctx->w_acc.p;
+    FK_CUDA(ctx->w_acc.ensure(std::max<size_t>(acc_need, 16)));
+    if (ctx->w_acc.p != before) ctx->acc_clean = 0;
+    if (acc_total > 0 && !whole_items && !(wfuse && ctx->acc_clean >= acc_need)) {
+      FK_CUDA(cudaMemsetAsync(ctx->w_acc.p, 0, acc_need, s));
+      ctx->acc_clean = std::max(ctx->acc_clean, acc_need);
+    }
   }
+  // (until this launch has finished without error, nothing is known to be zero)
+  const size_t acc_clean_after = wfuse ? ctx->acc_clean : 0;
+  if (!(round || wms)) ctx->acc_clean = 0;
   FK_CUDA(ctx->w_queue.ensure(16));
   FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));  // queue, error word, result flags
 
@@ -612,6 +636,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   a.max_steps = ctx->max_steps;
   a.wait_limit_ns = ctx->slot_wait_ns;
   a.cv = (bvp.cv == FK_CV_EXACT) ? 1 : 0;
+  a.any_cv = any_cv ? 1 : 0;
   if (bvp.cv == FK_CV_MLP) {
     const fk::Mlp& M = *ctx->mlps[bvp.mlp];
     if (M.table_grid < 2 || !M.d_table) return fail(ctx, FK_ERR_ARG, "learned control variate: build its table first");
@@ -630,8 +655,8 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   double* item_G = (kind && need_item_G) ? ctx->w_gout.as<double>() : nullptr;
   // G rows in the path kernel's flush: FP32 patch stencils whose chunks are
   // whole items and whose window corrections are small enough for FP32
-  const bool fuse = precision == FK_FP32 && kind == 2 && all_whole && (wms || !warp_mode) && g_off && d_csr_idx &&
-                    d_csr_val && !chunks.empty();
+  const bool fuse = (precision == FK_FP32 && kind == 2 && all_whole && (wms || !warp_mode) && g_off && d_csr_idx &&
+                     d_csr_val && !chunks.empty()) || wfuse;
   if (round && !(kind == 2 && g_off)) return fail(ctx, FK_ERR_ARG, "adaptive rounds need a square-patch mesh");
   if (fuse || round) {
     a.fuse_g = round ? 2 : 1;
@@ -725,6 +750,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
   if (q[3] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
   out.capped = q[2] != 0;
+  ctx->acc_clean = acc_clean_after;  // every warp zeroed the moments it used
   return FK_OK;
 }
 

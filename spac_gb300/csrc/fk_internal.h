@@ -39,7 +39,7 @@ struct PatchDev {
   double rect[4];
   double eps2;
   int m, k, closed, nwin;
-  int walk;             // kWalkFull, kWalkStop or kWalkSpan (how an exit visits its window's nodes)
+  int walk, walk32;     // kWalkFull, kWalkStop or kWalkSpan (how an exit visits its window's nodes), FP64 / FP32 cutoff
   long long node_off;   // 2*m doubles (x, y) in chain order
   long long ainv_off;   // nwin * k * k doubles, column-major per window
   // sides: chain index of the first node, node count, axis (0: node x varies),
@@ -68,16 +68,21 @@ enum { kStatScore = 0, kStatScore2, kStatXiAlias, kStatVR, kStatVR2, kStatXiScor
 // part padded to 16 bytes.
 constexpr int kSlotsFP32 = 3;
 
-// Gaussian stencil weights exp(-arg) with arg >= kPhiCut (< 1e-30) are not added.
+// Gaussian stencil weights exp(-arg) with arg >= kPhiCut (< 1e-30) are not
+// added; FP32 stepping drops them from arg >= kPhiCut32 (< 3.1e-8 = 2^-25,
+// below FP32 resolution next to the exit's own nearest weights, which are at
+// least exp(-(eps spacing / 2)^2): 0.105 at eps spacing = 3).
 constexpr float kPhiCut = 69.0f;
+constexpr float kPhiCut32 = 17.3f;
 // How an exit visits the nodes of its k-window (PatchDev::walk):
 //   kWalkFull  every node of the window;
 //   kWalkStop  outward from the exit's nearest node, each way until the first
 //              node beyond the weight cutoff;
-//   kWalkSpan  the nodes within kSpanMax chain places of the nearest node, a
-//              fixed unrolled range that holds every node within the cutoff.
+//   kWalkSpan  the nodes within kSpanMax (FP64 stepping) or kSpanMax32 (FP32)
+//              chain places of the nearest node, a fixed unrolled range that
+//              holds every node within the stepping precision's cutoff.
 constexpr int kWalkFull = 0, kWalkStop = 1, kWalkSpan = 2;
-constexpr int kSpanMax = 4;
+constexpr int kSpanMax = 4, kSpanMax32 = 2;
 // Window table of a patch side: the exit's k-window is L0 or L0 + 1 (the
 // latter iff node L0 + k is nearer than node L0); an entry with kKnnFull set
 // sends the exit to the sliding search.
@@ -88,12 +93,19 @@ __host__ __device__ inline size_t paths_slot_acc_bytes(int precision, int stenci
   const size_t w = (precision == 0 || stencil_kind == 1) ? 8 : 4;
   return (static_cast<size_t>(acc_words) * w + 15) & ~static_cast<size_t>(15);
 }
-__host__ __device__ inline size_t paths_slot_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes) {
+// The slot's stencil nodes (patch: x and y in the stepping precision; arc: angles).
+__host__ __device__ inline size_t paths_slot_nodes_bytes(int precision, int stencil_kind, int smem_nodes) {
   size_t nodes = 0;
   if (stencil_kind == 2) nodes = 2ull * smem_nodes * (precision == 0 ? 8 : 4);
   if (stencil_kind == 1) nodes = static_cast<size_t>(smem_nodes) * 8;
-  nodes = (nodes + 15) & ~static_cast<size_t>(15);
-  return paths_slot_acc_bytes(precision, stencil_kind, acc_words) + nodes;
+  return (nodes + 15) & ~static_cast<size_t>(15);
+}
+// Slot layout: moment accumulators, stencil nodes, and for patch stencils a
+// bit per window (the windows a warp-mode chunk's exits chose).
+__host__ __device__ inline size_t paths_slot_bytes(int precision, int stencil_kind, int acc_words, int smem_nodes) {
+  const size_t vis = stencil_kind == 2 ? ((4ull * ((smem_nodes + 31) / 32) + 15) & ~static_cast<size_t>(15)) : 0;
+  return paths_slot_acc_bytes(precision, stencil_kind, acc_words) + paths_slot_nodes_bytes(precision, stencil_kind, smem_nodes) +
+         vis;
 }
 
 struct LaunchArgs {
@@ -116,6 +128,7 @@ struct LaunchArgs {
   int max_steps;
   unsigned long long wait_limit_ns;  // slot waits give up after this (0: 60 s + 1 us x max_steps)
   int cv;                  // 0 none, 1 exact gradient functor, 2 learned (gradient table)
+  int any_cv;              // 1: some item of the launch has a control variate (else the build without xi)
   const float2* cv_tab;    // [regions][grid][grid] grad u_hat
   const double* cv_rect;   // 4 per region
   int cv_grid;
@@ -181,6 +194,8 @@ size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem
                         int block = 256, bool wm_shared = false);
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block,
                          size_t smem, cudaStream_t s, bool warp_mode = false);
+// FP32 path-kernel builds without the control-variate terms (fk_paths_plain.cu).
+const void* select_paths_plain(int problem, int st, bool warp_mode, bool four);
 int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem,
                            bool warp_mode = false);
 // host launchers (fk_kernels.cu)

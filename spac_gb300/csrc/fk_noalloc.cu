@@ -264,6 +264,7 @@ extern "C" int fk_solve_points_noalloc(const fk_bvp_desc* d, unsigned long long 
   a.stream = stream_id;
   a.max_steps = max_steps;
   a.cv = cvm;
+  a.any_cv = d->cv != FK_CV_NONE ? 1 : 0;
   a.stencil_kind = 0;
   if (launch_paths(a, d->problem, precision, grid, block, 0, s) != cudaSuccess) return FK_ERR_CUDA;
 
