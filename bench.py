@@ -438,6 +438,7 @@ def main():
         ctx.check(rc)
         e2e_t.append(time.perf_counter() - t0)
     e2e_step = float(np.mean(e2e_t))
+    windows = ctx.last_windows()  # stencil windows whose moments became G rows in the last assembly
     if dist:
         e2e_step = max_over_ranks(e2e_step, dist)
     # per call: one 96-byte item record and one 12-byte chunk record per item
@@ -455,7 +456,7 @@ def main():
     # roofline of the dominant kernel (the path kernel): algorithmic flops / its event time
     k_ms = float(np.mean([k[0] for k in kern]))
     f_ms = float(np.mean([k[1] for k in kern]))
-    steps_per_assembly, visited = _mean_steps(ctx, mesh, bvp, prec, paths)
+    steps_per_assembly = _mean_steps(ctx, mesh, bvp, prec, paths)
     flops = total_paths * steps_per_assembly * FLOPS_PER_STEP
     peaks, src = _peaks()
     smax = peaks.get("sm_max_mhz", 2070.0)
@@ -480,7 +481,7 @@ def main():
                 "fp64_stepping": fp64,
                 "kernels_ms": {"paths": k_ms, "finalize_scatter": f_ms},
                 "mean_steps_per_path": steps_per_assembly,
-                "roofline_scatter": _scatter_roofline(info, f_ms, peaks, src, visited),
+                "roofline_scatter": _scatter_roofline(info, f_ms, peaks, src, windows),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                              "frac": achieved / fp32_peak, "traffic": traffic,
                              "peak_source": f"nominal FP32: 152 SMs x 128 lanes x 2 flop x {smax:.0f} MHz "
@@ -490,7 +491,9 @@ def main():
                              # the path kernel is bound by instruction issue: ncu pipe figures of the
                              # committed capture of this kernel on this workload
                              "ncu_pipes": {k[len("paths_kernel_"):]: v for k, v in _read_profile_figures().items()
-                                           if k.startswith("paths_kernel_") and not k.endswith("per_launch")}},
+                                           if k.startswith("paths_kernel_") and
+                                           (k.endswith("_pipe") or k.endswith("issue_active"))},
+                             "issue": _issue_roofline(total_paths, steps_per_assembly, k_ms, smax)},
                 "clocks": clocks,
                 "time_to_1e-3": ttt,
                 "configs": cfgs,
@@ -842,32 +845,54 @@ def _cv_network(ctx, pxy, tgt, table):
 
 def _mean_steps(ctx, mesh, bvp, prec, paths):
     """Mean Euler steps per path of the workload (from the kernel's own
-    counters), and the stencil windows the exits chose (None: not counted)."""
+    counters, on a 2,000-path run of the same assembly)."""
     from spac_gb300 import fk
     st = (fk.Stats * ctx.mesh_info(mesh)["n_items"])()
     rc = ctx.L.fk_assemble(ctx.h, mesh, bvp, min(paths, 2000), None, CFG["h"], prec, None, None, None, None, st)
     ctx.check(rc)
     ms = np.array([s.mean_steps for s in st])
-    return float(ms.mean()), None
+    return float(ms.mean())
 
 
-def _scatter_roofline(info, f_ms, peaks, src, visited=None):
+def _scatter_roofline(info, f_ms, peaks, src, windows):
     """The G/B scatter of the 8x8 assembly.  It is fused into the path kernel:
     the last warp out of an item forms the item's G row from its moments in
     shared memory and adds it to the CSR values, so the window moments never
     reach DRAM and the scatter's time cannot be separated from the path
-    kernel's.  Algorithmic DRAM bytes (per row: its CSR entries written, 12 B
-    each with their column, and B, 12 B) against the path kernel's measured
-    DRAM traffic per launch; the finalize launch that remains writes only
-    statistics and B.  The standalone HBM-bound scatter is config 5's end pass
-    (configs.config5.gpu.end_pass)."""
+    kernel's.  Algorithmic DRAM bytes: per row its CSR entries written, 12 B
+    each with their column, and B, 12 B; the per-row figure that also counts
+    20 FP64 moments (160 B) per window the exits chose is given beside it,
+    with the window count the kernel reports (fk_last_windows).  Both against
+    the path kernel's DRAM traffic per launch in the committed capture; the
+    finalize launch that remains writes only statistics and B.  The standalone
+    HBM-bound scatter is config 5's end pass (configs.config5.gpu.end_pass)."""
     bytes_ = info["nnz"] * 12 + info["n_rows"] * 12
+    with_windows = bytes_ + 160 * windows
     traffic = _read_profile_figures().get("paths_kernel_dram_bytes_per_launch")
     return {"bound": "hbm", "fused_into": "paths_kernel", "algorithmic_bytes": bytes_, "traffic": traffic,
-            "traffic_over_algorithmic": traffic / bytes_ if traffic else None, "finalize_head_ms": f_ms,
-            "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+            "traffic_over_algorithmic": traffic / bytes_ if traffic else None,
+            "visited_windows": windows, "bytes_with_window_moments": with_windows,
+            "traffic_over_bytes_with_window_moments": traffic / with_windows if traffic else None,
+            "finalize_head_ms": f_ms, "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
             "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({src})",
             "note": "traffic: ncu dram bytes of one path-kernel launch (committed capture, slot mode, whole items)"}
+
+
+def _issue_roofline(total_paths, steps_per_path, k_ms, smax):
+    """The path kernel against its issue bound: its warp instructions (the
+    committed ncu fit, per path-step and per path, times this run's paths and
+    mean steps) over its event time, against one warp instruction per cycle
+    on each of the 4 x 152 schedulers at the maximum SM clock."""
+    figs = _read_profile_figures()
+    ips, ipp = figs.get("paths_kernel_warp_inst_per_step"), figs.get("paths_kernel_warp_inst_per_path")
+    if not (ips and ipp):
+        return None
+    inst = total_paths * (ipp + ips * steps_per_path)
+    achieved = inst / (k_ms / 1000.0) / 1e12
+    peak = 152 * 4 * smax * 1e6 / 1e12
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "T warp instructions/s", "frac": achieved / peak,
+            "warp_inst_per_step": ips, "warp_inst_per_path": ipp,
+            "source": "instruction counts: committed ncu fit over two step sizes (profiles/traffic.txt); time: this run"}
 
 
 def _read_profile_figures():

@@ -145,6 +145,11 @@ int fk_cuda_stream(const fk_ctx* ctx, void** stream);
 /* Device time (ms, CUDA events on the context stream) of the kernels of the
  * last solve: [0] path kernel, [1] finalize/scatter kernel, [2] launches. */
 int fk_last_timing(const fk_ctx* ctx, double out[3]);
+/* Stencil windows of the last patch-stencil solve whose moments were formed
+ * into G rows (summed over items and, in adaptive rounds, over chunks): the
+ * G/B scatter's work, 20 moments per window.  No reference counterpart (a
+ * measurement). */
+int fk_last_windows(const fk_ctx* ctx, long long* windows);
 
 /* ---- problem registry (BVP) ---------------------------------------------- */
 int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* desc, int* bvp_id);

@@ -138,7 +138,8 @@ struct fk_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double timing[3] = {0, 0, 0};
-  size_t acc_clean = 0;  // bytes at the start of w_acc known to be zero (left so by warp-mode fused launches)
+  size_t acc_clean = 0;
+  long long last_windows = 0;  // windows formed into G rows by the last solve (fk_last_windows)  // bytes at the start of w_acc known to be zero (left so by warp-mode fused launches)
   std::string err;
   std::vector<fk::BvpDev> bvps;
   fk::DBuf d_bvps;
@@ -611,8 +612,9 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   // (until this launch has finished without error, nothing is known to be zero)
   const size_t acc_clean_after = wfuse ? ctx->acc_clean : 0;
   if (!(round || wms)) ctx->acc_clean = 0;
-  FK_CUDA(ctx->w_queue.ensure(16));
-  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));  // queue, error word, result flags
+  FK_CUDA(ctx->w_queue.ensure(32));
+  // queue, error word, result flags, windows formed into rows
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 5 * sizeof(int), s));
 
   fk::LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -628,6 +630,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
     a.knn_tab = S->d_knn.as<unsigned short>();
   }
   a.queue = ctx->w_queue.as<int>();
+  a.vis_count = ctx->w_queue.as<int>() + 4;
   a.stats = ctx->w_stats.as<double>();
   a.acc = round ? nullptr : ctx->w_acc.as<double>();
   a.key0 = static_cast<uint32_t>(ctx->seed);
@@ -687,8 +690,9 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
     ctx->timing[1] = t1;
     ctx->timing[2] = chunks.empty() ? 1 : 2;
     ctx->stream_id++;
-    int q[4] = {0, 0, 0, 0};
+    int q[5] = {0, 0, 0, 0, 0};
     FK_CUDA(cudaMemcpy(q, ctx->w_queue.p, sizeof(q), cudaMemcpyDeviceToHost));
+    ctx->last_windows = q[4];
     if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
     if (q[3] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
     out.capped = q[2] != 0;
@@ -731,6 +735,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   f.row = d_row;
   f.B = d_B;
   f.flags = ctx->w_queue.as<int>() + 2;
+  f.vis_count = ctx->w_queue.as<int>() + 4;
   FK_CUDA(fk::launch_finalize(f, bvp.problem, s));
   FK_CUDA(cudaEventRecord(ctx->ev[2], s));
   FK_CUDA(cudaStreamSynchronize(s));
@@ -745,8 +750,9 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   out.item_B = f.item_B;
   out.item_stats = f.item_stats;
   // the kernels' own checks: slot waits, completed paths, capped paths
-  int q[4] = {0, 0, 0, 0};
+  int q[5] = {0, 0, 0, 0, 0};
   FK_CUDA(cudaMemcpy(q, ctx->w_queue.p, sizeof(q), cudaMemcpyDeviceToHost));
+  ctx->last_windows = q[4];
   if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
   if (q[3] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
   out.capped = q[2] != 0;
@@ -837,6 +843,12 @@ int fk_set_launch(fk_ctx* ctx, int block, int chunk) {
   return FK_OK;
 }
 int fk_cuda_stream(const fk_ctx* ctx, void** s) { if (!ctx || !s) return FK_ERR_ARG; *s = ctx->stream; return FK_OK; }
+int fk_last_windows(const fk_ctx* ctx, long long* windows) {
+  if (!ctx || !windows) return FK_ERR_ARG;
+  *windows = ctx->last_windows;
+  return FK_OK;
+}
+
 int fk_last_timing(const fk_ctx* ctx, double out[3]) {
   if (!ctx || !out) return FK_ERR_ARG;
   for (int i = 0; i < 3; ++i) out[i] = ctx->timing[i];

@@ -122,6 +122,7 @@ struct LaunchArgs {
   const double* patch_nodes;
   const unsigned short* knn_tab;  // window tables of the patches (PatchDev::knn_off)
   int* queue;              // [0] chunk counter, [1] error word (both zeroed before launch)
+  int* vis_count;          // may be null: += windows whose moments the kernel formed into G rows
   double* stats;           // n_items * kNumStats
   double* acc;             // stencil accumulators
   uint32_t key0, key1, stream;
@@ -179,6 +180,7 @@ struct FinalizeArgs {
   const int* row;           // item -> row (for B scatter)
   double* B;                // may be null
   int* flags;               // may be null: [0] |= an item had capped paths, [1] |= an item lost paths
+  int* vis_count;           // may be null: += windows whose moments the kernel formed into G rows
   int g_fused;              // 1: the path kernel already added the live items' G rows (LaunchArgs::fuse_g)
   // patch stencils: the largest nwin * k, m and the common k over the
   // launch's patches (fin_words = 0: the generic per-item path)

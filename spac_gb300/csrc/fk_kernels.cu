@@ -263,6 +263,11 @@ __global__ void __launch_bounds__(kPatchThreads, 4) finalize_patch_kernel(const 
     vis[W] = any != 0ull ? 1 : 0;
   }
   __syncthreads();
+  if (threadIdx.x == 0 && a.vis_count) {
+    int nvis = 0;
+    for (int W = 0; W < nwin; ++W) nvis += vis[W];
+    if (nvis) atomicAdd(a.vis_count, nvis);
+  }
   if (split)
     patch_window_pass<float, K>(a.patch_e32 + P.ainv_off, t32, vis, nwin, k, v32);
   else

@@ -316,6 +316,7 @@ __device__ bool fused_patch_row_fast(const LaunchArgs& a, const ItemDev& itg, in
   const int m = sp.m, k = sp.k, nwin = sp.closed ? m : m - k + 1;
   if (k != kFastK || !a.patch_e32) return false;
   const float* E = a.patch_e32 + a.patches[itg.stencil].ainv_off;
+  unsigned nvis = 0;
   for (int W = lane; W < nwin; W += 32) {
     float* t = sacc + W * kFastK;
     float tv[kFastK];
@@ -326,6 +327,7 @@ __device__ bool fused_patch_row_fast(const LaunchArgs& a, const ItemDev& itg, in
       vis |= tv[b] != 0.f;
     }
     if (!vis) continue;
+    ++nvis;
     const float4* Ew = reinterpret_cast<const float4*>(E + static_cast<long long>(W) * kFastK * kFastK);
     float v[kFastK];
 #pragma unroll
@@ -344,6 +346,8 @@ __device__ bool fused_patch_row_fast(const LaunchArgs& a, const ItemDev& itg, in
 #pragma unroll
     for (int r = 0; r < kFastK; ++r) t[r] = tv[r] + v[r];
   }
+  nvis = __reduce_add_sync(kFull, nvis);
+  if (lane == 0 && a.vis_count && nvis) atomicAdd(a.vis_count, static_cast<int>(nvis));
   __syncwarp();
   const long long goff = a.g_off[item];
   double ninv = 0.0;
@@ -395,6 +399,11 @@ __device__ void fused_patch_row_wm(const LaunchArgs& a, const ItemDev& itg, int 
   auto visited = [&](int W) { return ((wvis[W >> 5] >> (W & 31)) & 1u) != 0u; };
   __threadfence_block();
   __syncwarp();
+  if (lane == 0 && a.vis_count) {
+    int nvis = 0;
+    for (int i = 0; i < (nwin + 31) / 32; ++i) nvis += __popc(wvis[i]);
+    if (nvis) atomicAdd(a.vis_count, nvis);
+  }
   for (int W = lane; W < nwin; W += 32) {
     if (!visited(W)) continue;
     double* t = gacc + static_cast<long long>(W) * kFastK;
@@ -471,6 +480,7 @@ __device__ void fused_patch_row(const LaunchArgs& a, const ItemDev& itg, int ite
       for (int b = 0; b < k; ++b) vis |= t[b] != SAcc(0);
     }
     unsigned vm = __ballot_sync(kFull, vis);
+    if (lane == 0 && a.vis_count && vm) atomicAdd(a.vis_count, __popc(vm));
     while (vm) {
       const int W = W0 + __ffs(vm) - 1;
       vm &= vm - 1;

@@ -77,6 +77,7 @@ _SIGS = {
     "fk_set_wait_limits": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
     "fk_cuda_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "fk_last_timing": (C.c_int, [C.c_void_p, _dp]),
+    "fk_last_windows": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "fk_register_bvp": (C.c_int, [C.c_void_p, C.POINTER(BvpDesc), _ip]),
     "fk_solve_points": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _up, _dp, _ip, _dp, C.c_int,
                                   C.POINTER(Stats)]),
@@ -220,6 +221,12 @@ class Context:
         v = C.c_void_p()
         self.check(self.L.fk_cuda_stream(self.h, C.byref(v)))
         return v.value
+
+    def last_windows(self):
+        """Stencil windows whose moments the last patch-stencil solve formed into G rows."""
+        out = C.c_longlong()
+        self.check(self.L.fk_last_windows(self.h, C.byref(out)))
+        return int(out.value)
 
     def last_timing(self):
         out = (C.c_double * 3)()

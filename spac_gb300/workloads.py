@@ -2,7 +2,8 @@
 
   point_solves  32 x 32 grid nodes (i/33, j/33) of the Franke Poisson problem
                 on [0,1]^2, 1e4 paths per node, h = 1e-3 (FP64 and FP32)
-  assembly      square-patch G/B assembly (see bench.py for the 8 x 8 preset)
+  assembly      the plain 8 x 8 FP32 G/B assembly (bench.py's step) at --paths
+                per item (20000) and step --h (5e-4), three times
   uneven        16 independent disk BVPs, radius ~ U[0.25, 1], 2^14 nodes
                 (1024 per disk, uniform in area), paths log-uniform in
                 [1e3, 1e5], h in {1e-3, 5e-4}, one persistent launch with the
@@ -22,10 +23,11 @@
                 for interior circles, GMRES on the host, node error
 
   assembly_cv   the 8 x 8 assembly (eps = 1/spacing) with the learned control
-                variate at 870 paths per item, h = 5e-5: pilot, training,
-                refit, table and three assemblies
+                variate at --paths per item (734), step --h (5e-5): pilot,
+                training, refit, table and three assemblies
 
-  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows|serial_driver|robin|assembly_cv [--scale s]
+  python -m spac_gb300.workloads point_solves|uneven|large|disk_rows|serial_driver|robin|assembly|assembly_cv
+      [--scale s] [--paths n] [--h h]
 
 All inputs are seeded synthetic data; nothing is read from disk.
 """
@@ -206,6 +208,20 @@ def assembly_cv(ctx, paths=734, h=5e-5, eps_spacing=1.0, pilot_grid=24, pilot_pa
     return {"paths_per_item": paths, "h": h, "runs": out}
 
 
+def assembly(ctx, paths=20000, h=5e-4, eps_spacing=3.0, repeats=3):
+    """The plain 8 x 8 FP32 assembly (ANISO, 20-nearest Gaussian stencil) at
+    `paths` per item and step h, `repeats` times: path and statistics kernel
+    times and the mean steps per path (the item statistics of the last run)."""
+    mesh = ctx.mesh_square_patches((0, 0, 1, 1), 8, 31, 0.25, eps_spacing, 20)
+    b = ctx.register_bvp(fk.ANISO)
+    out = []
+    for i in range(repeats):
+        r, t = _sync_time(lambda: ctx.assemble(mesh, b, paths, h, fk.FP32, items=i == repeats - 1, item_G=False))
+        out.append({"seconds": t, "kernels_ms": ctx.last_timing()[:2]})
+    st = r["item_stats"]
+    return {"paths_per_item": paths, "h": h, "mean_steps": float(np.mean(st["mean_steps"])), "runs": out}
+
+
 def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_paths=256, max_rounds=6,
           max_paths=4_000_000, eps_spacing=3.0):
     """Adaptive assembly of the full CSR G/B: per item, paths until the
@@ -358,8 +374,10 @@ def serial_driver(ctx, paths=1000, h=1e-5, n_radial=43, precision=fk.FP64, repea
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("workload", choices=["point_solves", "uneven", "large", "disk_rows", "serial_driver", "robin",
-                                         "assembly_cv"])
+                                         "assembly_cv", "assembly"])
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--paths", type=int, default=0, help="assembly, assembly_cv: paths per item")
+    ap.add_argument("--h", type=float, default=0.0, help="assembly, assembly_cv: step size")
     ap.add_argument("--seed", type=int, default=2026)
     a = ap.parse_args()
     ctx = fk.Context(0, seed=a.seed)
@@ -372,7 +390,9 @@ def main():
     elif a.workload == "serial_driver":
         r = serial_driver(ctx, paths=max(16, int(1000 * a.scale)))
     elif a.workload == "assembly_cv":
-        r = assembly_cv(ctx, paths=max(32, int(870 * a.scale)))
+        r = assembly_cv(ctx, paths=a.paths or max(32, int(734 * a.scale)), h=a.h or 5e-5)
+    elif a.workload == "assembly":
+        r = assembly(ctx, paths=a.paths or max(32, int(20000 * a.scale)), h=a.h or 5e-4)
     elif a.workload == "robin":
         r = robin(ctx, paths=max(64, int(4000 * a.scale)))
     else:

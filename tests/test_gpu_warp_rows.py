@@ -5,6 +5,7 @@ so the next such launch needs no memset.
 
  - Warp mode against slot mode on the same Philox stream (the same paths,
    hence the same exits; only the order of the FP32 moment sums differs).
+   Both count the same stencil windows formed into rows (fk_last_windows).
  - A second warp-mode launch on the same stream gives the same system, also
    after an FP64 assembly (which leaves moments in the buffer) in between:
    nothing of one launch's moments reaches the next.
@@ -27,11 +28,15 @@ def test_warp_mode_rows_match_slot_mode(gpu, fk, eps_sp):
     b = gpu.register_bvp(fk.ANISO)
     paths, h = 300, 1e-3
     v_w, B_w, G_w = _assemble(gpu, fk, mesh, b, paths, h, fk.FP32, 41)
+    win_w = gpu.last_windows()
     gpu.set_launch(256, 1 << 20)  # one chunk per item in the shared slots
     try:
         v_s, B_s, G_s = _assemble(gpu, fk, mesh, b, paths, h, fk.FP32, 41)
+        win_s = gpu.last_windows()
     finally:
         gpu.set_launch(0, 0)
+    # the same exits choose the same windows (fk_last_windows: windows formed into rows)
+    assert win_s > 0 and abs(win_w - win_s) <= 1e-3 * win_s
     scale = np.abs(v_s).max()
     assert np.abs(v_w - v_s).max() <= 2e-6 * scale
     # (B_r sums items' estimates of both signs: compared on its overall scale;
