@@ -120,6 +120,8 @@ struct Mesh {
   // statistics on the device, paths and BVP per item on the host
   DBuf r_gsum, r_stats, r_var;
   std::vector<unsigned long long> r_paths;
+  std::vector<fk::ItemDev> r_items;  // the rounds' solve records (only paths and BVP change between rounds)
+  double r_items_h = 0.0;
   std::vector<int> r_bvp;
   double r_h = 0.0;
   bool r_active = false;
@@ -495,33 +497,33 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   int n_stencils = 0;
   if (S) n_stencils = static_cast<int>(S->kind == 1 ? S->arcs.size() : S->patches.size());
   const bool per_stencil = bvp.cv == FK_CV_MLP && n_stencils > 0 && ctx->mlps[bvp.mlp]->n_regions == n_stencils;
+  // one pass over the items: accumulator offsets, control variates, path
+  // totals, the largest stencil and the live items
   bool any_cv = false;  // some item has a control variate: the kernel build with the xi terms
+  long long total_paths = 0, n_live = 0;
+  int smem_nodes = 0;
+  const int n_bvps = static_cast<int>(ctx->bvps.size());
   for (auto& x : it) {
     if (!multi_bvp) x.bvp = bvp_id;
-    if (x.bvp >= 0 && x.bvp < static_cast<int>(ctx->bvps.size()) && ctx->bvps[x.bvp].cv != FK_CV_NONE) any_cv = true;
+    if (x.bvp >= 0 && x.bvp < n_bvps && ctx->bvps[x.bvp].cv != FK_CV_NONE) any_cv = true;
     x.cv_region = (per_stencil && x.stencil >= 0) ? x.stencil : 0;
     x.acc_off = acc_total;
     if (kind != 0 && x.stencil >= 0) {
       const long long w = S->acc_of(x.stencil);
       acc_total += w;
       acc_words = std::max<int>(acc_words, static_cast<int>(w));
+      smem_nodes = std::max(smem_nodes, S->size_of(x.stencil));
     }
+    if (!x.frontera) total_paths += x.paths;
+    if (!x.frontera && x.paths > 0) ++n_live;
   }
   // chunks: balance the persistent grid
-  long long total_paths = 0;
-  for (auto& x : it) if (!x.frontera) total_paths += x.paths;
   const int block = ctx->block;
-  int smem_nodes = 0;
-  if (kind != 0)
-    for (auto& x : it)
-      if (x.stencil >= 0) smem_nodes = std::max(smem_nodes, S->size_of(x.stencil));
   // Items of few paths (on average at most kWarpModeMaxPaths) run in warp
   // mode: every warp takes its own chunks and adds the stencil moments to
   // global memory, so an item's slowest path holds up one warp only.  A
   // launch shape set by the caller (fk_set_launch, the autotuner) keeps the
   // shared chunk slots.
-  long long n_live = 0;
-  for (auto& x : it) if (!x.frontera && x.paths > 0) ++n_live;
   bool warp_mode = ctx->chunk <= 0 && n_live > 0 && total_paths <= kWarpModeMaxPaths * n_live;
   // Adaptive rounds with items of few paths: warp mode with per-warp FP32
   // moment accumulators in shared memory, so that the kernel forms the G rows
@@ -1497,9 +1499,17 @@ int fk_assembly_round(fk_ctx* ctx, int mesh_id, int bvp_id, const int* bvp_of_it
     }
   }
   if (ctx->bvps.size() * sizeof(fk::BvpDev) > ctx->d_bvps.bytes) FK_CUDA(fk::upload(ctx->d_bvps, ctx->bvps, ctx->stream));
-  std::vector<unsigned long long> p(paths_per_item, paths_per_item + n);
-  std::vector<fk::ItemDev>& it = ctx->tmp_items;
-  mesh_items_dev(hm, it, h, p.data(), bv.data());
+  std::vector<fk::ItemDev>& it = M->r_items;
+  if (static_cast<int>(it.size()) != n || M->r_items_h != h) {
+    std::vector<unsigned long long> p(paths_per_item, paths_per_item + n);
+    mesh_items_dev(hm, it, h, p.data(), bv.data());
+    M->r_items_h = h;
+  } else {
+    for (int i = 0; i < n; ++i) {
+      it[i].paths = paths_per_item[i];
+      it[i].bvp = bv[i];
+    }
+  }
   RunOut ro;
   RunOpts o;
   o.multi_bvp = true;

@@ -448,18 +448,22 @@ class Context:
                                             var.ctypes.data_as(_dp) if want_var else None), allow)
         return var
 
-    def assembly_end(self, mesh, csr=True, items=True, item_G=True, allow=()):
+    def assembly_end(self, mesh, csr=True, items=True, item_G=True, allow=(), out=None):
+        """fk_assembly_end.  `out` may hold caller-owned output buffers (e.g.
+        page-locked): "val", "B", "item_B" (float64 arrays of the right sizes)
+        and "item_stats" (a ctypes Stats array of n_items)."""
         info = self.mesh_info(mesh)
-        val = np.zeros(info["nnz"]) if csr else None
-        B = np.zeros(info["n_rows"]) if csr else None
+        out = out or {}
+        val = (out["val"] if "val" in out else np.zeros(info["nnz"])) if csr else None
+        B = (out["B"] if "B" in out else np.zeros(info["n_rows"])) if csr else None
         G = iB = st = None
         if items:
             if item_G:
                 sizes = [len(self.mesh_stencil_nodes(mesh, s)) for s in range(info["n_stencils"])]
                 _, _, stn, _ = self.mesh_items(mesh)
                 G = np.zeros(int(sum(sizes[s] for s in stn)))
-            iB = np.zeros(info["n_items"])
-            st = (Stats * info["n_items"])()
+            iB = out["item_B"] if "item_B" in out else np.zeros(info["n_items"])
+            st = out["item_stats"] if "item_stats" in out else (Stats * info["n_items"])()
         self.check(self.L.fk_assembly_end(self.h, mesh, val.ctypes.data_as(_dp) if csr else None,
                                           B.ctypes.data_as(_dp) if csr else None,
                                           G.ctypes.data_as(_dp) if G is not None else None,
