@@ -637,6 +637,7 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   a.acc = round ? nullptr : ctx->w_acc.as<double>();
   a.key0 = static_cast<uint32_t>(ctx->seed);
   a.key1 = static_cast<uint32_t>(ctx->seed >> 32);
+  fk::set_round_keys(a);
   a.stream = ctx->stream_id;
   a.max_steps = ctx->max_steps;
   a.wait_limit_ns = ctx->slot_wait_ns;
@@ -1549,10 +1550,19 @@ int fk_assembly_end(fk_ctx* ctx, int mesh_id, double* val, double* B, double* it
     problem = ctx->bvps.empty() ? 0 : ctx->bvps[bv[i]].problem;
   }
   if (ctx->bvps.empty()) return fail(ctx, FK_ERR_REGISTRY, "no BVP registered");
-  std::vector<fk::ItemDev>& it = ctx->tmp_items;
-  mesh_items_dev(hm, it, M->r_h > 0 ? M->r_h : 1.0, M->r_paths.data(), bv.data());
   for (int i = 0; i < n; ++i)
     if (M->r_paths[i] > 0xffffffffull) return fail(ctx, FK_ERR_CAPACITY, "an item ran more than 2^32 - 1 paths");
+  // the rounds' solve records with the path totals (built afresh if no round ran)
+  std::vector<fk::ItemDev>& it = M->r_items;
+  if (static_cast<int>(it.size()) != n || !(M->r_h > 0) || M->r_items_h != M->r_h) {
+    mesh_items_dev(hm, it, M->r_h > 0 ? M->r_h : 1.0, M->r_paths.data(), bv.data());
+    M->r_items_h = M->r_h;
+  } else {
+    for (int i = 0; i < n; ++i) {
+      it[i].paths = static_cast<unsigned>(M->r_paths[i]);
+      it[i].bvp = bv[i];
+    }
+  }
   FK_CUDA(fk::upload_pinned(ctx->w_items, ctx->h_items, it, s));
   FK_CUDA(fk::upload_pinned(ctx->w_goff, ctx->h_goff, M->g_off, s));
   FK_CUDA(ctx->w_val.ensure(std::max<size_t>(hm.nnz * sizeof(double), 16)));

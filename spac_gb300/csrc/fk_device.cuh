@@ -16,14 +16,35 @@ constexpr double kGobet = -0.5826;  // Gobet-Menozzi shift, FeynmanKacSolver.cpp
 // ------------------------------------------------------------------ Philox ----
 // Philox4x32-10 (Salmon et al., SC'11).  Counter (step, path, item, stream),
 // key (seed lo, seed hi); the step's Box-Muller pair takes words x and y.
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u, kPhiloxM1 = 0xCD9E8D57u;  // round multipliers
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u, kPhiloxW1 = 0xBB67AE85u;  // key increments
+// Both words of the 64-bit product m c from one wide multiply.
+__device__ __forceinline__ void mul_hilo(uint32_t m, uint32_t c, uint32_t& hi, uint32_t& lo) {
+  const unsigned long long p = static_cast<unsigned long long>(m) * c;
+  hi = static_cast<uint32_t>(p >> 32);
+  lo = static_cast<uint32_t>(p);
+}
 __device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    uint32_t hi0, lo0, hi1, lo1;
+    mul_hilo(kPhiloxM0, c.x, hi0, lo0);
+    mul_hilo(kPhiloxM1, c.z, hi1, lo1);
     c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
+    k0 += kPhiloxW0;
+    k1 += kPhiloxW1;
+  }
+  return c;
+}
+// The same with the ten rounds' keys given (rk[2r], rk[2r + 1]): from a
+// kernel's parameters each key is an operand of the round's xor.
+__device__ __forceinline__ uint4 philox10_rk(uint4 c, const uint32_t* rk) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mul_hilo(kPhiloxM0, c.x, hi0, lo0);
+    mul_hilo(kPhiloxM1, c.z, hi1, lo1);
+    c = make_uint4(hi1 ^ c.y ^ rk[2 * r], lo1, hi0 ^ c.w ^ rk[2 * r + 1], lo0);
   }
   return c;
 }
@@ -44,6 +65,12 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& z0, d
 // Carlo error of any node estimate.  FP64 stepping keeps the correctly
 // rounded forms (it follows the oracle's paths).
 __device__ __forceinline__ float fexp(float v) { return __expf(v); }
+// 2^v (ex2.approx: the SFU's base-2 exponential)
+__device__ __forceinline__ float fexp2(float v) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
 __device__ __forceinline__ double fexp(double v) { return exp(v); }
 __device__ __forceinline__ float fsqrt(float v) {
   float r;
@@ -203,7 +230,8 @@ struct StepCoef {
 // evaluated once (BVPs/Franke_Poisson.hpp:4-60).
 template <typename R>
 struct FrankeEval {
-  R e1, e2, e3, e4, a, b, c, d, p, q, r, t;  // t unused
+  R e1, e2, e3, e4, a, b, c, d, p, q, r, t;
+  R s1, s3, s4;  // a^2 + b^2, p^2 + q^2, r^2 + t^2 (the exponents' sums, reused by lap)
   __device__ __forceinline__ FrankeEval(R x, R y) {
     a = R(9) * x - R(2);
     b = R(9) * y - R(2);
@@ -213,10 +241,29 @@ struct FrankeEval {
     q = R(9) * y - R(3);
     r = R(9) * x - R(4);
     t = R(9) * y - R(7);
-    e1 = fexp(R(-0.25) * (a * a + b * b));
-    e2 = fexp(R(-1.0 / 49.0) * (c * c) - R(0.1) * d);
-    e3 = fexp(R(-0.25) * (p * p + q * q));
-    e4 = fexp(R(-1) * (r * r + t * t));
+    s1 = a * a + b * b;
+    s3 = p * p + q * q;
+    s4 = r * r + t * t;
+    if constexpr (std::is_same<R, float>::value) {
+      // 2^(log2(e) v): the log2(e) scale folded into each exponent's constants
+      constexpr float L2E = 1.44269504088896340736f;
+      e1 = fexp2(-0.25f * L2E * s1);
+      e2 = fexp2((-1.0f / 49.0f * L2E) * (c * c) - 0.1f * L2E * d);
+      e3 = fexp2(-0.25f * L2E * s3);
+      e4 = fexp2(-L2E * s4);
+    } else {
+      e1 = fexp(R(-0.25) * s1);
+      e2 = fexp(R(-1.0 / 49.0) * (c * c) - R(0.1) * d);
+      e3 = fexp(R(-0.25) * s3);
+      e4 = fexp(R(-1) * s4);
+    }
+  }
+  // uxx + uyy with each exponential's two second derivatives combined:
+  // -3.375 (18 - 4.5 s1) e1 + (-(27/98)(9 - (18/49) c^2) + 243/400) e2
+  // - 2.25 (18 - 4.5 s3) e3 + 3.6 (18 - 18 s4) e4
+  __device__ __forceinline__ R lap() const {
+    return (R(15.1875) * s1 - R(60.75)) * e1 + (R(27.0 * 18.0 / (98.0 * 49.0)) * (c * c) - R(243.0 / 98.0 - 243.0 / 400.0)) * e2 +
+           (R(10.125) * s3 - R(40.5)) * e3 + (R(64.8) - R(64.8) * s4) * e4;
   }
   __device__ __forceinline__ R u() const { return R(0.75) * e1 + R(0.75) * e2 + R(0.5) * e3 - R(0.2) * e4; }
   __device__ __forceinline__ R ux() const {
@@ -286,7 +333,7 @@ struct Problem<0> {
   __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
     FrankeEval<R> F(x, y);
     o.s = R(1.41421356237);
-    o.f = -F.uxx() - F.uyy();
+    o.f = -F.lap();
     o.c = R(0);
     o.bx = R(0);
     o.by = R(0);
@@ -341,7 +388,7 @@ struct Problem<2> {
     const R Fv = F.u(), Fx = F.ux(), Fy = F.uy();
     const R u = Fv * q;
     const R ux = Fx * q + Fv * y, uy = Fy * q + Fv * x;
-    const R lap = (F.uxx() + F.uyy()) * q + R(2) * (Fx * y + Fy * x);
+    const R lap = F.lap() * q + R(2) * (Fx * y + Fy * x);
     o.s = fsqrt(R(2) * a);
     o.c = -(R(1) + x * x + y * y);
     o.bx = y - R(0.5);
@@ -369,7 +416,7 @@ struct Problem<3> {
     const R xi = (x - R(b.prob[0])) * inv + R(0.5), eta = (y - R(b.prob[1])) * inv + R(0.5);
     FrankeEval<R> F(xi, eta);
     o.s = R(1.41421356237);
-    o.f = -(F.uxx() + F.uyy()) * (inv * inv);
+    o.f = -F.lap() * (inv * inv);
     o.c = R(0);
     o.bx = R(0);
     o.by = R(0);

@@ -126,6 +126,7 @@ struct LaunchArgs {
   double* stats;           // n_items * kNumStats
   double* acc;             // stencil accumulators
   uint32_t key0, key1, stream;
+  uint32_t rkey[20];        // Philox round keys from (key0, key1): set_round_keys
   int max_steps;
   unsigned long long wait_limit_ns;  // slot waits give up after this (0: 60 s + 1 us x max_steps)
   int cv;                  // 0 none, 1 exact gradient functor, 2 learned (gradient table)
@@ -153,6 +154,18 @@ struct LaunchArgs {
   double* csr_val;
   double* item_G;          // may be null
 };
+// The ten Philox4x32-10 round keys of a launch's seed key (key0, key1):
+// round r uses (key0 + r 0x9E3779B9, key1 + r 0xBB67AE85) mod 2^32.
+inline void set_round_keys(LaunchArgs& a) {
+  uint32_t k0 = a.key0, k1 = a.key1;
+  for (int r = 0; r < 10; ++r) {
+    a.rkey[2 * r] = k0;
+    a.rkey[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
 
 struct FinalizeArgs {
   const BvpDev* bvp;

@@ -261,6 +261,7 @@ extern "C" int fk_solve_points_noalloc(const fk_bvp_desc* d, unsigned long long 
   a.stats = d_stats;
   a.key0 = static_cast<uint32_t>(seed);
   a.key1 = static_cast<uint32_t>(seed >> 32);
+  set_round_keys(a);
   a.stream = stream_id;
   a.max_steps = max_steps;
   a.cv = cvm;

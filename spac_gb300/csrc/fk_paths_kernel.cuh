@@ -830,7 +830,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         // x and y: every lane computes a block at every step, so the warp
         // stays converged (a block split over two steps put the lanes' step
         // parities, and with them the Philox branch, out of step)
-        const uint4 r = philox10(make_uint4(static_cast<uint32_t>(k), ch.p0 + pl, item, a.stream), a.key0, a.key1);
+        const uint4 r = philox10_rk(make_uint4(static_cast<uint32_t>(k), ch.p0 + pl, item, a.stream), a.rkey);
         const uint32_t wa = r.x, wb = r.y;
         R z0, z1;
         box_muller(wa, wb, z0, z1);
@@ -856,8 +856,8 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
               const R dq = q == 0 ? d0 - x : (q == 1 ? d1 - y : (q == 2 ? x - d2 : y - d3));
               if (!(dq > -rho)) continue;
               if (!drawn) {
-                re = philox10(make_uint4(0x80000000u | static_cast<uint32_t>(k), ch.p0 + pl, item, a.stream), a.key0,
-                              a.key1);
+                re = philox10_rk(make_uint4(0x80000000u | static_cast<uint32_t>(k), ch.p0 + pl, item, a.stream),
+                                 a.rkey);
                 drawn = true;
               }
               const R E = exp1_draw(q == 0 ? re.x : (q == 1 ? re.y : (q == 2 ? re.z : re.w)), R(0));
