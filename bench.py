@@ -664,7 +664,7 @@ def time_to_target_all(ctx, target=1e-3):
     return res
 
 
-def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=300, pilot_h=1e-3, train_steps=20,
+def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=300, pilot_h=1e-3, train_steps=10,
                    table=128, lr=1e-2, batch=4096, fit_output=True, n_cal=4000, only=None, gmres=True,
                    rep_streams=(7101, 7102)):
     """Time to `target` RMS row residual of the assembled system, plain FK vs

@@ -121,6 +121,7 @@ struct Mesh {
   DBuf r_gsum, r_stats, r_var;
   std::vector<unsigned long long> r_paths;
   std::vector<fk::ItemDev> r_items;  // the rounds' solve records (only paths and BVP change between rounds)
+  std::vector<fk::ItemDev> a_items;  // fk_assemble's solve records (only h and paths change between calls)
   double r_items_h = 0.0;
   std::vector<int> r_bvp;
   double r_h = 0.0;
@@ -152,7 +153,7 @@ struct fk_ctx {
   fk::DBuf w_items, w_chunks, w_stats, w_acc, w_queue, w_gout, w_bout, w_sout, w_val, w_B, w_goff, w_row, w_tmp;
   fk::DBuf w_dgrid, w_dcbar, w_dvar, w_dminv, w_dz, w_dG, w_dB, w_dflags;
   fk::DiskBufs w_disk;
-  fk::HBuf h_items, h_chunks, h_goff, h_stats;  // pinned staging of the per-call transfers
+  fk::HBuf h_items, h_chunks, h_goff, h_stats, h_queue;  // pinned staging of the per-call transfers
   std::vector<fk::ItemDev> tmp_items;            // host scratch kept across calls
   std::vector<fk::ChunkDev> tmp_chunks;
 };
@@ -467,6 +468,7 @@ struct RunOpts {
   double* g_sum = nullptr;
   double* run_stats = nullptr;
   double* item_var = nullptr;
+  bool defer = false;  // queue the launch and leave the stream synchronisation and the checks to finish_run
 };
 
 // Runs items through the path kernel and the finalize kernel.
@@ -475,7 +477,42 @@ struct RunOut {
   double* item_B = nullptr;
   double* item_stats = nullptr;
   bool capped = false;
+  // RunOpts::defer: the launch is queued with its check words copied to
+  // pinned memory; finish_run, after the caller's own stream synchronisation,
+  // reads them (one synchronisation for the whole call)
+  bool deferred = false;
+  int kernels = 0;
+  size_t acc_clean_after = 0;
 };
+
+// The completed-paths check failed: the first item the finalize kernel
+// found (q[5] - 1) and the paths it completed (q[6]).
+int fail_lost(fk_ctx* ctx, const int* q) {
+  char msg[160];
+  std::snprintf(msg, sizeof(msg), "path kernel: an item completed a different number of paths than requested "
+                "(item %d: %d completed)", q[5] - 1, q[6]);
+  return fail(ctx, FK_ERR_CUDA, msg);
+}
+
+// The kernels' own checks of a queued launch (slot waits, completed paths,
+// capped paths) and its timing, once its stream has drained.
+int finish_run(fk_ctx* ctx, RunOut& out) {
+  if (!out.deferred) return FK_OK;
+  out.deferred = false;
+  float t0 = 0, t1 = 0;
+  cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[2]);
+  ctx->timing[0] = t0;
+  ctx->timing[1] = t1;
+  ctx->timing[2] = out.kernels;
+  const int* q = static_cast<const int*>(ctx->h_queue.p);
+  ctx->last_windows = q[4];
+  if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
+  if (q[3] != 0) return fail_lost(ctx, q);
+  out.capped = q[2] != 0;
+  ctx->acc_clean = out.acc_clean_after;  // every warp zeroed the moments it used
+  return FK_OK;
+}
 
 int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& it, fk::StencilSet* S,
               const std::vector<long long>* g_off, long long g_total, const int* d_csr_idx, double* d_csr_val,
@@ -615,8 +652,9 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   const size_t acc_clean_after = wfuse ? ctx->acc_clean : 0;
   if (!(round || wms)) ctx->acc_clean = 0;
   FK_CUDA(ctx->w_queue.ensure(32));
-  // queue, error word, result flags, windows formed into rows
-  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 5 * sizeof(int), s));
+  // queue, error word, result flags, windows formed into rows, the first item
+  // whose completed path count differs and that count
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 7 * sizeof(int), s));
 
   fk::LaunchArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -739,8 +777,21 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   f.B = d_B;
   f.flags = ctx->w_queue.as<int>() + 2;
   f.vis_count = ctx->w_queue.as<int>() + 4;
+  f.lost = ctx->w_queue.as<int>() + 5;
   FK_CUDA(fk::launch_finalize(f, bvp.problem, s));
   FK_CUDA(cudaEventRecord(ctx->ev[2], s));
+  out.item_G = kind ? ctx->w_gout.as<double>() : nullptr;
+  out.item_B = f.item_B;
+  out.item_stats = f.item_stats;
+  if (o.defer) {
+    FK_CUDA(ctx->h_queue.ensure(32));
+    FK_CUDA(cudaMemcpyAsync(ctx->h_queue.p, ctx->w_queue.p, 7 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    out.deferred = true;
+    out.kernels = chunks.empty() ? 1 : 2;
+    out.acc_clean_after = acc_clean_after;
+    ctx->stream_id++;
+    return FK_OK;
+  }
   FK_CUDA(cudaStreamSynchronize(s));
   float t0 = 0, t1 = 0;
   cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[1]);
@@ -749,15 +800,12 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   ctx->timing[1] = t1;
   ctx->timing[2] = chunks.empty() ? 1 : 2;
   ctx->stream_id++;
-  out.item_G = kind ? ctx->w_gout.as<double>() : nullptr;
-  out.item_B = f.item_B;
-  out.item_stats = f.item_stats;
   // the kernels' own checks: slot waits, completed paths, capped paths
-  int q[5] = {0, 0, 0, 0, 0};
+  int q[7] = {0, 0, 0, 0, 0, 0, 0};
   FK_CUDA(cudaMemcpy(q, ctx->w_queue.p, sizeof(q), cudaMemcpyDeviceToHost));
   ctx->last_windows = q[4];
   if (q[1] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: a wait for a chunk slot timed out");
-  if (q[3] != 0) return fail(ctx, FK_ERR_CUDA, "path kernel: an item completed fewer paths than requested");
+  if (q[3] != 0) return fail_lost(ctx, q);
   out.capped = q[2] != 0;
   ctx->acc_clean = acc_clean_after;  // every warp zeroed the moments it used
   return FK_OK;
@@ -1386,18 +1434,27 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   if ((rc = upload_mesh(ctx, M))) return rc;
   const fk::HostMesh& hm = M->host;
   const int n = static_cast<int>(hm.items.size());
-  std::vector<fk::ItemDev>& it = ctx->tmp_items;
-  it.resize(n);
+  // the mesh's solve records (kept across calls: only h and the path counts change)
+  std::vector<fk::ItemDev>& it = M->a_items;
+  if (static_cast<int>(it.size()) != n) {
+    it.resize(n);
+    for (int i = 0; i < n; ++i) {
+      const fk::MeshItem& q = hm.items[i];
+      fk::ItemDev& d = it[i];
+      std::memset(&d, 0, sizeof(d));
+      d.x = q.x; d.y = q.y;
+      d.stencil = q.stencil; d.frontera = q.frontera ? 1 : 0;
+      const fk::MeshStencil& S = hm.stencils[q.stencil];
+      if (hm.kind == 1) { d.sub_shape = FK_SHAPE_CIRCLE; d.sub[0] = S.radius; d.sub[1] = S.cx; d.sub[2] = S.cy; }
+      else { d.sub_shape = FK_SHAPE_RECT; for (int k = 0; k < 4; ++k) d.sub[k] = S.rect[k]; }
+    }
+  }
+  const double sqrth = std::sqrt(h);
   for (int i = 0; i < n; ++i) {
-    const fk::MeshItem& q = hm.items[i];
     fk::ItemDev& d = it[i];
-    std::memset(&d, 0, sizeof(d));
-    d.x = q.x; d.y = q.y; d.h = h; d.sqrth = std::sqrt(h);
+    d.h = h;
+    d.sqrth = sqrth;
     d.paths = paths_per_item ? paths_per_item[i] : paths;
-    d.stencil = q.stencil; d.frontera = q.frontera ? 1 : 0;
-    const fk::MeshStencil& S = hm.stencils[q.stencil];
-    if (hm.kind == 1) { d.sub_shape = FK_SHAPE_CIRCLE; d.sub[0] = S.radius; d.sub[1] = S.cx; d.sub[2] = S.cy; }
-    else { d.sub_shape = FK_SHAPE_RECT; for (int k = 0; k < 4; ++k) d.sub[k] = S.rect[k]; }
   }
   cudaStream_t s = ctx->stream;
   FK_CUDA(ctx->w_val.ensure(std::max<size_t>(hm.nnz * sizeof(double), 16)));
@@ -1407,6 +1464,7 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
   RunOut ro;
   RunOpts asm_opts;
   asm_opts.need_item_G = item_G != nullptr;
+  asm_opts.defer = !(M->disk_radial > 0 && !M->disk.disks.empty());  // (the disk rows run their own launches)
   rc = run_items(ctx, bvp_id, precision, it, &M->st, &M->g_off, M->g_total, M->d_csr_idx.as<int>(),
                  ctx->w_val.as<double>(), M->d_row.as<int>(), ctx->w_B.as<double>(), ro, asm_opts);
   if (rc) return rc;
@@ -1423,6 +1481,7 @@ int fk_assemble(fk_ctx* ctx, int mesh_id, int bvp_id, unsigned paths, const unsi
     if ((rc = read_stats(ctx, ro.item_stats, n, item_stats))) return rc;
   }
   FK_CUDA(cudaStreamSynchronize(s));
+  if ((rc = finish_run(ctx, ro))) return rc;
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
   return FK_OK;
 }

@@ -193,6 +193,7 @@ struct FinalizeArgs {
   const int* row;           // item -> row (for B scatter)
   double* B;                // may be null
   int* flags;               // may be null: [0] |= an item had capped paths, [1] |= an item lost paths
+  int* lost;                // may be null: [0] = 1 + the first item whose completed paths differ, [1] = their count
   int* vis_count;           // may be null: += windows whose moments the kernel formed into G rows
   int g_fused;              // 1: the path kernel already added the live items' G rows (LaunchArgs::fuse_g)
   // patch stencils: the largest nwin * k, m and the common k over the

@@ -51,7 +51,10 @@ __device__ __forceinline__ void finalize_item_head(const FinalizeArgs& a, int it
   if (a.B) atomicAdd(&a.B[a.row[item]], Bv);
   if (a.flags && live) {
     if (S[kStatCap] > 0.0) atomicOr(&a.flags[0], 1);
-    if (S[kStatPaths] != N) atomicOr(&a.flags[1], 1);  // every requested path must have completed
+    if (S[kStatPaths] != N) {  // every requested path must have completed, once
+      atomicOr(&a.flags[1], 1);
+      if (a.lost && atomicCAS(&a.lost[0], 0, item + 1) == 0) a.lost[1] = static_cast<int>(S[kStatPaths]);
+    }
   }
 }
 

@@ -204,7 +204,7 @@ def learned_cv(ctx, problem, pxy, target, steps=50, lr=1e-2, table=256, seed=99)
     return ctx.register_bvp(problem, cv=fk.CV_MLP, mlp_id=mid)
 
 
-def assembly_cv(ctx, paths=734, h=5e-5, eps_spacing=1.0, pilot_grid=24, pilot_paths=300, pilot_h=1e-3, steps=20,
+def assembly_cv(ctx, paths=734, h=5e-5, eps_spacing=1.0, pilot_grid=24, pilot_paths=300, pilot_h=1e-3, steps=10,
                 lr=1e-2, table=128, repeats=3):
     """The 8 x 8 assembly with the learned control variate (the metric's CV
     arm at a fixed path count): pilot point solves, training, output refit,
