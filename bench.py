@@ -666,7 +666,7 @@ def time_to_target_all(ctx, target=1e-3):
 
 def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=300, pilot_h=1e-3, train_steps=10,
                    table=128, lr=1e-2, batch=4096, fit_output=True, n_cal=4000, only=None, gmres=True,
-                   rep_streams=(7101, 7102)):
+                   rep_streams=(7101, 7102), pilot_max_steps=0):
     """Time to `target` RMS row residual of the assembled system, plain FK vs
     the learned control variate (both FP32 stepping, same h, same paths for
     every item).
@@ -730,7 +730,13 @@ def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=30
         pxy = np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2)  # x outer, y inner
         # the pilot only has to approximate u (any u_hat keeps the estimator
         # unbiased), so it runs at the coarse step pilot_h
-        pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec)
+        if pilot_max_steps:
+            # the pilot's paths stop after pilot_max_steps (a stopped path is
+            # scored at its nearest boundary point): the pilot only shapes u_hat
+            ctx.set_max_steps(pilot_max_steps)
+        pst = ctx.solve_points(b_plain, pxy, pilot_paths, pilot_h, prec, allow=(fk.FK_ERR_STEP_CAP,))
+        if pilot_max_steps:
+            ctx.set_max_steps(1 << 24)
         t_pilot = time.perf_counter() - t0
         pilot_kernel_ms = ctx.last_timing()[0]
         tgt = np.ascontiguousarray(pst["phi"])

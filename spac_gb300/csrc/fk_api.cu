@@ -981,9 +981,12 @@ int fk_solve_points(fk_ctx* ctx, int bvp_id, int n, const double* xy, const unsi
     if (it.sub_shape > 1) return fail(ctx, FK_ERR_ARG, "unknown subdomain shape");
   }
   RunOut ro;
-  rc = run_items(ctx, bvp_id, precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro);
+  RunOpts o;
+  o.defer = true;  // one stream synchronisation: read_stats's
+  rc = run_items(ctx, bvp_id, precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro, o);
   if (rc) return rc;
   if ((rc = read_stats(ctx, ro.item_stats, n, out))) return rc;
+  if ((rc = finish_run(ctx, ro))) return rc;
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
   return FK_OK;
 }
@@ -1022,9 +1025,11 @@ int fk_solve_points_multi(fk_ctx* ctx, int n, const int* bvp_ids, const double* 
   RunOut ro;
   RunOpts opts;
   opts.multi_bvp = true;
+  opts.defer = true;  // one stream synchronisation: read_stats's
   rc = run_items(ctx, bvp_ids[0], precision, items, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, ro, opts);
   if (rc) return rc;
   if ((rc = read_stats(ctx, ro.item_stats, n, out))) return rc;
+  if ((rc = finish_run(ctx, ro))) return rc;
   if (ro.capped) return fail(ctx, FK_ERR_STEP_CAP, "paths reached max_steps");
   return FK_OK;
 }
