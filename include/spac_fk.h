@@ -241,6 +241,17 @@ int fk_mesh_nodes(fk_ctx* ctx, int mesh_id, double* xy, int* flags);
 int fk_mesh_items(fk_ctx* ctx, int mesh_id, int* row, double* xy, int* stencil, int* frontera);
 /* stencil s: node ids (global rows) of its nodes, count returned in *n */
 int fk_mesh_stencil_nodes(fk_ctx* ctx, int mesh_id, int s, int* gids, int* n);
+/* The k-window of the Gaussian exit stencil that the path kernel picks for a
+ * point (x, y) on the boundary of patch s of a square-patch mesh: the
+ * window's first chain node (*window; the window is k consecutive chain
+ * nodes, modulo the chain length on a closed patch), the point's nearest
+ * node on its side (*nearest), and how an exit there visits the window's
+ * nodes (*walk: bits 0-1 FP32 stepping, bits 2-3 FP64; 0 every node, 1 outward
+ * from the nearest node to the first node beyond the weight cutoff, 2 a fixed
+ * range of +-2 (FP32) or +-4 (FP64) chain places around it).  Evaluated on
+ * the host in FP64 with the kernel's window table.  Introspection of the
+ * stencil; no reference counterpart. */
+int fk_mesh_window(fk_ctx* ctx, int mesh_id, int s, double x, double y, int* window, int* nearest, int* walk);
 /* SistemaLineal::Inicializa_CSR (Mesh/SistemaLineal.cpp:39-66): sorted CSR
  * pattern, diagonal = number of containing patches, placeholder 1e-23. */
 int fk_mesh_csr(fk_ctx* ctx, int mesh_id, int* rowptr, int* col, double* val0);

@@ -1345,6 +1345,54 @@ int fk_mesh_stencil_nodes(fk_ctx* ctx, int mesh_id, int s, int* gids, int* n) {
   return FK_OK;
 }
 
+int fk_mesh_window(fk_ctx* ctx, int mesh_id, int s, double x, double y, int* window, int* nearest, int* walk) {
+  fk::Mesh* M = get_mesh(ctx, mesh_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");
+  if (M->host.kind != 2) return fail(ctx, FK_ERR_ARG, "not a square-patch mesh");
+  if (s < 0 || s >= static_cast<int>(M->st.patches.size())) return fail(ctx, FK_ERR_REGISTRY, "unknown stencil");
+  if (!window || !nearest || !walk) return fail(ctx, FK_ERR_ARG, "null argument");
+  const fk::PatchDev& P = M->st.patches[s];
+  const fk::MeshStencil& MS = M->host.stencils[s];
+  const int m = P.m, k = P.k;
+  *walk = (P.walk32 & 3) | ((P.walk & 3) << 2);
+  // the kernel's knn_window, in FP64: the side nearest to the point ...
+  int best_s = -1;
+  double best = 1e300;
+  for (int q = 0; q < 4; ++q) {
+    if (P.side_count[q] > 0) {
+      const double dist = std::fabs((P.side_axis[q] == 0 ? y : x) - P.side_fixed[q]);
+      if (dist < best) { best = dist; best_s = q; }
+    }
+  }
+  if (best_s < 0) return fail(ctx, FK_ERR_ARG, "patch without sides");
+  const double u = ((P.side_axis[best_s] == 0 ? x : y) - P.side_start[best_s]) * (1.0 / P.side_step[best_s]);
+  int j = static_cast<int>(std::rint(u));
+  j = std::max(0, std::min(P.side_count[best_s] - 1, j));
+  *nearest = P.side_first[best_s] + j;
+  // ... then its window-table bin and the one comparison
+  if (P.knn_n[best_s] > 0) {
+    int b = static_cast<int>(std::floor((u - P.knn_u0[best_s]) * fk::kKnnBins));
+    b = std::max(0, std::min(P.knn_n[best_s] - 1, b));
+    const unsigned short t = M->st.knn_tab[P.knn_off + P.knn_base[best_s] + b];
+    if (!(t & fk::kKnnFull)) {
+      int L = t;
+      const int up = L + k;
+      if (P.closed || up < m) {
+        auto d2 = [&](int idx) {
+          if (idx >= m) idx -= m;
+          const double dx = x - MS.nodes[idx].x, dy = y - MS.nodes[idx].y;
+          return dx * dx + dy * dy;
+        };
+        if (d2(up) < d2(L)) L = (L + 1 == m) ? 0 : L + 1;
+      }
+      *window = L;
+      return FK_OK;
+    }
+  }
+  *window = knn_window_host(MS, k, x, y);  // a bin the table does not certify: the sliding search
+  return FK_OK;
+}
+
 int fk_mesh_csr(fk_ctx* ctx, int mesh_id, int* rowptr, int* col, double* val0) {
   fk::Mesh* M = get_mesh(ctx, mesh_id);
   if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mesh id");

@@ -78,6 +78,7 @@ _SIGS = {
     "fk_cuda_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "fk_last_timing": (C.c_int, [C.c_void_p, _dp]),
     "fk_last_windows": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "fk_mesh_window": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, _ip, _ip, _ip]),
     "fk_register_bvp": (C.c_int, [C.c_void_p, C.POINTER(BvpDesc), _ip]),
     "fk_solve_points": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _up, _dp, _ip, _dp, C.c_int,
                                   C.POINTER(Stats)]),
@@ -221,6 +222,13 @@ class Context:
         v = C.c_void_p()
         self.check(self.L.fk_cuda_stream(self.h, C.byref(v)))
         return v.value
+
+    def mesh_window(self, mesh, s, x, y):
+        """(first chain node of the k-window, nearest node, walk modes) the path
+        kernel picks for a point on the boundary of patch s (fk_mesh_window)."""
+        w, nr, wk = C.c_int(), C.c_int(), C.c_int()
+        self.check(self.L.fk_mesh_window(self.h, mesh, s, x, y, C.byref(w), C.byref(nr), C.byref(wk)))
+        return w.value, nr.value, wk.value
 
     def last_windows(self):
         """Stencil windows whose moments the last patch-stencil solve formed into G rows."""
