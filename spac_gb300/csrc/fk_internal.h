@@ -70,8 +70,9 @@ constexpr int kSlotsFP32 = 3;
 
 // Gaussian stencil weights exp(-arg) with arg >= kPhiCut (< 1e-30) are not
 // added; FP32 stepping drops them from arg >= kPhiCut32 (< 3.1e-8 = 2^-25,
-// below FP32 resolution next to the exit's own nearest weights, which are at
-// least exp(-(eps spacing / 2)^2): 0.105 at eps spacing = 3).
+// below FP32 resolution next to the exit's own nearest weight: at least
+// exp(-(eps spacing / 2)^2) along a side, 0.78 at eps spacing = 1 and 0.105
+// at 3, and exp(-(eps spacing)^2) in a patch corner).
 constexpr float kPhiCut = 69.0f;
 constexpr float kPhiCut32 = 17.3f;
 // How an exit visits the nodes of its k-window (PatchDev::walk):
