@@ -1683,7 +1683,7 @@ int fk_assembly_end(fk_ctx* ctx, int mesh_id, double* val, double* B, double* it
   FK_CUDA(ctx->w_bout.ensure(std::max<size_t>(n * sizeof(double), 16)));
   FK_CUDA(ctx->w_sout.ensure(std::max<size_t>(static_cast<size_t>(n) * 16 * sizeof(double), 16)));
   FK_CUDA(ctx->w_queue.ensure(16));
-  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 4 * sizeof(int), s));
+  FK_CUDA(cudaMemsetAsync(ctx->w_queue.p, 0, 7 * sizeof(int), s));  // (run_items' seven check words)
   FK_CUDA(cudaMemcpyAsync(ctx->w_val.p, M->d_val0.p, hm.nnz * sizeof(double), cudaMemcpyDeviceToDevice, s));
   FK_CUDA(cudaMemsetAsync(ctx->w_B.p, 0, hm.n_rows * sizeof(double), s));
   fk::FinalizeArgs f;
@@ -1737,7 +1737,7 @@ int fk_mlp_create(fk_ctx* ctx, int n_regions, const double* rects, unsigned long
   int rc = need_device(ctx);
   if (rc) return rc;
   std::unique_ptr<fk::Mlp> M(new fk::Mlp());
-  rc = fk::mlp_init(*M, n_regions, rects, seed, ctx->err);
+  rc = fk::mlp_init(*M, n_regions, rects, seed, ctx->stream, ctx->err);
   if (rc) return rc;
   ctx->mlps.push_back(std::move(M));
   *mlp_id = static_cast<int>(ctx->mlps.size()) - 1;
@@ -1755,7 +1755,9 @@ int fk_mlp_get_params(fk_ctx* ctx, int mlp_id, float* params) {
   fk::Mlp* M = get_mlp(ctx, mlp_id);
   if (!M || !params) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
   cudaSetDevice(ctx->device);
-  FK_CUDA(cudaMemcpy(params, M->d_master, sizeof(float) * M->n_regions * fk::mlp_nparam(), cudaMemcpyDeviceToHost));
+  FK_CUDA(cudaMemcpyAsync(params, M->d_master, sizeof(float) * M->n_regions * fk::mlp_nparam(), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  FK_CUDA(cudaStreamSynchronize(ctx->stream));
   return FK_OK;
 }
 
@@ -1763,7 +1765,7 @@ int fk_mlp_set_params(fk_ctx* ctx, int mlp_id, const float* params) {
   fk::Mlp* M = get_mlp(ctx, mlp_id);
   if (!M || !params) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
   cudaSetDevice(ctx->device);
-  const int rc = fk::mlp_set_params(*M, params);
+  const int rc = fk::mlp_set_params(*M, params, ctx->stream);
   if (rc) return fail(ctx, rc, "mlp: set params failed");
   M->table_grid = 0;  // the gradient table is stale
   return FK_OK;

@@ -211,8 +211,8 @@ size_t paths_smem_bytes(int precision, int stencil_kind, int acc_words, int smem
                         int block = 256, bool wm_shared = false);
 cudaError_t launch_paths(const LaunchArgs& a, int problem, int precision, int grid, int block,
                          size_t smem, cudaStream_t s, bool warp_mode = false);
-// FP32 path-kernel builds without the control-variate terms (fk_paths_plain.cu).
-const void* select_paths_plain(int problem, int st, bool warp_mode, bool four);
+// path-kernel builds without the control-variate terms (fk_paths_plain.cu)
+const void* select_paths_plain(int problem, int precision, int st, bool warp_mode, bool four);
 int paths_kernel_occupancy(int problem, int precision, int stencil_kind, int cv, int block, size_t smem,
                            bool warp_mode = false);
 // host launchers (fk_kernels.cu)

@@ -829,7 +829,8 @@ cudaError_t mlp_eval_device(const float* params, const void* wbf, const float4* 
 // (the context-side parts live in fk_api.cu; these helpers are called there)
 namespace fk {
 
-int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed, std::string& err) {
+int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed, cudaStream_t s,
+             std::string& err) {
   M.n_regions = n_regions;
   M.n_params = NPARAM;
   M.rects.assign(rects, rects + 4 * n_regions);
@@ -876,24 +877,30 @@ int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed
     err = "mlp: device allocation failed";
     return FK_ERR_CUDA;
   }
-  cudaMemcpy(M.d_master, p.data(), np * sizeof(float), cudaMemcpyHostToDevice);
-  cudaMemset(M.d_m, 0, np * sizeof(float));
-  cudaMemset(M.d_v, 0, np * sizeof(float));
-  cudaMemcpy(M.d_norm, norm.data(), n_regions * sizeof(float4), cudaMemcpyHostToDevice);
-  cudaMemcpy(M.d_rect, rects, 4 * n_regions * sizeof(double), cudaMemcpyHostToDevice);
-  mlp_refresh_bf16<<<64, 256>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), n_regions);
-  if (cudaDeviceSynchronize() != cudaSuccess) { err = "mlp: init kernels failed"; return FK_ERR_CUDA; }
+  cudaMemcpyAsync(M.d_master, p.data(), np * sizeof(float), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(M.d_m, 0, np * sizeof(float), s);
+  cudaMemsetAsync(M.d_v, 0, np * sizeof(float), s);
+  cudaMemcpyAsync(M.d_norm, norm.data(), n_regions * sizeof(float4), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M.d_rect, rects, 4 * n_regions * sizeof(double), cudaMemcpyHostToDevice, s);
+  mlp_refresh_bf16<<<64, 256, 0, s>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), n_regions);
+  if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    err = "mlp: init kernels failed";
+    return FK_ERR_CUDA;
+  }
   return FK_OK;
 }
 
-int mlp_set_params(Mlp& M, const float* host) {
+// (on the context's stream, which does not synchronise with the legacy
+// default stream: queued training, refit and table work is ordered before it)
+int mlp_set_params(Mlp& M, const float* host, cudaStream_t s) {
   const size_t np = static_cast<size_t>(M.n_regions) * NPARAM;
-  if (cudaMemcpy(M.d_master, host, np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return FK_ERR_CUDA;
-  cudaMemset(M.d_m, 0, np * sizeof(float));
-  cudaMemset(M.d_v, 0, np * sizeof(float));
+  cudaError_t e = cudaMemcpyAsync(M.d_master, host, np * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(M.d_m, 0, np * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(M.d_v, 0, np * sizeof(float), s);
+  if (e != cudaSuccess) return FK_ERR_CUDA;
   M.adam_t = 0;
-  mlp_refresh_bf16<<<64, 256>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), M.n_regions);
-  return cudaDeviceSynchronize() == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+  mlp_refresh_bf16<<<64, 256, 0, s>>>(M.d_master, static_cast<__nv_bfloat16*>(M.d_bf16), M.n_regions);
+  return cudaStreamSynchronize(s) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
 // Uploads (x, y, target) samples grouped by region.
@@ -911,7 +918,7 @@ static cudaError_t grow(T*& p, size_t& cap, size_t need) {
 }
 
 static int upload_samples(Mlp& M, int n, const double* xy, const double* target, const int* region,
-                          std::vector<int>& off, std::string& err) {
+                          std::vector<int>& off, cudaStream_t s, std::string& err) {
   std::vector<std::vector<float4>> by(M.n_regions);
   for (int i = 0; i < n; ++i) {
     const int r = region ? region[i] : 0;
@@ -931,9 +938,12 @@ static int upload_samples(Mlp& M, int n, const double* xy, const double* target,
     err = "mlp: sample allocation failed";
     return FK_ERR_CUDA;
   }
-  cudaMemcpy(M.d_samples, flat.data(), flat.size() * sizeof(float4), cudaMemcpyHostToDevice);
+  // (pageable sources: each copy has read its source when it returns)
   int* d_off = reinterpret_cast<int*>(M.d_samples + std::max<size_t>(flat.size(), 1));
-  cudaMemcpy(d_off, off.data(), (M.n_regions + 1) * sizeof(int), cudaMemcpyHostToDevice);
+  cudaError_t e = cudaSuccess;
+  if (!flat.empty()) e = cudaMemcpyAsync(M.d_samples, flat.data(), flat.size() * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off.data(), (M.n_regions + 1) * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) { err = cudaGetErrorString(e); return FK_ERR_CUDA; }
   M.d_sample_off = d_off;
   return FK_OK;
 }
@@ -942,7 +952,7 @@ int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* 
               double lr, unsigned long long seed, float* loss_hist, cudaStream_t s, std::string& err) {
   if (steps < 0 || batch < kRows || batch % kRows) { err = "batch must be a positive multiple of " + std::to_string(kRows); return FK_ERR_ARG; }
   std::vector<int> off;
-  int rc = upload_samples(M, n, xy, target, region, off, err);
+  int rc = upload_samples(M, n, xy, target, region, off, s, err);
   if (rc) return rc;
   // Persistent training (all steps in one cooperative launch) when the grid
   // fits on the device at once, with as many CTAs (one 64-row tile each) as
@@ -1093,7 +1103,7 @@ int mlp_loss_grad(Mlp& M, int n, const double* xy, const double* target, double*
   // region 0, all n samples, no sampling
   std::vector<int> off;
   std::vector<int> reg(n, 0);
-  int rc = upload_samples(M, n, xy, target, reg.data(), off, err);
+  int rc = upload_samples(M, n, xy, target, reg.data(), off, s, err);
   if (rc) return rc;
   const int rows = (n + kRows - 1) / kRows * kRows;
   const int ctas = rows / kRows;
@@ -1105,8 +1115,9 @@ int mlp_loss_grad(Mlp& M, int n, const double* xy, const double* target, double*
     err = "mlp: loss-grad buffers";
     return FK_ERR_CUDA;
   }
-  cudaMemset(d_partial, 0, np * ctas * sizeof(float));
-  cudaMemset(d_loss, 0, static_cast<size_t>(M.n_regions) * ctas * sizeof(float));
+  // (on s: the legacy default stream does not order work on the context's non-blocking stream)
+  cudaMemsetAsync(d_partial, 0, np * ctas * sizeof(float), s);
+  cudaMemsetAsync(d_loss, 0, static_cast<size_t>(M.n_regions) * ctas * sizeof(float), s);
   cudaFuncSetAttribute(mlp_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(Smem)));
   PassArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -1158,10 +1169,11 @@ int mlp_eval_host(Mlp& M, int n, const double* xy, const int* region, double* ou
       err = "mlp eval buffers";
       return FK_ERR_CUDA;
     }
-    cudaMemcpy(d_pts, pts.data(), pts.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    cudaError_t e = mlp_eval_device(M.d_master + static_cast<size_t>(r) * NPARAM,
-                                    static_cast<__nv_bfloat16*>(M.d_bf16) + static_cast<size_t>(r) * BF_PER_REGION,
-                                    M.d_norm + r, static_cast<int>(pts.size()), d_pts, d_out, s);
+    cudaError_t e = cudaMemcpyAsync(d_pts, pts.data(), pts.size() * sizeof(float2), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = mlp_eval_device(M.d_master + static_cast<size_t>(r) * NPARAM,
+                          static_cast<__nv_bfloat16*>(M.d_bf16) + static_cast<size_t>(r) * BF_PER_REGION,
+                          M.d_norm + r, static_cast<int>(pts.size()), d_pts, d_out, s);
     std::vector<float> o(3 * pts.size());
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = cudaMemcpy(o.data(), d_out, o.size() * sizeof(float), cudaMemcpyDeviceToHost);

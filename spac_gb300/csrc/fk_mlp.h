@@ -49,8 +49,9 @@ struct Mlp {
 
 size_t mlp_pass_smem();
 int mlp_nparam();
-int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed, std::string& err);
-int mlp_set_params(Mlp& M, const float* host);
+int mlp_init(Mlp& M, int n_regions, const double* rects, unsigned long long seed, cudaStream_t s,
+             std::string& err);
+int mlp_set_params(Mlp& M, const float* host, cudaStream_t s);
 int mlp_train(Mlp& M, int n, const double* xy, const double* target, const int* region, int steps, int batch,
               double lr, unsigned long long seed, float* loss_hist, cudaStream_t s, std::string& err);
 int mlp_loss_grad(Mlp& M, int n, const double* xy, const double* target, double* loss, float* grad, cudaStream_t s,

@@ -1,6 +1,6 @@
 // Path-kernel launches: the instantiations with the control-variate terms
 // (FP32 and FP64 stepping), the choice of build for a launch and the launch
-// itself.  The kernel is in fk_paths_kernel.cuh; the FP32 builds without the
+// itself.  The kernel is in fk_paths_kernel.cuh; the builds without the
 // control-variate terms are instantiated in fk_paths_plain.cu.
 #include "fk_paths_kernel.cuh"
 
@@ -9,7 +9,7 @@ namespace fk {
 namespace {
 
 const void* select_paths_v(int problem, int precision, int st, bool warp_mode, bool four, bool cv) {
-  if (precision == 1 && !cv) return select_paths_plain(problem, st, warp_mode, four);
+  if (!cv) return select_paths_plain(problem, precision, st, warp_mode, four);
   if (warp_mode)
     return precision == 1 ? paths_fn_r<float, true, true>(problem, st, false)
                           : paths_fn_r<double, true, true>(problem, st, false);
