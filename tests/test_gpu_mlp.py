@@ -231,3 +231,48 @@ def test_fit_output_layer_is_least_squares(gpu, orc, fk, regions):
         l1, g1 = _loss_grad(gpu, fk, mid, n, xy, tgt)
         assert l1 <= l0 * (1 + 1e-4)
         assert np.abs(g1[off_w4:]).max() <= 2e-2 * np.abs(g0[off_w4:]).max()
+
+
+@pytest.mark.parametrize("trainer", ["steps", "grid"])
+def test_adam_steps_match_cpu_adam(gpu, orc, fk, trainer):
+    """Four training calls of one step each against a CPU Adam in FP64
+    (beta1 0.9, beta2 0.999, eps 1e-8, bias corrections 1 - beta^t with t
+    counted across calls; a one-step call runs at the full rate lr).  The
+    batch rows are drawn as the trainer draws them: row r of step t takes
+    sample Philox4x32-10((t, r, region, 0x6d6c70), seed).x mod n.  The
+    batch-mean gradient comes from fk_mlp_loss_grad on those rows in batch
+    order, at the trainer's current weights; with 64-row tiles it sums the
+    same tile partials in the same order as the per-step trainer, so there
+    the gradients are the trainer's own and only the FP32 Adam arithmetic
+    differs from the CPU's.  The grid trainer sums the partials in another
+    fixed order: its updates agree except for components whose gradient is
+    at rounding level."""
+    rect = (0.0, 0.0, 1.0, 1.0)
+    mid, n = _mlp(gpu, fk, [rect], seed=13)
+    gpu.check(gpu.L.fk_mlp_set_trainer(gpu.h, mid, fk.TRAIN_STEPS if trainer == "steps" else fk.TRAIN_GRID))
+    rng = np.random.default_rng(6)
+    xy = rng.uniform(0, 1, size=(500, 2))
+    tgt = _franke(orc, xy)
+    batch, lr, seed = 256, 1e-2, 0x1234567890ab
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    key = (seed & 0xFFFFFFFF, seed >> 32)
+    m = np.zeros(n)
+    v = np.zeros(n)
+    agree = []
+    for t in range(4):
+        p0 = _params(gpu, fk, mid, n)
+        rows = np.array([orc.philox((t, r, 0, 0x6D6C70), key)[0] % len(xy) for r in range(batch)])
+        _, g = _loss_grad(gpu, fk, mid, n, xy[rows], tgt[rows])
+        g = g.astype(np.float64)
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        upd = lr * (m / (1 - b1 ** (t + 1))) / (np.sqrt(v / (1 - b2 ** (t + 1))) + eps)
+        _train(gpu, fk, mid, xy, tgt, steps=1, batch=batch, lr=lr, seed=seed)
+        d = (p0.astype(np.float64) - _params(gpu, fk, mid, n).astype(np.float64))
+        # one FP32 rounding of the weight, FP32 Adam arithmetic
+        tol = 2 * np.spacing(np.abs(p0).astype(np.float32)).astype(np.float64) + 1e-5 * np.abs(upd)
+        agree.append((np.abs(d - upd) <= tol).mean())
+    if trainer == "steps":
+        assert min(agree) == 1.0, agree
+    else:
+        assert min(agree) > 0.99, agree
