@@ -679,12 +679,37 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     unsigned n_dom = 0, n_cap = 0, n_done = 0;
     R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0;
     int k = 0;
+    // learned control variate: grad u_hat at (px, py), bilinear in the
+    // region's table (clamped to it)
+    auto cv_grad = [&](R px, R py, R& gx, R& gy) {
+      R u = (px - cx0) * csx, v = (py - cy0) * csy;
+      u = fmin(fmax(u, R(0)), R(G - 1) - R(1e-3));
+      v = fmin(fmax(v, R(0)), R(G - 1) - R(1e-3));
+      if (std::is_same<R, float>::value && a.cv_tex) {
+        // the texture unit's bilinear filter (texel centres at i + 1/2)
+        const float2 g = tex2D<float2>(a.cv_tex, static_cast<float>(u) + 0.5f, static_cast<float>(v) + tex_y0);
+        gx = R(g.x);
+        gy = R(g.y);
+      } else {
+        const int i = static_cast<int>(u), j = static_cast<int>(v);
+        const R fu = u - R(i), fv = v - R(j);
+        const float2* T = ctab + j * G + i;
+        const float2 t00 = __ldg(T), t10 = __ldg(T + 1), t01 = __ldg(T + G), t11 = __ldg(T + G + 1);
+        gx = (R(1) - fv) * ((R(1) - fu) * R(t00.x) + fu * R(t10.x)) + fv * ((R(1) - fu) * R(t01.x) + fu * R(t11.x));
+        gy = (R(1) - fv) * ((R(1) - fu) * R(t00.y) + fu * R(t10.y)) + fv * ((R(1) - fu) * R(t01.y) + fu * R(t11.y));
+      }
+    };
+    // grad u_hat at the lane's current point: fetched as soon as the lane
+    // reaches the point, so that the lookup's latency overlaps the rest of
+    // the iteration and the next step's coefficients and normals
+    R cgx = R(0), cgy = R(0);
     // every lane's first path of the chunk (chunk-local index); in warp mode
     // the warp owns the chunk and counts its paths in a register
     unsigned base = 0, wnext = 32u;
     if (!WM && lane == 0) base = atomicAdd(&sl.next, 32u);
     unsigned pl = __shfl_sync(kFull, base, 0) + lane;
     bool active = pl < n_ch;
+    if (cv_table && active) cv_grad(x, y, cgx, cgy);
     int qn = 0;  // queued exits of this warp (warp-uniform)
 
     // Processes the top `cnt` (<= 32) queued exits, one per lane: exit value
@@ -805,26 +830,10 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         StepCoef<R> co;
         Problem<PROB>::step(bvp, x, y, st, cv_exact, co);
         if (cv_table) {
-          // F = -sigma^T grad u_hat, bilinear in the region's table
-          R u = (x - cx0) * csx, v = (y - cy0) * csy;
-          u = fmin(fmax(u, R(0)), R(G - 1) - R(1e-3));
-          v = fmin(fmax(v, R(0)), R(G - 1) - R(1e-3));
-          R gx, gy;
-          if (std::is_same<R, float>::value && a.cv_tex) {
-            // the texture unit's bilinear filter (texel centres at i + 1/2)
-            const float2 g = tex2D<float2>(a.cv_tex, static_cast<float>(u) + 0.5f, static_cast<float>(v) + tex_y0);
-            gx = R(g.x);
-            gy = R(g.y);
-          } else {
-            const int i = static_cast<int>(u), j = static_cast<int>(v);
-            const R fu = u - R(i), fv = v - R(j);
-            const float2* T = ctab + j * G + i;
-            const float2 t00 = __ldg(T), t10 = __ldg(T + 1), t01 = __ldg(T + G), t11 = __ldg(T + G + 1);
-            gx = (R(1) - fv) * ((R(1) - fu) * R(t00.x) + fu * R(t10.x)) + fv * ((R(1) - fu) * R(t01.x) + fu * R(t11.x));
-            gy = (R(1) - fv) * ((R(1) - fu) * R(t00.y) + fu * R(t10.y)) + fv * ((R(1) - fu) * R(t01.y) + fu * R(t11.y));
-          }
-          co.Fx = -co.s * gx;
-          co.Fy = -co.s * gy;
+          // F = -sigma^T grad u_hat at the step's start point, looked up
+          // when the lane reached it (end of the previous iteration)
+          co.Fx = -co.s * cgx;
+          co.Fy = -co.s * cgy;
         }
         // one Philox block per step, counter (step, path, item, stream), words
         // x and y: every lane computes a block at every step, so the warp
@@ -1001,6 +1010,9 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         qn += __popc(em);
         __syncwarp();
       }
+      // the next step's grad u_hat: at the new point, or at the start point
+      // of the lane's next path
+      if (cv_table && active) cv_grad(x, y, cgx, cgy);
       if (qn >= 32 || !any) {
         process(qn >= 32 ? 32 : qn);
         __syncwarp();
