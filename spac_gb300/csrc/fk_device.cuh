@@ -318,7 +318,9 @@ struct MonegrosEval {
 
 // Problem functors.  state(x, y) is what sigma needs at a point (the
 // anisotropy factor a(x, y) of FK_PROBLEM_ANISO; nothing for constant sigma);
-// the exit rule computes it at the new point and the next step reuses it.
+// the exit rule computes it and sigma_of(state) at the new point, and the
+// next step reuses both: step(bvp, x, y, a, s, cv, o) gets the state a and
+// s = sigma_of(a).
 template <int PROB>
 struct Problem;
 
@@ -330,7 +332,7 @@ struct Problem<0> {
   template <typename R>
   __device__ static R sigma_of(R) { return R(1.41421356237); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
+  __device__ static void step(const BvpDev&, R x, R y, R, R, bool cv, StepCoef<R>& o) {
     FrankeEval<R> F(x, y);
     o.s = R(1.41421356237);
     o.f = -F.lap();
@@ -354,7 +356,7 @@ struct Problem<1> {
   template <typename R>
   __device__ static R sigma_of(R) { return R(1.41421356237); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
+  __device__ static void step(const BvpDev&, R x, R y, R, R, bool cv, StepCoef<R>& o) {
     MonegrosEval<R> M(x, y);
     o.s = R(1.41421356237);
     o.c = R(-1);
@@ -382,14 +384,14 @@ struct Problem<2> {
   template <typename R>
   __device__ static R sigma_of(R a) { return fsqrt(R(2) * a); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, R a, bool cv, StepCoef<R>& o) {
+  __device__ static void step(const BvpDev&, R x, R y, R a, R s, bool cv, StepCoef<R>& o) {
     FrankeEval<R> F(x, y);
     const R q = R(1) + x * y;
     const R Fv = F.u(), Fx = F.ux(), Fy = F.uy();
     const R u = Fv * q;
     const R ux = Fx * q + Fv * y, uy = Fy * q + Fv * x;
     const R lap = F.lap() * q + R(2) * (Fx * y + Fy * x);
-    o.s = fsqrt(R(2) * a);
+    o.s = s;  // sigma_of(a), formed where the state was
     o.c = -(R(1) + x * x + y * y);
     o.bx = y - R(0.5);
     o.by = R(0.5) - x;
@@ -411,7 +413,7 @@ struct Problem<3> {
   template <typename R>
   __device__ static R sigma_of(R) { return R(1.41421356237); }
   template <typename R>
-  __device__ static void step(const BvpDev& b, R x, R y, R, bool cv, StepCoef<R>& o) {
+  __device__ static void step(const BvpDev& b, R x, R y, R, R, bool cv, StepCoef<R>& o) {
     const R inv = R(1) / (R(2) * R(b.prob[2]));
     const R xi = (x - R(b.prob[0])) * inv + R(0.5), eta = (y - R(b.prob[1])) * inv + R(0.5);
     FrankeEval<R> F(xi, eta);
@@ -461,7 +463,7 @@ struct Problem<5> {
   template <typename R>
   __device__ static R sigma_of(R) { return R(1.41421356237); }
   template <typename R>
-  __device__ static void step(const BvpDev&, R x, R y, R, bool cv, StepCoef<R>& o) {
+  __device__ static void step(const BvpDev&, R x, R y, R, R, bool cv, StepCoef<R>& o) {
     MonegrosEval<R> M(x, y);
     o.s = R(1.41421356237);
     o.c = R(0);

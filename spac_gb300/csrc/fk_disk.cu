@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(kCoefThreads) disk_coef_kernel(const DiskArgs 
     const double th = l * dt + D.theta0;
     const double x = r[j] * cos(th) + D.cx, y = r[j] * sin(th) + D.cy;
     StepCoef<double> o;
-    Problem<PROB>::template step<double>(bvp, x, y, Problem<PROB>::template state<double>(bvp, x, y), false, o);
+    const double a_xy = Problem<PROB>::template state<double>(bvp, x, y);
+    Problem<PROB>::template step<double>(bvp, x, y, a_xy, Problem<PROB>::template sigma_of<double>(a_xy), false, o);
     cg[q] = o.c;
     fg[q] = (-1.0) * o.f;
   }

@@ -648,6 +648,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         dom_can_win = !(s0 > d0 && s1 > d1 && s2 < d2 && s3 < d3);
     }
     const R st0 = Problem<PROB>::template state<R>(bvp, x0, y0);  // sigma state at the start point
+    const R sg0 = Problem<PROB>::template sigma_of<R>(st0);
     // Reflecting sides (FK_PROBLEM_ROBIN), only where the domain can win
     // Dentro's comparison.
     int rmask = 0;
@@ -677,7 +678,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
     Acc acc[kNumAcc];
     unsigned long long n_steps = 0;
     unsigned n_dom = 0, n_cap = 0, n_done = 0;
-    R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0;
+    R x = x0, y = y0, Y = R(1), Z = R(0), xi = R(0), st = st0, sgc = sg0;  // sgc = sigma_of(st)
     int k = 0;
     // learned control variate: grad u_hat at (px, py), bilinear in the
     // region's table (clamped to it)
@@ -828,7 +829,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
       if (active) {
         // ---- one Euler-Maruyama step (Paso_Absorbente, FeynmanKacSolver.cpp:7-18)
         StepCoef<R> co;
-        Problem<PROB>::step(bvp, x, y, st, cv_exact, co);
+        Problem<PROB>::step(bvp, x, y, st, sgc, cv_exact, co);
         if (cv_table) {
           // F = -sigma^T grad u_hat at the step's start point, looked up
           // when the lane reached it (end of the previous iteration)
@@ -933,8 +934,11 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
         // projection: one evaluation at the selected point, no divergence
         const bool inside = w.d < R(0);
         const R stq = Problem<PROB>::template state<R>(bvp, inside ? x : w.ex, inside ? y : w.ey);
-        if (inside) st = stq;
         const R sg = Problem<PROB>::template sigma_of<R>(stq);
+        if (inside) {
+          st = stq;
+          sgc = sg;
+        }
         // Gobet shift kGobet |sigma^T n| sqrt(h) (FeynmanKacSolver.cpp:85,92).
         // Every registered sigma is s I, and the normals are unit vectors (axes
         // or the normalised diagonal), so FP32 stepping takes |sigma^T n| = s;
@@ -981,7 +985,10 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
           }
           // a path that goes on from a point on (or, by rounding, just past)
           // a reflecting side steps with sigma at that point
-          if (!exits && !inside) st = Problem<PROB>::template state<R>(bvp, x, y);
+          if (!exits && !inside) {
+            st = Problem<PROB>::template state<R>(bvp, x, y);
+            sgc = Problem<PROB>::template sigma_of<R>(st);
+          }
         }
         ex = w.ex;
         ey = w.ey;
@@ -1005,7 +1012,7 @@ __global__ void __launch_bounds__(256, MB) paths_kernel(const LaunchArgs a) {
           q.kf[e] = static_cast<unsigned>(k) | (dom_wins ? 1u << 30 : 0u) | (capped ? 1u << 31 : 0u);
           pl = nb + rank;
           active = pl < n_ch;
-          x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0; st = st0;
+          x = x0; y = y0; Y = R(1); Z = R(0); xi = R(0); k = 0; st = st0; sgc = sg0;
         }
         qn += __popc(em);
         __syncwarp();
