@@ -394,6 +394,13 @@ int fk_mlp_loss_grad(fk_ctx* ctx, int mlp_id, int n, const double* xy, const dou
                      double* loss, float* grad);
 /* tabulates grad u_hat on a grid x grid lattice of every region (used by FK_CV_MLP solves) */
 int fk_mlp_build_table(fk_ctx* ctx, int mlp_id, int grid);
+/* The table of fk_mlp_build_table, as FK_CV_MLP steps interpolate it:
+ * *grid = its lattice size (0 before the first build or after
+ * fk_mlp_set_params); if table is not NULL it receives n_regions x grid x
+ * grid FP32 pairs (du_hat/dx, du_hat/dy), the pair of lattice point (i, j) of
+ * region r, at x0 + (x1 - x0) i / (grid - 1), y0 + (y1 - y0) j / (grid - 1)
+ * of the region's rectangle, at table[2 ((r grid + j) grid + i)]. */
+int fk_mlp_get_table(fk_ctx* ctx, int mlp_id, int* grid, float* table);
 
 #ifdef __cplusplus
 }

@@ -246,6 +246,28 @@ double aniso_a(double x, double y) {
 
 double mlp_grad(const orc_mlp* m, double x, double y, double g[2], double* val);
 
+// Tabulated grad u_hat (cv == 3).  The learned control variate has no
+// counterpart in the reference; this is the library's own deployment of it
+// (the FK_CV_MLP step interpolates its gradient table), restated in FP64 so
+// that the GPU's FP64 stepping can be checked path for path: the point mapped
+// to lattice units and clamped to [0, grid - 1 - 1e-3], then bilinear between
+// the four surrounding lattice points.
+void cv_table_grad(const orc_cv_table* T, double x, double y, double g[2]) {
+  const int G = T->grid;
+  const double sx = (G - 1) / (T->rect[2] - T->rect[0]), sy = (G - 1) / (T->rect[3] - T->rect[1]);
+  double u = (x - T->rect[0]) * sx, v = (y - T->rect[1]) * sy;
+  u = std::fmin(std::fmax(u, 0.0), static_cast<double>(G - 1) - 1e-3);
+  v = std::fmin(std::fmax(v, 0.0), static_cast<double>(G - 1) - 1e-3);
+  const int i = static_cast<int>(u), j = static_cast<int>(v);
+  const double fu = u - i, fv = v - j;
+  const float* t00 = T->tab + 2 * (static_cast<long>(j) * G + i);
+  const float* t10 = t00 + 2;
+  const float* t01 = t00 + 2 * G;
+  const float* t11 = t01 + 2;
+  for (int c = 0; c < 2; ++c)
+    g[c] = (1.0 - fv) * ((1.0 - fu) * t00[c] + fu * t10[c]) + fv * ((1.0 - fu) * t01[c] + fu * t11[c]);
+}
+
 Coef coefficients(const orc_bvp* B, double x, double y) {
   Coef c;
   c.b = V2{0.0 * x, 0.0 * y};  // Vector_Defecto: position * 0.0
@@ -321,6 +343,11 @@ Coef coefficients(const orc_bvp* B, double x, double y) {
     double g[2], v;
     mlp_grad(static_cast<const orc_mlp*>(B->mlp), x, y, g, &v);
     // F = -sigma^T grad u_hat (the reference's control-variate hook)
+    c.F = V2{-(c.s.a00 * g[0] + c.s.a10 * g[1]), -(c.s.a01 * g[0] + c.s.a11 * g[1])};
+  }
+  if (B->cv == 3 && B->mlp) {
+    double g[2];
+    cv_table_grad(static_cast<const orc_cv_table*>(B->mlp), x, y, g);
     c.F = V2{-(c.s.a00 * g[0] + c.s.a10 * g[1]), -(c.s.a01 * g[0] + c.s.a11 * g[1])};
   }
   return c;

@@ -31,12 +31,25 @@ enum { ORC_OUT_INSIDE = 0, ORC_OUT_DOMAIN = 1, ORC_OUT_SUBDOMAIN = 2 };
 
 typedef struct {
   int problem;      /* ORC_PROBLEM_* */
-  int cv;           /* 0: F = 0; 1: exact-gradient control variate F = -sigma^T grad u; 2: MLP */
+  int cv;           /* 0: F = 0; 1: exact-gradient control variate F = -sigma^T grad u; 2: MLP;
+                       3: tabulated grad u_hat (orc_cv_table) */
   int dom_shape;    /* ORC_SHAPE_* */
   double dom[4];    /* rect: x0,y0,x1,y1; circle: r,cx,cy */
   double prob[4];   /* disk problem: cx, cy, R */
-  const void* mlp;  /* cv == 2: orc_mlp* */
+  const void* mlp;  /* cv == 2: orc_mlp*; cv == 3: orc_cv_table* */
 } orc_bvp;
+
+/* cv == 3: F = -sigma^T grad u_hat with grad u_hat interpolated bilinearly in
+ * FP64 from FP32 values on a grid x grid lattice of rect (x0, y0, x1, y1):
+ * the pair (d/dx, d/dy) of lattice point (i, j), at x0 + (x1 - x0) i /
+ * (grid - 1), y0 + (y1 - y0) j / (grid - 1), at tab[2 (j grid + i)] (the
+ * layout of fk_mlp_get_table, one region); the point is clamped into the
+ * rectangle, as the GPU's FK_CV_MLP step does. */
+typedef struct {
+  int grid;
+  double rect[4];
+  const float* tab;
+} orc_cv_table;
 
 typedef struct {
   int shape;        /* ORC_SHAPE_* */

@@ -46,6 +46,11 @@ class Exit(C.Structure):
                 ("t", C.c_double), ("outcome", C.c_int), ("steps", C.c_int)]
 
 
+class CvTable(C.Structure):
+    """orc_cv_table: a tabulated grad u_hat (bvp cv = 3; the layout of fk_mlp_get_table)."""
+    _fields_ = [("grid", C.c_int), ("rect", C.c_double * 4), ("tab", C.POINTER(C.c_float))]
+
+
 class Mlp(C.Structure):
     _fields_ = [("width", C.c_int), ("in_lo", C.c_double * 2), ("in_scale", C.c_double * 2)] + \
         [(n, _dp) for n in ("W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4")]

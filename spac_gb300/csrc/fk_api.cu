@@ -1826,5 +1826,20 @@ int fk_mlp_build_table(fk_ctx* ctx, int mlp_id, int grid) {
   return fk::mlp_build_table(*M, grid, ctx->stream, ctx->err);
 }
 
+int fk_mlp_get_table(fk_ctx* ctx, int mlp_id, int* grid, float* table) {
+  fk::Mlp* M = get_mlp(ctx, mlp_id);
+  if (!M) return fail(ctx, FK_ERR_REGISTRY, "unknown mlp id");
+  if (!grid) return fail(ctx, FK_ERR_ARG, "null argument");
+  const int G = (M->table_grid >= 2 && M->d_table) ? M->table_grid : 0;
+  *grid = G;
+  if (table && G) {
+    cudaSetDevice(ctx->device);
+    const size_t bytes = static_cast<size_t>(M->n_regions) * G * G * 2 * sizeof(float);
+    FK_CUDA(cudaMemcpyAsync(table, M->d_table, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    FK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return FK_OK;
+}
+
 }  // extern "C"
 

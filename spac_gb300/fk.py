@@ -114,6 +114,7 @@ _SIGS = {
     "fk_mlp_set_trainer": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fk_mlp_fit_output": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _ip, C.c_double]),
     "fk_mlp_build_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "fk_mlp_get_table": (C.c_int, [C.c_void_p, C.c_int, _ip, _fp]),
     "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
     "fk_gmres_csr": (C.c_int, [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, _ip, _dp]),
     "fk_write_gb_coo": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _dp, _dp]),

@@ -69,6 +69,49 @@ def test_point_solves_fp64_match_oracle(gpu, orc, fk, case, launch):
         assert st["n_paths"][i] == N and st["n_capped"][i] == 0
 
 
+@pytest.mark.parametrize("problem", [0, 2])
+def test_learned_cv_table_fp64_matches_oracle(gpu, orc, fk, problem, launch):
+    """FK_CV_MLP with FP64 stepping against the oracle given the GPU's own
+    gradient table (fk_mlp_get_table; oracle cv = 3): the same paths, and at
+    every step the same bilinear lookup of grad u_hat at the step's start
+    point, so every statistic, the control variate's included, agrees to
+    rounding.  The network gets a few Adam steps on the exact solution, so
+    that the table is far from zero."""
+    import ctypes as C
+    rects = np.array([[0.0, 0.0, 1.0, 1.0]])
+    mid = C.c_int()
+    gpu.check(gpu.L.fk_mlp_create(gpu.h, 1, rects.ctypes.data_as(fk._dp), 3, C.byref(mid)))
+    rng = np.random.default_rng(8)
+    xy = np.ascontiguousarray(rng.uniform(0, 1, size=(512, 2)))
+    ob0 = orc.bvp(problem)
+    tgt = np.ascontiguousarray([orc.coefficients(ob0, x, y)[0] for x, y in xy])
+    gpu.check(gpu.L.fk_mlp_train(gpu.h, mid.value, len(tgt), xy.ctypes.data_as(fk._dp), tgt.ctypes.data_as(fk._dp),
+                                 None, 20, 512, 1e-2, 5, None))
+    G = C.c_int()
+    gpu.check(gpu.L.fk_mlp_get_table(gpu.h, mid.value, C.byref(G), None))
+    assert G.value == 0  # no table yet
+    gpu.check(gpu.L.fk_mlp_build_table(gpu.h, mid.value, 48))
+    gpu.check(gpu.L.fk_mlp_get_table(gpu.h, mid.value, C.byref(G), None))
+    assert G.value == 48
+    tab = np.zeros(2 * G.value * G.value, dtype=np.float32)
+    gpu.check(gpu.L.fk_mlp_get_table(gpu.h, mid.value, C.byref(G), tab.ctypes.data_as(fk._fp)))
+    assert np.abs(tab).max() > 0.1
+    b = gpu.register_bvp(problem, cv=fk.CV_MLP, mlp_id=mid.value)
+    pts = [(0.3, 0.4), (0.05, 0.9), (0.72, 0.18)]
+    N, h = 1500, 1e-3
+    gpu.set_stream(300 + problem)
+    st = gpu.solve_points(b, np.array(pts), N, h, fk.FP64)
+    s = _oracle_session(orc, gpu)
+    s.set_stream(300 + problem)
+    table = orc.CvTable(G.value, (C.c_double * 4)(0.0, 0.0, 1.0, 1.0), tab.ctypes.data_as(C.POINTER(C.c_float)))
+    ob = orc.bvp(problem, cv=3, mlp=table)
+    for i, (x, y) in enumerate(pts):
+        o = s.point_solve(ob, x, y, N, h, item=i)
+        for k in orc.STAT_NAMES:
+            assert np.isclose(st[k][i], o[k], rtol=RTOL, atol=1e-12), (k, i, st[k][i], o[k])
+    assert np.all(st["xixi"] > 1e-6)  # the control term is live
+
+
 def test_point_solves_fp32_paired_with_fp64(gpu, fk):
     b = gpu.register_bvp(fk.ANISO)
     pts = np.array([[0.3, 0.4], [0.8, 0.7], [0.1, 0.5]])

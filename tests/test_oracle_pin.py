@@ -43,6 +43,32 @@ def test_monegros_coefficients(orc):
         assert orc.coefficients(b5, x, y) == list(g["coefs"][i][12:])
 
 
+@pytest.mark.parametrize("problem", [0, 2])
+def test_cv_table_lookup(orc, problem):
+    """The oracle's tabulated grad u_hat (cv = 3, the layout of
+    fk_mlp_get_table): F = -sigma grad u_hat with grad u_hat bilinear in the
+    lattice, the point clamped into the rectangle; against numpy on a random
+    table, at points inside, outside and on the edges of the rectangle."""
+    G, rect = 17, (0.2, -0.1, 1.3, 0.7)
+    rng = np.random.default_rng(3)
+    tab = rng.standard_normal((G, G, 2)).astype(np.float32)  # [j][i][component]
+    flat = np.ascontiguousarray(tab.ravel())
+    T = orc.CvTable(G, (C.c_double * 4)(*rect), flat.ctypes.data_as(C.POINTER(C.c_float)))
+    b = orc.bvp(problem, cv=3, mlp=T)
+    pts = np.concatenate([rng.uniform(-0.2, 1.5, size=(200, 2)), [[rect[0], rect[1]], [rect[2], rect[3]]]])
+    for x, y in pts:
+        c = orc.coefficients(b, x, y)
+        s = c[6]  # sigma = s I for both problems
+        u = min(max((x - rect[0]) * (G - 1) / (rect[2] - rect[0]), 0.0), G - 1 - 1e-3)
+        v = min(max((y - rect[1]) * (G - 1) / (rect[3] - rect[1]), 0.0), G - 1 - 1e-3)
+        i, j = int(u), int(v)
+        fu, fv = u - i, v - j
+        t = tab.astype(np.float64)
+        g = (1 - fv) * ((1 - fu) * t[j, i] + fu * t[j, i + 1]) + fv * ((1 - fu) * t[j + 1, i] + fu * t[j + 1, i + 1])
+        assert np.allclose(c[10:12], -s * g, rtol=1e-13, atol=1e-14), (x, y)
+        assert c[7] == 0.0 and c[8] == 0.0
+
+
 def test_point_solves_bit_exact(orc):
     pts = np.load(os.path.join(GOLDEN, "points.npy"))
     for row in pts:
