@@ -110,6 +110,12 @@ def test_learned_cv_table_fp64_matches_oracle(gpu, orc, fk, problem, launch):
         for k in orc.STAT_NAMES:
             assert np.isclose(st[k][i], o[k], rtol=RTOL, atol=1e-12), (k, i, st[k][i], o[k])
     assert np.all(st["xixi"] > 1e-6)  # the control term is live
+    # FP32 stepping, whose lookup is the texture unit's bilinear filter (8-bit
+    # weights), paired with FP64 on the same stream
+    gpu.set_stream(300 + problem)
+    s32 = gpu.solve_points(b, np.array(pts), N, h, fk.FP32)
+    se = np.sqrt((st["phiphi_VR"] - st["phi_VR"] ** 2) / N)
+    assert np.all(np.abs(s32["phi_VR"] - st["phi_VR"]) < 0.5 * se), (s32["phi_VR"], st["phi_VR"], se)
 
 
 def test_point_solves_fp32_paired_with_fp64(gpu, fk):
