@@ -64,15 +64,22 @@ class ClockSampler:
         self.proc = None
         self.lines = []
 
-    def start(self):
+    def start(self, interval_ms=50, wait_s=5.0):
+        """Starts sampling every interval_ms and returns once the first sample
+        has arrived (nvidia-smi takes a while to start), so that the samples
+        cover the region timed after this call."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(interval_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < wait_s:
+            time.sleep(0.005)
 
     def _read(self):
         for line in self.proc.stdout:
