@@ -118,7 +118,12 @@ def robin(ctx, paths=4000, h=1e-4, n=24, mask=1 + 8, varphi=-0.5, rho=0.05):
     return out
 
 
-def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp64_fraction=0.05):
+def uneven_nodes(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0):
+    """The uneven batch: n_bvp disks of random radius 0.25..1 (FK_PROBLEM_DISK,
+    one registered BVP each, centres 2.5 apart on the x axis), nodes//n_bvp
+    uniform nodes in each, paths log-uniform in 1e3..1e5 (times scale), h
+    1e-3 or 5e-4 at random.  Returns a dict: bvp_ids (per node), xy, paths,
+    h, u (the exact solution), disks [(radius, cx, cy)] and disk (per node)."""
     rng = np.random.default_rng(seed)
     R = rng.uniform(0.25, 1.0, n_bvp)
     centers = np.stack([2.5 * np.arange(n_bvp), np.zeros(n_bvp)], axis=1)
@@ -132,7 +137,7 @@ def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp
         th = rng.uniform(0, 2 * np.pi, per)
         xy.append(np.stack([centers[k, 0] + r * np.cos(th), centers[k, 1] + r * np.sin(th)], axis=1))
         bvp_of += [k] * per
-    xy = np.concatenate(xy)
+    xy = np.ascontiguousarray(np.concatenate(xy))
     bvp_of = np.array(bvp_of)
     bvp_ids = np.array(ids, dtype=np.int32)[bvp_of]
     paths = np.exp(rng.uniform(np.log(1e3), np.log(1e5), len(xy)))
@@ -140,8 +145,17 @@ def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp
     h = rng.choice([1e-3, 5e-4], len(xy))
     xi = (xy[:, 0] - centers[bvp_of, 0]) / (2 * R[bvp_of]) + 0.5
     eta = (xy[:, 1] - centers[bvp_of, 1]) / (2 * R[bvp_of]) + 0.5
-    u = franke(xi, eta)
-    out = {"bvps": n_bvp, "nodes": len(xy), "total_paths": int(paths.sum()), "radius": R.tolist()}
+    return {"bvp_ids": bvp_ids, "xy": xy, "paths": paths, "h": h, "u": franke(xi, eta),
+            "disks": [(float(R[k]), float(centers[k, 0]), float(centers[k, 1])) for k in range(n_bvp)],
+            "disk": bvp_of, "rng": rng}
+
+
+def uneven(ctx, seed=2026, n_bvp=16, nodes=1 << 14, scale=1.0, autotune=True, fp64_fraction=0.05):
+    U = uneven_nodes(ctx, seed, n_bvp, nodes, scale)
+    bvp_ids, xy, paths, h, u, rng = U["bvp_ids"], U["xy"], U["paths"], U["h"], U["u"], U["rng"]
+    bvp_of = U["disk"]
+    R = [d[0] for d in U["disks"]]
+    out = {"bvps": n_bvp, "nodes": len(xy), "total_paths": int(paths.sum()), "radius": R}
     if autotune:
         bb, bc, tms = ctx.autotune_points(bvp_ids, xy, paths, h, fk.FP32, sample_fraction=0.05)
         out["autotune"] = {"block": bb, "chunk": bc, "sample_kernel_ms": tms}

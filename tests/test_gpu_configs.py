@@ -1,0 +1,106 @@
+"""Configs 1, 3 and 5 at their full shapes (config 2's shape is in
+test_gpu_config2.py): the CUDA path on the whole workload, checked through
+properties that hold at any size (FP32 paired with FP64 on the same Philox
+stream, errors against the exact solution within the step's bias and the
+Monte Carlo error, the adaptive assembly's own targets), and FP64 nodes of
+the same launch against the oracle path for path (rtol 1e-9).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+SEED = 20251203  # the gpu fixture's Philox seed
+
+
+def _franke(x, y):
+    from spac_gb300.workloads import franke
+    return franke(x, y)
+
+
+def test_config1_franke_grid(gpu, orc, fk):
+    """Config 1: Franke point solves on the 32 x 32 interior lattice of the
+    unit square, 1e4 paths, h = 1e-3, both precisions on one stream."""
+    g = np.arange(1, 33) / 33.0
+    xy = np.array([(x, y) for x in g for y in g])
+    u = _franke(xy[:, 0], xy[:, 1])
+    b = gpu.register_bvp(fk.FRANKE)
+    N, h = 10000, 1e-3
+    gpu.set_stream(401)
+    s64 = gpu.solve_points(b, xy, N, h, fk.FP64)
+    gpu.set_stream(401)
+    s32 = gpu.solve_points(b, xy, N, h, fk.FP32)
+    assert np.all(s64["n_paths"] == N) and np.all(s32["n_paths"] == N)
+    se = np.sqrt(np.maximum(s64["phiphi"] - s64["phi"] ** 2, 0) / N)
+    # paired paths: FP32 differs from FP64 only where rounding moves an exit
+    d = np.abs(s32["phi"] - s64["phi"]) / se
+    assert d.mean() < 0.25 and d.max() < 2.0, (d.mean(), d.max())
+    # error against exact u: the O(h) exit bias (~8e-3 RMS at h = 1e-3) and the Monte Carlo error
+    rms = np.sqrt(np.mean((s64["phi"] - u) ** 2))
+    assert rms < 0.015, rms
+    assert np.sqrt(np.mean(se ** 2)) < 0.006
+    # eight nodes of the same FP64 launch against the oracle (item = the node's index in the call)
+    s = orc.Session(orc.RNG_PHILOX, seed=SEED)
+    s.set_stream(401)
+    ob = orc.bvp(fk.FRANKE)
+    for i in np.random.default_rng(5).choice(len(xy), size=8, replace=False):
+        o = s.point_solve(ob, xy[i, 0], xy[i, 1], N, h, item=int(i))
+        for k in orc.STAT_NAMES:
+            assert np.isclose(s64[k][i], o[k], rtol=RTOL, atol=1e-12), (k, i, s64[k][i], o[k])
+
+
+def test_config3_uneven_disks(gpu, orc, fk):
+    """Config 3: 16 disks of random radius (one registered BVP each), 2^14
+    nodes, paths log-uniform in 1e3..1e5, h 1e-3 or 5e-4, in one persistent
+    FP32 launch; then an FP64 launch of a node sample at a quarter of their
+    paths, paired with FP32 on the same stream, and its cheapest nodes against
+    the oracle."""
+    from spac_gb300 import workloads as W
+    U = W.uneven_nodes(gpu)
+    ids, xy, paths, h, u = U["bvp_ids"], U["xy"], U["paths"], U["h"], U["u"]
+    assert len(xy) == 1 << 14 and len(set(ids.tolist())) == 16
+    st = gpu.solve_points_multi(ids, xy, paths, h, fk.FP32)
+    assert np.all(st["n_paths"] == paths)
+    err = st["phi"] - u
+    se = np.sqrt(np.maximum(st["phiphi"] - st["phi"] ** 2, 0) / paths)
+    rms = {hh: float(np.sqrt(np.mean(err[h == hh] ** 2))) for hh in (1e-3, 5e-4)}
+    assert rms[1e-3] < 0.02 and rms[5e-4] < 0.02, rms
+    # the exit bias is O(h): halving h lowers the error
+    assert rms[5e-4] < 0.85 * rms[1e-3], rms
+    assert np.all(np.abs(err) < 5 * se + 0.1)
+    # FP64 on a sample of the same nodes, paired with FP32 on one stream
+    sub = np.random.default_rng(7).choice(len(xy), size=256, replace=False)
+    p64 = np.maximum(1000, paths[sub] // 4).astype(np.uint32)
+    gpu.set_stream(402)
+    s64 = gpu.solve_points_multi(ids[sub], xy[sub], p64, h[sub], fk.FP64)
+    gpu.set_stream(402)
+    s32 = gpu.solve_points_multi(ids[sub], xy[sub], p64, h[sub], fk.FP32)
+    se64 = np.sqrt(np.maximum(s64["phiphi"] - s64["phi"] ** 2, 0) / p64)
+    d = np.abs(s32["phi"] - s64["phi"]) / se64
+    assert d.mean() < 0.25 and d.max() < 2.0, (d.mean(), d.max())
+    # the six cheapest nodes of the FP64 launch against the oracle
+    s = orc.Session(orc.RNG_PHILOX, seed=SEED)
+    s.set_stream(402)
+    for j in np.argsort(p64 * (1.0 / h[sub]))[:6]:
+        i = sub[j]
+        R, cx, cy = U["disks"][U["disk"][i]]
+        ob = orc.bvp(fk.DISK, dom=(R, cx, cy), dom_shape=orc.CIRCLE, prob=(cx, cy, R, 0))
+        o = s.point_solve(ob, xy[i, 0], xy[i, 1], int(p64[j]), float(h[i]), item=int(j))
+        for k in orc.STAT_NAMES:
+            assert np.isclose(s64[k][j], o[k], rtol=RTOL, atol=1e-12), (k, j, s64[k][j], o[k])
+
+
+def test_config5_adaptive_assembly(gpu, fk):
+    """Config 5: the 32 x 32 square-patch mesh (409k items, 179M nonzeros),
+    adaptive rounds to a standard error of 1e-4 per item with the learned
+    control variate and the plain fallback, full CSR G/B from the
+    device-resident sums (ε·spacing = 1, where the stencil is accurate)."""
+    from spac_gb300 import workloads as W
+    r = W.large(gpu, eps_spacing=1.0)
+    assert r["items"] == 408952 and r["nnz"] == 178904560
+    assert r["items_below_target"] > 0.9999 and r["se_max"] < 1.05e-4, (r["items_below_target"], r["se_max"])
+    assert r["cv_items"] > r["items"] // 2 and r["variance_reduction_median"] > 1.5
+    # the assembled rows against the exact solution: the exit bias at h = 2.5e-4 and the stencil's error
+    assert r["rms_row_residual"] < 0.05, r["rms_row_residual"]
+    assert r["rms_node_error_exact_exit"] < 0.01, r["rms_node_error_exact_exit"]
