@@ -334,6 +334,14 @@ int fk_mesh_set_disk_solver(fk_ctx* ctx, int mesh_id, int n_radial);
  * Returns FK_ERR_NOT_FOUND if the relative residual stays above 10 tol. */
 int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x, double tol,
                  int max_iter, int restart, int* iters, double* rel_resid);
+/* The same GMRES with a choice of right preconditioner: FK_PC_JACOBI
+ * (diag(A)^-1, as fk_gmres_csr) or FK_PC_ILU0 (incomplete LU on A's own
+ * sparsity pattern; each row's columns ascending with its diagonal present,
+ * as the assembled CSR patterns are, else FK_ERR_ARG; FK_ERR_NUMERIC on a
+ * zero pivot). */
+enum { FK_PC_JACOBI = 0, FK_PC_ILU0 = 1 };
+int fk_gmres_csr_pc(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x,
+                    double tol, int max_iter, int restart, int precond, int* iters, double* rel_resid);
 /* The reference's text formats (values in C++ general format, as its
  * setf(fixed, scientific) leaves them): dir/G.txt "row col value" (%.8g) and
  * dir/B.txt (%.8g) -- SistemaLineal::Escribe_GB_COO (Mesh/SistemaLineal.cpp:96-110);

@@ -1,8 +1,8 @@
 // Host-side consumers of the assembled system: a restarted GMRES to check the
 // assembled solution (the reference solves with METIS + MUMPS Schwarz GMRES
 // over MPI, Solvers/SistemaLinealSolverGMRES.hpp:157-597; here a plain
-// single-process GMRES(m) with Jacobi preconditioning), and the reference's
-// text formats for G, B and the node positions.
+// single-process GMRES(m) with a Jacobi or ILU(0) preconditioner), and the
+// reference's text formats for G, B and the node positions.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,20 +33,94 @@ std::string join(const char* dir, const char* name) {
   return d + name;
 }
 
+// Right preconditioners of the GMRES: apply(v, out) = M^-1 v.
+struct Precond {
+  int kind = FK_PC_JACOBI;
+  int n = 0;
+  const int* rp = nullptr;
+  const int* col = nullptr;
+  std::vector<double> dinv;  // Jacobi: diag(A)^-1
+  std::vector<double> lu;    // ILU(0): L (unit, below the diagonal) and U on A's pattern
+  std::vector<int> diag;     // position of each row's diagonal
+  std::vector<double> y;
+
+  // Jacobi: M = diag(A).  ILU(0): M = L U with L and U restricted to A's
+  // sparsity (the IKJ elimination dropping every fill-in entry); needs each
+  // row's columns ascending with the diagonal present.
+  int setup(int kind_, int n_, const int* rp_, const int* col_, const double* val) {
+    kind = kind_;
+    n = n_;
+    rp = rp_;
+    col = col_;
+    if (kind == FK_PC_JACOBI) {
+      dinv.assign(n, 1.0);
+      for (int i = 0; i < n; ++i)
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+          if (col[k] == i && val[k] != 0.0) dinv[i] = 1.0 / val[k];
+      return FK_OK;
+    }
+    if (kind != FK_PC_ILU0) return FK_ERR_ARG;
+    diag.assign(n, -1);
+    for (int i = 0; i < n; ++i)
+      for (int k = rp[i]; k < rp[i + 1]; ++k) {
+        if (k > rp[i] && col[k] <= col[k - 1]) return FK_ERR_ARG;  // columns not ascending
+        if (col[k] < 0 || col[k] >= n) return FK_ERR_ARG;
+        if (col[k] == i) diag[i] = k;
+      }
+    for (int i = 0; i < n; ++i)
+      if (diag[i] < 0) return FK_ERR_ARG;
+    lu.assign(val, val + rp[n]);
+    std::vector<int> pos(n, -1);
+    for (int i = 0; i < n; ++i) {
+      for (int k = rp[i]; k < rp[i + 1]; ++k) pos[col[k]] = k;
+      for (int k = rp[i]; k < diag[i]; ++k) {  // l_ik for the columns left of the diagonal, in order
+        const int c = col[k];
+        const double piv = lu[diag[c]];
+        if (piv == 0.0) return FK_ERR_NUMERIC;
+        const double l = lu[k] / piv;
+        lu[k] = l;
+        for (int q = diag[c] + 1; q < rp[c + 1]; ++q) {  // row i -= l_ik (U row c), on row i's pattern
+          const int p = pos[col[q]];
+          if (p >= 0) lu[p] -= l * lu[q];
+        }
+      }
+      for (int k = rp[i]; k < rp[i + 1]; ++k) pos[col[k]] = -1;
+      if (lu[diag[i]] == 0.0) return FK_ERR_NUMERIC;
+    }
+    y.assign(n, 0.0);
+    return FK_OK;
+  }
+
+  void apply(const double* v, double* out) {
+    if (kind == FK_PC_JACOBI) {
+      for (int i = 0; i < n; ++i) out[i] = dinv[i] * v[i];
+      return;
+    }
+    for (int i = 0; i < n; ++i) {  // L y = v
+      double s = v[i];
+      for (int k = rp[i]; k < diag[i]; ++k) s -= lu[k] * y[col[k]];
+      y[i] = s;
+    }
+    for (int i = n - 1; i >= 0; --i) {  // U out = y
+      double s = y[i];
+      for (int k = diag[i] + 1; k < rp[i + 1]; ++k) s -= lu[k] * out[col[k]];
+      out[i] = s / lu[diag[i]];
+    }
+  }
+};
+
 }  // namespace
 
 extern "C" {
 
-int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x, double tol,
-                 int max_iter, int restart, int* iters, double* rel_resid) {
+int fk_gmres_csr_pc(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x,
+                    double tol, int max_iter, int restart, int precond, int* iters, double* rel_resid) {
   if (n < 1 || !rowptr || !col || !val || !b || !x || restart < 1 || max_iter < 1 || !(tol > 0)) return FK_ERR_ARG;
-  // Jacobi (right) preconditioner: M^{-1} = diag(A)^{-1}
-  std::vector<double> dinv(n, 1.0);
-  for (int i = 0; i < n; ++i)
-    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
-      if (col[k] == i && val[k] != 0.0) dinv[i] = 1.0 / val[k];
+  Precond M;
+  int rc = M.setup(precond, n, rowptr, col, val);
+  if (rc) return rc;
   const int m = restart;
-  std::vector<double> r(n), w(n), z(n), bnrm_v(b, b + n);
+  std::vector<double> r(n), w(n), z(n), t(n), bnrm_v(b, b + n);
   const double bnrm = std::sqrt(dot(bnrm_v, bnrm_v));
   const double ref = bnrm > 0 ? bnrm : 1.0;
   std::vector<std::vector<double>> V(m + 1, std::vector<double>(n));
@@ -64,7 +138,7 @@ int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, co
     g[0] = beta;
     int j = 0;
     for (; j < m && it < max_iter; ++j, ++it) {
-      for (int i = 0; i < n; ++i) z[i] = dinv[i] * V[j][i];
+      M.apply(V[j].data(), z.data());
       spmv(n, rowptr, col, val, z.data(), w.data());
       for (int k = 0; k <= j; ++k) {  // modified Gram-Schmidt
         const double hk = dot(w, V[k]);
@@ -76,9 +150,9 @@ int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, co
       if (hn > 0)
         for (int i = 0; i < n; ++i) V[j + 1][i] = w[i] / hn;
       for (int k = 0; k < j; ++k) {  // Givens rotations
-        const double t = cs[k] * H[k * m + j] + sn[k] * H[(k + 1) * m + j];
+        const double tk = cs[k] * H[k * m + j] + sn[k] * H[(k + 1) * m + j];
         H[(k + 1) * m + j] = -sn[k] * H[k * m + j] + cs[k] * H[(k + 1) * m + j];
-        H[k * m + j] = t;
+        H[k * m + j] = tk;
       }
       const double a = H[j * m + j], c = H[(j + 1) * m + j];
       const double d = std::sqrt(a * a + c * c);
@@ -101,8 +175,10 @@ int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, co
     for (int i = 0; i < n; ++i) {
       double s = 0.0;
       for (int k = 0; k < j; ++k) s += V[k][i] * y[k];
-      x[i] += dinv[i] * s;
+      t[i] = s;
     }
+    M.apply(t.data(), z.data());
+    for (int i = 0; i < n; ++i) x[i] += z[i];
     if (res <= tol) break;
   }
   // true residual
@@ -112,6 +188,11 @@ int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, co
   if (iters) *iters = it;
   if (rel_resid) *rel_resid = res;
   return res <= tol * 10 ? FK_OK : FK_ERR_NOT_FOUND;
+}
+
+int fk_gmres_csr(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x, double tol,
+                 int max_iter, int restart, int* iters, double* rel_resid) {
+  return fk_gmres_csr_pc(n, rowptr, col, val, b, x, tol, max_iter, restart, FK_PC_JACOBI, iters, rel_resid);
 }
 
 int fk_write_gb_coo(const char* dir, int n_rows, const int* rowptr, const int* col, const double* val, const double* B) {

@@ -117,6 +117,8 @@ _SIGS = {
     "fk_mlp_get_table": (C.c_int, [C.c_void_p, C.c_int, _ip, _fp]),
     "fk_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _fp]),
     "fk_gmres_csr": (C.c_int, [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, _ip, _dp]),
+    "fk_gmres_csr_pc": (C.c_int, [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_int, _ip,
+                                  _dp]),
     "fk_write_gb_coo": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _dp, _dp]),
     "fk_write_gb_csr": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _dp, _dp]),
     "fk_read_gb_coo": (C.c_int, [C.c_char_p, _ip, _ip, _ip, _ip, _dp]),
@@ -523,8 +525,12 @@ class FeynmanKacSolverGPU:
 
 
 # ---- host-side consumers of the assembled system ------------------------------
-def gmres(rowptr, col, val, b, x0=None, tol=1e-10, max_iter=2000, restart=50):
-    """fk_gmres_csr: returns (x, iterations, relative residual, status)."""
+PC_JACOBI, PC_ILU0 = 0, 1
+
+
+def gmres(rowptr, col, val, b, x0=None, tol=1e-10, max_iter=2000, restart=50, precond=None):
+    """fk_gmres_csr (precond None: Jacobi) or fk_gmres_csr_pc (PC_JACOBI,
+    PC_ILU0): returns (x, iterations, relative residual, status)."""
     L = load()
     rp, prp = _i(rowptr)
     cl, pcl = _i(col)
@@ -532,8 +538,12 @@ def gmres(rowptr, col, val, b, x0=None, tol=1e-10, max_iter=2000, restart=50):
     bb, pb = _d(b)
     x = np.array(np.zeros(len(bb)) if x0 is None else x0, dtype=np.float64)
     it, res = C.c_int(), C.c_double()
-    rc = L.fk_gmres_csr(len(bb), prp, pcl, pv, pb, x.ctypes.data_as(_dp), tol, max_iter, restart, C.byref(it),
-                        C.byref(res))
+    if precond is None:
+        rc = L.fk_gmres_csr(len(bb), prp, pcl, pv, pb, x.ctypes.data_as(_dp), tol, max_iter, restart, C.byref(it),
+                            C.byref(res))
+    else:
+        rc = L.fk_gmres_csr_pc(len(bb), prp, pcl, pv, pb, x.ctypes.data_as(_dp), tol, max_iter, restart, precond,
+                               C.byref(it), C.byref(res))
     return x, it.value, res.value, rc
 
 

@@ -53,3 +53,44 @@ def test_gmres_solves_assembled_system(fk):
     for i in range(n):
         M[i, A["col"][A["rowptr"][i]:A["rowptr"][i + 1]]] = A["val"][A["rowptr"][i]:A["rowptr"][i + 1]]
     assert np.allclose(M @ x, A["B"], atol=1e-8 * np.abs(A["B"]).max())
+
+
+def _csr(M):
+    rp, col, val = [0], [], []
+    for i in range(M.shape[0]):
+        nz = np.flatnonzero(M[i])
+        col += nz.tolist()
+        val += M[i, nz].tolist()
+        rp.append(len(col))
+    return np.array(rp, dtype=np.int32), np.array(col, dtype=np.int32), np.array(val)
+
+
+def test_gmres_ilu0(fk):
+    """fk_gmres_csr_pc with ILU(0): exact on a tridiagonal matrix (its LU has
+    no fill-in), the Jacobi solution in fewer iterations on an assembled
+    system, and the patterns it cannot use refused."""
+    rng = np.random.default_rng(2)
+    n = 200
+    T = np.diag(4.0 + rng.uniform(0, 1, n)) + np.diag(rng.uniform(-1, 1, n - 1), 1) + \
+        np.diag(rng.uniform(-1, 1, n - 1), -1)
+    b = rng.standard_normal(n)
+    x, it, res, rc = fk.gmres(*_csr(T), b, tol=1e-12, precond=fk.PC_ILU0)
+    assert rc == 0 and it <= 2 and np.allclose(T @ x, b, atol=1e-10), (rc, it, res)
+    A = _assembly()
+    args = (A["rowptr"], A["col"], A["val"], A["B"])
+    xj, itj, rj, rcj = fk.gmres(*args, tol=1e-11, max_iter=4000, restart=60, precond=fk.PC_JACOBI)
+    xi, iti, ri, rci = fk.gmres(*args, tol=1e-11, max_iter=4000, restart=60, precond=fk.PC_ILU0)
+    assert rcj == 0 and rci == 0 and ri < 1e-10
+    assert np.allclose(xi, xj, atol=1e-8 * np.abs(xj).max())
+    assert iti < itj, (iti, itj)
+    # Jacobi through fk_gmres_csr_pc is fk_gmres_csr
+    x0, it0, _, _ = fk.gmres(*args, tol=1e-11, max_iter=4000, restart=60)
+    assert it0 == itj and np.array_equal(x0, xj)
+    # a row without its diagonal, or columns out of order: FK_ERR_ARG
+    rp, col, val = _csr(T)
+    bad = col.copy()
+    bad[rp[5]:rp[6]] = bad[rp[5]:rp[6]][::-1]
+    assert fk.gmres(rp, bad, val, b, precond=fk.PC_ILU0)[3] == fk.FK_ERR_ARG
+    T2 = T.copy()
+    T2[7, 7] = 0.0
+    assert fk.gmres(*_csr(T2), b, precond=fk.PC_ILU0)[3] == fk.FK_ERR_ARG
