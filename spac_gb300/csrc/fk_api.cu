@@ -155,7 +155,8 @@ struct fk_ctx {
   fk::DiskBufs w_disk;
   fk::HBuf h_items, h_chunks, h_goff, h_stats, h_queue;  // pinned staging of the per-call transfers
   std::vector<fk::ItemDev> tmp_items;            // host scratch kept across calls
-  std::vector<fk::ChunkDev> tmp_chunks;
+  std::vector<fk::ChunkDev> tmp_chunks, tmp_chunks2;
+  std::vector<unsigned> tmp_count;
 };
 
 namespace {
@@ -614,9 +615,25 @@ int run_items(fk_ctx* ctx, int bvp_id, int precision, std::vector<fk::ItemDev>& 
   bool uneven = false;
   for (size_t c = 1; c < chunks.size() && !uneven; ++c)
     uneven = (chunks[c].p1 - chunks[c].p0) != (chunks[0].p1 - chunks[0].p0);
-  if (uneven)
-    std::stable_sort(chunks.begin(), chunks.end(),
-                     [](const fk::ChunkDev& a, const fk::ChunkDev& b) { return (a.p1 - a.p0) > (b.p1 - b.p0); });
+  if (uneven) {
+    // stable, by descending length: a counting sort (lengths are at most the
+    // chunk size), the order std::stable_sort gives, in linear time
+    unsigned maxlen = 0;
+    for (const fk::ChunkDev& c : chunks) maxlen = std::max(maxlen, c.p1 - c.p0);
+    if (maxlen <= (1u << 16)) {
+      std::vector<unsigned>& start = ctx->tmp_count;
+      start.assign(maxlen + 2, 0u);
+      for (const fk::ChunkDev& c : chunks) ++start[maxlen - (c.p1 - c.p0) + 1];
+      for (unsigned l = 1; l <= maxlen + 1; ++l) start[l] += start[l - 1];
+      std::vector<fk::ChunkDev>& sorted = ctx->tmp_chunks2;
+      sorted.resize(chunks.size());
+      for (const fk::ChunkDev& c : chunks) sorted[start[maxlen - (c.p1 - c.p0)]++] = c;
+      chunks.swap(sorted);
+    } else {
+      std::stable_sort(chunks.begin(), chunks.end(),
+                       [](const fk::ChunkDev& a, const fk::ChunkDev& b) { return (a.p1 - a.p0) > (b.p1 - b.p0); });
+    }
+  }
   FK_CUDA(fk::upload_pinned(ctx->w_items, ctx->h_items, it, s));
   FK_CUDA(fk::upload_pinned(ctx->w_chunks, ctx->h_chunks, chunks, s));
   FK_CUDA(ctx->w_stats.ensure(std::max<size_t>(static_cast<size_t>(n) * fk::kNumStats * sizeof(double), 16)));
@@ -941,21 +958,28 @@ int fk_register_bvp(fk_ctx* ctx, const fk_bvp_desc* d, int* id) {
   return FK_OK;
 }
 
-static void stats_to_struct(const double* s, fk_stats* o) {
-  o->phi = s[0]; o->phiphi = s[1]; o->phi_VR = s[2]; o->phiphi_VR = s[3]; o->xi = s[4]; o->xixi = s[5];
-  o->xiphi = s[6]; o->APL = s[7]; o->RNGC = s[8]; o->B = s[9]; o->n_paths = s[10]; o->n_domain_exits = s[11];
-  o->n_capped = s[12]; o->xi_mean = s[13]; o->xi_sq_mean = s[14]; o->mean_steps = s[15];
-}
+// The device's per-item statistics record is fk_stats itself (16 doubles in
+// the struct's field order), so it is copied as it is.
+static_assert(sizeof(fk_stats) == 16 * sizeof(double), "fk_stats is the device's per-item record");
 
-// Per-item statistics (device, fk_stats layout) into out[n] through the
-// pinned staging buffer; drains the context stream.
+// Per-item statistics (device, fk_stats layout) into out[n]: straight into a
+// page-locked out, else through the pinned staging buffer; drains the
+// context stream.
 static int read_stats(fk_ctx* ctx, const double* d_stats, int n, fk_stats* out) {
-  const size_t bytes = static_cast<size_t>(n) * 16 * sizeof(double);
+  const size_t bytes = static_cast<size_t>(n) * sizeof(fk_stats);
+  cudaPointerAttributes at;
+  bool pinned = false;
+  if (cudaPointerGetAttributes(&at, out) == cudaSuccess) pinned = at.type == cudaMemoryTypeHost;
+  else cudaGetLastError();
+  if (pinned) {
+    FK_CUDA(cudaMemcpyAsync(out, d_stats, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    FK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FK_OK;
+  }
   FK_CUDA(ctx->h_stats.ensure(std::max<size_t>(bytes, 16)));
   FK_CUDA(cudaMemcpyAsync(ctx->h_stats.p, d_stats, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   FK_CUDA(cudaStreamSynchronize(ctx->stream));
-  const double* st = static_cast<const double*>(ctx->h_stats.p);
-  for (int i = 0; i < n; ++i) stats_to_struct(st + static_cast<size_t>(i) * 16, &out[i]);
+  std::memcpy(out, ctx->h_stats.p, bytes);
   return FK_OK;
 }
 

@@ -496,7 +496,9 @@ class Context:
                                           B.ctypes.data_as(_dp) if csr else None,
                                           G.ctypes.data_as(_dp) if G is not None else None,
                                           iB.ctypes.data_as(_dp) if items else None, st if items else None), allow)
-        return dict(val=val, B=B, item_G=G, item_B=iB, item_stats=stats_array(st) if items else None)
+        # (columns over the statistics buffer, which the arrays keep alive)
+        cols = _stats_cols(np.frombuffer(st, dtype=np.float64).reshape(-1, len(STAT_FIELDS))) if items else None
+        return dict(val=val, B=B, item_G=G, item_B=iB, item_stats=cols)
 
 
 class FeynmanKacSolverGPU:

@@ -47,16 +47,18 @@ def franke(x, y):
             0.2 * np.exp(-((9 * x - 4) ** 2) - (9 * y - 7) ** 2))
 
 
-_PINNED = []
+_PINNED = {}
 
 
-def _pinned(n):
+def _pinned(n, what):
     """A page-locked float64 host array of n entries (torch's pinned
-    allocator; kept alive for the process)."""
+    allocator) for the output `what`, one per (output, size), kept for the
+    process as a caller keeps its output buffers across calls."""
     import torch
-    t = torch.empty(max(int(n), 1), dtype=torch.float64, pin_memory=True)
-    _PINNED.append(t)
-    return t.numpy()[:n]
+    key = (what, max(int(n), 1))
+    if key not in _PINNED:
+        _PINNED[key] = torch.empty(key[1], dtype=torch.float64, pin_memory=True)
+    return _PINNED[key].numpy()
 
 
 def _sync_time(fn):
@@ -268,8 +270,8 @@ def large(ctx, n_sub=32, nodes_per_side=63, h=2.5e-4, se_target=1e-4, pilot_path
     b_plain = ctx.register_bvp(fk.FRANKE)
     # the caller's output buffers (page-locked, as a caller keeps them):
     # the CSR values (1.4 GB at 32 x 32), B, per-item B and statistics
-    outs = {"val": _pinned(info["nnz"]), "B": _pinned(info["n_rows"]), "item_B": _pinned(n)}
-    outs["item_stats"] = (fk.Stats * n).from_address(_pinned(n * len(fk.STAT_FIELDS)).ctypes.data)
+    outs = {"val": _pinned(info["nnz"], "val"), "B": _pinned(info["n_rows"], "B"), "item_B": _pinned(n, "item_B")}
+    outs["item_stats"] = (fk.Stats * n).from_address(_pinned(n * len(fk.STAT_FIELDS), "item_stats").ctypes.data)
     # the mesh's device side (stencil inverses, window tables) and the rounds'
     # buffers are set up once per mesh: counted with the mesh, not the assembly
     _, t_dev = _sync_time(lambda: ctx.assembly_begin(mesh))
