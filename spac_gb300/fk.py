@@ -165,10 +165,6 @@ def _u(a):
     return a, a.ctypes.data_as(_up)
 
 
-def stats_dict(s):
-    return {k: getattr(s, k) for k in STAT_FIELDS}
-
-
 def stats_array(arr):
     """fk_stats array -> dict of per-item numpy columns (a copy of the buffer, no per-item Python work)."""
     n = len(arr)
