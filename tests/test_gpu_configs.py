@@ -104,3 +104,35 @@ def test_config5_adaptive_assembly(gpu, fk):
     # the assembled rows against the exact solution: the exit bias at h = 2.5e-4 and the stencil's error
     assert r["rms_row_residual"] < 0.05, r["rms_row_residual"]
     assert r["rms_node_error_exact_exit"] < 0.01, r["rms_node_error_exact_exit"]
+
+
+def test_h_sweep_franke(gpu, fk):
+    """The reference's h-sweep check (the commented known-answer block of
+    main_test_serial.cpp:90-100): Franke point solves against exact u as h
+    shrinks, with the standard error.  The exit rule's bias is first order:
+    on a GB300 the error at these points stayed within 19-22 h (h = 4e-3 ..
+    2.5e-4, FP32 and FP64 alike) and halved with every halving of h.  The
+    exact-gradient control variate cuts the standard error, not the bias, and
+    cuts it more as h falls."""
+    pts = np.array([[0.3, 0.4], [0.7, 0.2], [0.5, 0.8], [0.15, 0.15]])
+    u = _franke(pts[:, 0], pts[:, 1])
+    b = gpu.register_bvp(fk.FRANKE)
+    b_cv = gpu.register_bvp(fk.FRANKE, cv=fk.CV_EXACT)
+    N = 1 << 20
+    rms, vr = [], []
+    for h in (4e-3, 2e-3, 1e-3, 5e-4):
+        st = gpu.solve_points(b, pts, N, h, fk.FP32)
+        se = np.sqrt(np.maximum(st["phiphi"] - st["phi"] ** 2, 0) / N)
+        err = st["phi"] - u
+        assert np.all(np.abs(err) < 25 * h + 4 * se), (h, err, se)
+        rms.append(float(np.sqrt(np.mean(err ** 2))))
+        sc = gpu.solve_points(b_cv, pts, N, h, fk.FP32)
+        se_cv = np.sqrt(np.maximum(sc["phiphi_VR"] - sc["phi_VR"] ** 2, 0) / N)
+        assert np.all(se_cv < 0.75 * se)
+        vr.append(float(np.mean((se / se_cv) ** 2)))
+        assert np.all(np.abs(sc["phi_VR"] - st["phi"]) < 4 * se + 2 * se_cv)  # another stream, the same bias
+    ratio = np.array(rms[1:]) / np.array(rms[:-1])
+    assert np.all((ratio > 0.3) & (ratio < 0.7)), (rms, ratio)  # first order: halving h halves the error
+    # what the control term leaves is the exit's own O(sqrt(h)) jump onto the
+    # boundary, so its variance reduction grows as h falls
+    assert vr[-1] > 2 * vr[0], vr
